@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""Momentum-loop integration benchmark on GB300.
+
+Workload (default): C2, the finite-T 3+1D loop -- 384 integrals (T in {0.05, 0.2, 1.0} x 128
+external momenta), each 129 Matsubara modes x 64 q x 32 cos = 264192 integrand points, one
+seeded 64x128 FP32 dressing table Z(mode, |q|).
+
+Arms:
+  ours (default)      one step = one batched, fused FP32-compensated evaluation of the whole
+                      workload (libgbint, inputs resident in HBM) -> `value` (integrals/s);
+                      `e2e` = the same through the public API with the dressing table uploaded
+                      from pinned host memory and the results read back every step.  Beside it:
+                      the plain per-integral FP64 GPU path (the reference's execution pattern,
+                      the 20x denominator), the fused FP64 path, p50/p99 latencies, the roofline
+                      against this GPU's measured FP32/MUFU peaks and the CPU baseline (the FP64
+                      oracle on all host cores).
+  --impl reference    the reference's CPU integrator restated (the FP64 oracle port; DiFfRG's
+                      own build needs deal.II/TBB/GSL/RMM, absent here) on all host cores.
+
+Multi-GPU: replicas (integrals are independent; no data-path collective) -- every rank runs the
+full workload on its GPU, time = max over ranks, value = all ranks' integrals / time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "integrals/s and p99 request latency, batched FP32-comp vs plain FP64, 1 GPU"
+UNIT = "integrals/s"
+# algorithmic work per integrand point of the FTLOOP mixed factor (per sign of the Matsubara
+# frequency, as the reference counts points): F basic FP32 flops (FMA = 2), S special functions
+FLOPS_PER_POINT = 18
+SPECIALS_PER_POINT = 4
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="C2", choices=["C1", "C2", "C3", "C5"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(w, W, reps=2):
+    """The FP64 oracle (C++ restatement of the reference CPU integrators) on all host cores."""
+    from oracle import oracle as O
+
+    O.build()
+    threads = os.cpu_count() or 1
+    W.oracle_values(w, O, threads=threads, subset=np.arange(4))  # warm caches
+    n = len(w["p"]) if "p" in w else len(w["P"])
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ref = W.oracle_values(w, O, threads=threads)
+    dt = (time.perf_counter() - t0) / reps
+    return ref, {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                 "sample": "the whole %s workload (%d integrals), %d repetitions, FP64 OpenMP over integrals"
+                           % (w["name"], n, reps)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from diffrg_gb300 import workloads as W
+    from oracle import oracle as O
+
+    O.build()
+    w = getattr(W, args.workload.lower())()
+    threads = os.cpu_count() or 1
+    n = len(w["p"]) if "p" in w else len(w["P"])
+    # each step: a bounded sample of the workload (every 4th integral)
+    sub = np.arange(0, n, 4)
+    for _ in range(max(1, args.warmup)):
+        W.oracle_values(w, O, threads=threads, subset=sub[:8])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        W.oracle_values(w, O, threads=threads, subset=sub)
+    dt = time.perf_counter() - t0
+    value = sub.size * args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "%s finite-T 3+1D loop" % args.workload if args.workload == "C2" else args.workload,
+                       "integrals_per_step": int(sub.size), "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d of %d %s integrals per step (every 4th), FP64 restatement of the "
+                                       "reference CPU integrators, OpenMP over integrals" % (sub.size, n, args.workload)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_env()
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    from diffrg_gb300 import build as B
+    from diffrg_gb300 import capi
+    from diffrg_gb300 import workloads as W
+    from diffrg_gb300.engine import Context
+
+    B.build()
+    import ctypes as C
+
+    w = getattr(W, args.workload.lower())()
+    items, tabs = W.engine_items(w)
+    n_int = len(items)
+    ctx = Context(local)
+    L = capi.lib()
+    T = [ctx.table(s, d) for s, d in tabs]
+    b32 = ctx.batch(items, T, "fp32c")
+    b64 = ctx.batch(items, T, "fp64")
+    points = b32.points
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
+    launches_per_step = len([1 for _ in range(1)]) + 1  # hoisted-factor kernel + one fused kernel
+
+    def timed(batch, steps, warm):
+        for _ in range(warm):
+            batch.run(stream=sh)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for i in range(steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            batch.run(stream=sh)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        per = [a.elapsed_time(b) for a, b in ev]
+        return per
+
+    # ---------------------------------------------------------------- main (device-resident) timing
+    sampler = ClockSampler(local)
+    sampler.start()
+    per32 = timed(b32, args.steps, args.warmup)
+    clocks = sampler.stop()
+    tot = sum(per32) / 1e3
+    if world > 1:
+        t = torch.tensor([tot], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot = float(t.item())
+    value = n_int * args.steps * world / tot
+    res32 = b32.results(stream=sh)
+
+    # ---------------------------------------------------------------- e2e through the public API
+    # every step: dressing table H2D from pinned host memory (RG-step update), fused run, results D2H
+    pinned = [torch.from_numpy(np.ascontiguousarray(d, dtype=np.float32)).pin_memory() for _, d in tabs]
+    host_out = torch.zeros(n_int, dtype=torch.float64).pin_memory()
+    h2d = sum(p.numel() * 4 for p in pinned)
+    d2h = n_int * 8
+
+    def e2e_step():
+        for t, p in zip(T, pinned):
+            ctx.check(L.gb_table_update(ctx.h, t.h, C.cast(p.data_ptr(), C.POINTER(C.c_float)), C.c_void_p(sh)))
+        ctx.check(L.gb_batch_run(ctx.h, b32.h, None, C.c_void_p(sh)))
+        ctx.check(L.gb_batch_results(ctx.h, b32.h, C.cast(host_out.data_ptr(), C.POINTER(C.c_double)), C.c_void_p(sh)))
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    lat = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        e2e_step()
+        lat.append(time.perf_counter() - s0)
+    e2e_total = sum(lat)
+    e2e_value = n_int * args.steps * world / e2e_total
+
+    # ---------------------------------------------------------------- fused FP64 and plain FP64 paths
+    per64 = timed(b64, max(3, args.steps // 4), 2)
+    fused64 = n_int / (statistics.mean(per64) / 1e3)
+    res64 = b64.results(stream=sh)
+    plain = None
+    if not args.no_plain:
+        b64.run_plain(16)  # warm-up (allocations, CUB)
+        reps = 2
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            resp = b64.run_plain(16)
+        plain_dt = (time.perf_counter() - t0) / reps
+        plain = {"value": n_int / plain_dt, "unit": UNIT, "ms_per_step": plain_dt * 1e3,
+                 "pattern": "one launch per integral writing one FP64 value per point, CUB DeviceReduce, "
+                            "D2H + stream sync per integral, 16 pooled streams"}
+
+    # ---------------------------------------------------------------- single-integral request latency
+    single = ctx.batch(items[:1], T, "fp32c")
+    one = np.zeros(1)
+    for _ in range(5):
+        single.get()
+    sl = []
+    for _ in range(50):
+        s0 = time.perf_counter()
+        single.get()
+        sl.append(time.perf_counter() - s0)
+    single.close()
+
+    # ---------------------------------------------------------------- roofline
+    fp32_peak, mufu_peak, fp64_peak = ctx.measure_peaks()
+    pts_per_s = points / (statistics.mean(per32) / 1e3)
+    fp32_achieved = FLOPS_PER_POINT * pts_per_s / 1e12
+    xu_achieved = SPECIALS_PER_POINT * pts_per_s / 1e9
+    frac32 = fp32_achieved / fp32_peak
+    fracxu = xu_achieved / mufu_peak
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    roof = {"bound": "xu" if fracxu >= frac32 else "fp32",
+            "achieved": xu_achieved if fracxu >= frac32 else fp32_achieved,
+            "peak": mufu_peak if fracxu >= frac32 else fp32_peak,
+            "unit": "Gop/s" if fracxu >= frac32 else "TFLOP/s",
+            "frac": max(frac32, fracxu), "traffic": traffic,
+            "fp32": {"achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": frac32},
+            "xu": {"achieved": xu_achieved, "peak": mufu_peak, "unit": "Gop/s", "frac": fracxu},
+            "per_point": {"F": FLOPS_PER_POINT, "S": SPECIALS_PER_POINT},
+            "points_per_launch": points,
+            "peak_source": "measured in this run by the library's FFMA/MUFU probes (gb_measure_peaks); "
+                           "MEASURED_PEAKS.json lists only HBM and BF16",
+            "fp64_peak_tflops": fp64_peak}
+
+    # ---------------------------------------------------------------- accuracy + CPU baseline
+    cpu = None
+    err = None
+    if rank == 0 and not args.no_cpu:
+        ref, cpu = cpu_baseline(w, W)
+        e = np.abs(res32 - ref) / np.abs(ref)
+        e64 = np.abs(res64 - ref) / np.abs(ref)
+        err = {"fp32c_max_rel_err_vs_oracle": float(e.max()), "fp32c_median_rel_err": float(np.median(e)),
+               "fp64_fused_max_rel_err_vs_oracle": float(e64.max())}
+        if plain is not None:
+            err["plain_fp64_max_rel_err_vs_oracle"] = float((np.abs(resp - ref) / np.abs(ref)).max())
+
+    lat_ms = sorted(x * 1e3 for x in lat)
+    sl_ms = sorted(x * 1e3 for x in sl)
+
+    def pct(v, q):
+        return v[min(len(v) - 1, int(round(q * (len(v) - 1))))]
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": statistics.mean(per32), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (compensated) + f64 reduction",
+            "data": "synthetic (seeded tables and momenta, no dataset)",
+            "config": {"workload": "C2 finite-T 3+1D loop: 3 T x 128 p, n=-64..64 x 64 q x 32 cos"
+                       if args.workload == "C2" else args.workload,
+                       "integrals_per_step": n_int, "points_per_step": points,
+                       "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clocks,
+            "roofline": roof,
+            "plain_fp64_gpu": plain,
+            "fp32c_over_plain_fp64": (value / world) / plain["value"] if plain else None,
+            "fused_fp64_gpu": {"value": fused64, "unit": UNIT},
+            "latency_ms": {"batch_e2e_p50": pct(lat_ms, 0.5), "batch_e2e_p99": pct(lat_ms, 0.99),
+                           "single_integral_get_p50": pct(sl_ms, 0.5), "single_integral_get_p99": pct(sl_ms, 0.99)},
+            "accuracy": err,
+            "cpu_baseline": cpu}
+    if rank == 0:
+        print(json.dumps(line))
+    b32.close()
+    b64.close()
+    for t in T:
+        t.close()
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

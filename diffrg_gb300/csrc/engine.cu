@@ -1,0 +1,1227 @@
+// engine.cu -- C ABI of libgbint: context, QuadratureProvider, dressing tables, batch planning
+// and execution, and the reference-pattern FP64 path.
+#include "engine.hh"
+#include "kernels.hh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <set>
+
+#include <cub/device/device_reduce.cuh>
+
+using namespace gbint;
+
+namespace gbint
+{
+  int set_error(gb_ctx *ctx, int code, const std::string &msg)
+  {
+    if (ctx) ctx->last_error = msg;
+    return code;
+  }
+  int cuda_fail(gb_ctx *ctx, cudaError_t e, const char *what)
+  {
+    return set_error(ctx, GB_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+} // namespace gbint
+
+#define GB_CUDA(call)                                  \
+  do {                                                 \
+    cudaError_t e__ = (call);                          \
+    if (e__ != cudaSuccess) return cuda_fail(ctx, e__, #call); \
+  } while (0)
+
+namespace
+{
+  constexpr double kPi = 3.14159265358979323846;
+  constexpr int kPoolCapacity = 1 << 21;  // nodes (about 112 MB of device memory)
+  constexpr int kPoolStreams = 16;
+
+  double S_d(int d) { return 2.0 * std::pow(kPi, d / 2.0) / std::tgamma(d / 2.0); }
+  double powi(double x, int n)
+  {
+    if (n < 0) return 1.0 / powi(x, -n);
+    double r = 1;
+    for (int i = 0; i < n; ++i) r *= x;
+    return r;
+  }
+
+  dev::AxisDev make_axis(int n, int log, double lo, double hi)
+  {
+    dev::AxisDev a{};
+    a.n = n;
+    a.log = log;
+    if (n < 2) {
+      a.scale64 = 0;
+      a.shift64 = 0;
+    } else if (log) {
+      a.scale64 = (n - 1) / std::log2(hi / lo);
+      a.shift64 = -std::log2(lo) * a.scale64;
+    } else {
+      a.scale64 = (n - 1) / (hi - lo);
+      a.shift64 = -lo * a.scale64;
+    }
+    a.scale = dev::df_from(a.scale64);
+    a.shift = dev::df_from(a.shift64);
+    return a;
+  }
+
+  const GLRule &gl_host(gb_ctx *ctx, int n)
+  {
+    auto it = ctx->gl.find(n);
+    if (it != ctx->gl.end()) return it->second;
+    GLRule &r = ctx->gl[n];
+    gl_rule01(n, r.x, r.w);
+    return r;
+  }
+
+  // Matsubara cache with the reference's relative 1e-6 match on T and E
+  // (MatsubaraStorage::find_T_d / find_E_d, quadrature_provider.cu:12-58)
+  MatsEntry &mats_host(gb_ctx *ctx, double T, double E)
+  {
+    auto close = [](double a, double b) { return std::fabs(a - b) <= 1e-6 * std::fabs(b) || a == b; };
+    for (auto &m : ctx->mats)
+      if (close(T, m->T) && close(E, m->E)) return *m;
+    auto e = std::make_unique<MatsEntry>();
+    e->T = T;
+    e->E = E;
+    e->rule = matsubara_rule(T, E, 2, ctx->mats_min, 128, ctx->mats_vacuum, ctx->mats_add);
+    ctx->mats.push_back(std::move(e));
+    return *ctx->mats.back();
+  }
+
+  // ------------------------------------------------------------------ axes
+  enum AxisKind : int {
+    AK_XRAD = 1,   // q = k sqrt(t x_ext), w = w_t x_ext C q^pw
+    AK_QRAD = 2,   // q = qmax t, w = qmax w_t C q^pw
+    AK_COS = 3,    // c = 2(t - 1/2), w = 2 w_t C [sqrt(1-c^2)]
+    AK_PHI = 4,    // phi = 2 pi t, w = 2 pi w_t C
+    AK_CART = 5,   // v = qmin + ext t, w = ext w_t C
+    AK_PQ0 = 6,    // q0 = s t ext, w = w_t ext, all nodes +-
+    AK_MATS = 7,   // [0 (w = T)] + Monien nodes, +- from 1
+    AK_FTX0 = 8,   // explicit sum (w = T) + log-mapped tail
+    AK_MODES = 9,  // w_m = 2 pi T m, m = 0..M, w = C, +- from 1
+    AK_ONE = 10    // single node 0 with weight C
+  };
+
+  int pool_append(gb_ctx *ctx, const HostAxis &h, AxisRef &ref)
+  {
+    const int n = (int)h.v.size();
+    if (ctx->pool.used + n > ctx->pool.capacity) return set_error(ctx, GB_ENOMEM, "node pool exhausted");
+    std::vector<NodeRec> rec(n);
+    for (int i = 0; i < n; ++i) {
+      const dev::df v = dev::df_from(h.v[i]), w = dev::df_from(h.w[i]), a = dev::df_from(h.a[i]),
+                    aw = dev::df_from(h.w[i] * h.a[i]);
+      rec[i] = NodeRec{v.hi, v.lo, w.hi, w.lo, a.hi, a.lo, aw.hi, aw.lo};
+    }
+    const int off = ctx->pool.used;
+    GB_CUDA(cudaMemcpy(ctx->pool.d_v + off, h.v.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(ctx->pool.d_w + off, h.w.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(ctx->pool.d_a + off, h.a.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(ctx->pool.d_rec + off, rec.data(), n * sizeof(NodeRec), cudaMemcpyHostToDevice));
+    ctx->pool.used += n;
+    ref.off = off;
+    ref.n = n;
+    ref.pm_from = std::min(h.pm_from, n);
+    return GB_OK;
+  }
+
+  int build_axis(gb_ctx *ctx, const AxisKey &key, HostAxis &h)
+  {
+    const int n = key.n;
+    const double *p = key.p;
+    auto gl = [&](int order) -> const GLRule & { return gl_host(ctx, order); };
+    switch (key.kind) {
+    case AK_XRAD: {  // p: x_ext, k, pw, C
+      const GLRule &R = gl(n);
+      for (int i = 0; i < n; ++i) {
+        const double q = p[1] * std::sqrt(R.x[i] * p[0]);
+        h.v.push_back(q);
+        h.w.push_back(R.w[i] * p[0] * p[3] * powi(q, (int)p[2]));
+        h.a.push_back(q * q);
+      }
+      break;
+    }
+    case AK_QRAD: {  // p: qmax, pw, C
+      const GLRule &R = gl(n);
+      for (int i = 0; i < n; ++i) {
+        const double q = p[0] * R.x[i];
+        h.v.push_back(q);
+        h.w.push_back(p[0] * R.w[i] * p[2] * powi(q, (int)p[1]));
+        h.a.push_back(q * q);
+      }
+      break;
+    }
+    case AK_COS: {  // p: jac, C
+      const GLRule &R = gl(n);
+      for (int i = 0; i < n; ++i) {
+        const double t = R.x[i];
+        const double c = 2 * (t - 0.5);
+        const double s = 2.0 * std::sqrt(t * (1.0 - t));  // sqrt(1 - c^2) without cancellation
+        h.v.push_back(c);
+        h.w.push_back(2 * R.w[i] * p[1] * (p[0] != 0 ? s : 1.0));
+        h.a.push_back(s);
+      }
+      break;
+    }
+    case AK_PHI: {  // p: C
+      const GLRule &R = gl(n);
+      for (int i = 0; i < n; ++i) {
+        const double ph = 2 * kPi * R.x[i];
+        h.v.push_back(ph);
+        h.w.push_back(2 * kPi * R.w[i] * p[0]);
+        h.a.push_back(std::cos(ph));
+      }
+      break;
+    }
+    case AK_CART: {  // p: qmin, ext, C
+      const GLRule &R = gl(n);
+      for (int i = 0; i < n; ++i) {
+        const double v = p[0] + p[1] * R.x[i];
+        h.v.push_back(v);
+        h.w.push_back(p[1] * R.w[i] * p[2]);
+        h.a.push_back(v * v);
+      }
+      break;
+    }
+    case AK_PQ0: {  // p: ext, scale
+      const GLRule &R = gl(n);
+      for (int i = 0; i < n; ++i) {
+        const double q0 = p[1] * R.x[i] * p[0];
+        h.v.push_back(q0);
+        h.w.push_back(R.w[i] * p[0]);
+        h.a.push_back(q0 * q0);
+      }
+      h.pm_from = 0;
+      break;
+    }
+    case AK_MATS: {  // p: T, E
+      const MatsEntry &M = mats_host(ctx, p[0], p[1]);
+      const bool zero = p[0] > 0;  // the integrator's m_T decides (integrator_finiteTq0_cpu.hh:107-108)
+      if (zero) {
+        h.v.push_back(0.0);
+        h.w.push_back(p[0]);
+        h.a.push_back(0.0);
+      }
+      for (size_t i = 0; i < M.rule.x.size(); ++i) {
+        h.v.push_back(M.rule.x[i]);
+        h.w.push_back(M.rule.w[i]);
+        h.a.push_back(M.rule.x[i] * M.rule.x[i]);
+      }
+      h.pm_from = zero ? 1 : 0;
+      break;
+    }
+    case AK_FTX0: {  // n = tail order; p: T, k, x0_ext, ns, C_int
+      const double T = p[0], k = p[1], x0e = p[2];
+      const int ns = (int)p[3];
+      for (int m = 0; m < ns; ++m) {
+        const double q0 = 2 * kPi * T * m;
+        h.v.push_back(q0);
+        h.w.push_back(T);
+        h.a.push_back(q0 * q0);
+      }
+      const bool Tzero = std::fabs(T) <= 1e-12;
+      const double off = Tzero ? 1e-3 : 0.0;
+      const double start = (2 * ns * kPi * (Tzero ? 0.0 : T)) / k;
+      const double ls = std::log(start + off), le = std::log(x0e / (start + off));
+      if (n > 0) {
+        const GLRule &R = gl(n);
+        for (int i = 0; i < n; ++i) {
+          const double q0 = k * (std::exp(ls + le * R.x[i]) - off);
+          h.v.push_back(q0);
+          h.w.push_back(p[4] * R.w[i] * le * q0 / k);
+          h.a.push_back(q0 * q0);
+        }
+      }
+      h.pm_from = ns > 0 ? 1 : 0;
+      break;
+    }
+    case AK_MODES: {  // n = M + 1; p: T, C
+      for (int m = 0; m < n; ++m) {
+        const double w = 2 * kPi * p[0] * m;
+        h.v.push_back(w);
+        h.w.push_back(p[1]);
+        h.a.push_back(w * w);
+      }
+      h.pm_from = 1;
+      break;
+    }
+    case AK_ONE: {
+      h.v.push_back(0.0);
+      h.w.push_back(p[0]);
+      h.a.push_back(0.0);
+      break;
+    }
+    default:
+      return set_error(ctx, GB_EINVAL, "unknown axis kind");
+    }
+    return GB_OK;
+  }
+
+  int get_axis(gb_ctx *ctx, const AxisKey &key, int role, AxisRef &ref)
+  {
+    auto it = ctx->axis_cache.find(key);
+    if (it != ctx->axis_cache.end()) {
+      ref = it->second;
+      ref.role = role;
+      return GB_OK;
+    }
+    HostAxis h;
+    int rc = build_axis(ctx, key, h);
+    if (rc) return rc;
+    if (h.v.empty()) return set_error(ctx, GB_EINVAL, "empty quadrature axis");
+    rc = pool_append(ctx, h, ref);
+    if (rc) return rc;
+    ref.role = role;
+    ctx->axis_cache[key] = ref;
+    return GB_OK;
+  }
+
+  AxisKey K(int kind, int n, std::initializer_list<double> ps)
+  {
+    AxisKey k;
+    k.kind = kind;
+    k.n = n;
+    int i = 0;
+    for (double v : ps) k.p[i++] = v;
+    return k;
+  }
+
+  // Family -> axes.  Every reference int_element / weight factor is folded into the axes
+  // (constants into the radial axis).  Sources per family in gbint.h.
+  int family_axes(gb_ctx *ctx, const gb_integral &g, AxisRef ax[4], int &na)
+  {
+    const double k = g.k, xe = g.x_extent, tp = 2 * kPi;
+    const int d = g.d;
+    for (int i = 0; i < 4; ++i) ax[i] = AxisRef{0, 0, R_NONE, 1 << 30};
+    na = 0;
+    auto add = [&](const AxisKey &key, int role) -> int {
+      if (key.kind != AK_MATS && key.kind != AK_FTX0 && key.kind != AK_ONE && key.kind != AK_MODES &&
+          (key.n <= 0 || key.n > 4096))
+        return set_error(ctx, GB_EINVAL, "quadrature order out of range (1..4096)");
+      int rc = get_axis(ctx, key, role, ax[na]);
+      if (rc) return rc;
+      ++na;
+      return GB_OK;
+    };
+    const int *n = g.n;
+    int rc = GB_OK;
+    switch (g.family) {
+    case GB_FAM_1D:
+      rc = add(K(AK_XRAD, n[0], {xe, k, double(d - 2), S_d(d) * k * k / 2 / powi(tp, d)}), R_Q);
+      break;
+    case GB_FAM_ANGLE:
+      if ((rc = add(K(AK_XRAD, n[0], {xe, k, double(d - 2), S_d(d) * k * k / 2 * 0.5 / powi(tp, d)}), R_Q))) break;
+      rc = add(K(AK_COS, n[1], {0, 1}), R_C1);
+      break;
+    case GB_FAM_3D:
+      if ((rc = add(K(AK_XRAD, n[0], {xe, k, 1, k * k / 2 / powi(tp, 3)}), R_Q))) break;
+      if ((rc = add(K(AK_COS, n[1], {0, 1}), R_C1))) break;
+      rc = add(K(AK_PHI, n[2], {1}), R_PHI);
+      break;
+    case GB_FAM_4D2ANG:
+      if ((rc = add(K(AK_XRAD, n[0], {xe, k, 2, tp * 0.5 * k * k / powi(tp, 4)}), R_Q))) break;
+      if ((rc = add(K(AK_COS, n[1], {1, 1}), R_C1))) break;
+      rc = add(K(AK_COS, n[2], {0, 1}), R_C2);
+      break;
+    case GB_FAM_4D:
+      if ((rc = add(K(AK_XRAD, n[0], {xe, k, 2, 0.5 * k * k / powi(tp, 4)}), R_Q))) break;
+      if ((rc = add(K(AK_COS, n[1], {1, 1}), R_C1))) break;
+      if ((rc = add(K(AK_COS, n[2], {0, 1}), R_C2))) break;
+      rc = add(K(AK_PHI, n[3], {1}), R_PHI);
+      break;
+    case GB_FAM_CART1:
+    case GB_FAM_CART2:
+    case GB_FAM_CART3: {
+      const int dim = g.family - GB_FAM_CART1 + 1;
+      const int roles[3] = {R_QX, R_QY, R_QZ};
+      for (int a = 0; a < dim && !rc; ++a)
+        rc = add(K(AK_CART, n[a], {g.qmin[a], g.qmax[a] - g.qmin[a], a == 0 ? powi(tp, -dim) : 1.0}), roles[a]);
+      break;
+    }
+    case GB_FAM_2DPQ0:
+    case GB_FAM_2DPX0: {
+      const bool px = g.family == GB_FAM_2DPX0;
+      if ((rc = add(K(AK_XRAD, n[0], {xe, k, 0, 0.5 * k * k * tp * 0.5 * (px ? k : 1.0) / powi(tp, 3)}), R_Q))) break;
+      if ((rc = add(K(AK_COS, n[1], {0, 1}), R_C1))) break;
+      rc = add(K(AK_PQ0, n[2], {g.x0_extent, px ? k : 1.0}), R_Q0);
+      break;
+    }
+    case GB_FAM_3DPQ0:
+    case GB_FAM_3DPX0: {
+      const bool px = g.family == GB_FAM_3DPX0;
+      if ((rc = add(K(AK_XRAD, n[0], {xe, k, 1, 0.5 * k * k * (px ? k : 1.0) / powi(tp, 4)}), R_Q))) break;
+      if ((rc = add(K(AK_COS, n[1], {0, 1}), R_C1))) break;
+      if ((rc = add(K(AK_PHI, n[2], {1}), R_PHI))) break;
+      rc = add(K(AK_PQ0, n[3], {g.x0_extent, px ? k : 1.0}), R_Q0);
+      break;
+    }
+    case GB_FAM_FTQ0:
+    case GB_FAM_ANGLE_FTQ0:
+    case GB_FAM_4D_FTQ0: {
+      // E: given, else the reference rule (E = 10T, re-selected to k if |k-E|/max > 2.5%)
+      double E = g.E;
+      if (!(E > 0)) {
+        E = 10 * g.T;
+        if (std::fabs(k - E) / std::max(k, E) > 2.5e-2) E = k;
+      }
+      if (g.family == GB_FAM_4D_FTQ0) {
+        if ((rc = add(K(AK_XRAD, n[0], {xe, k, 1, 0.5 * k * k / powi(tp, 3)}), R_Q))) break;
+        if ((rc = add(K(AK_COS, n[1], {0, 1}), R_C1))) break;
+        if ((rc = add(K(AK_PHI, n[2], {1}), R_PHI))) break;
+      } else {
+        const double half = g.family == GB_FAM_ANGLE_FTQ0 ? 0.5 : 1.0;
+        if ((rc = add(K(AK_XRAD, n[0], {xe, k, double(d - 3), S_d(d - 1) * 0.5 * k * k * half / powi(tp, d - 1)}), R_Q)))
+          break;
+        if (g.family == GB_FAM_ANGLE_FTQ0 && (rc = add(K(AK_COS, n[1], {0, 1}), R_C1))) break;
+      }
+      rc = add(K(AK_MATS, 0, {g.T, E, (double)ctx->mats_min, (double)ctx->mats_vacuum, (double)ctx->mats_add}), R_Q0);
+      break;
+    }
+    case GB_FAM_FTX0:
+    case GB_FAM_ANGLE_FTX0:
+    case GB_FAM_4D_FTX0: {
+      const bool Tzero = std::fabs(g.T) <= 1e-12;
+      const int ns = Tzero ? 0 : g.x0_summands;
+      int tail;
+      if (g.family == GB_FAM_4D_FTX0) {
+        if ((rc = add(K(AK_XRAD, n[0], {xe, k, 1, 0.5 * k * k / powi(tp, 3)}), R_Q))) break;
+        if ((rc = add(K(AK_COS, n[1], {0, 1}), R_C1))) break;
+        if ((rc = add(K(AK_PHI, n[2], {1}), R_PHI))) break;
+        tail = n[3];
+      } else {
+        const double half = g.family == GB_FAM_ANGLE_FTX0 ? 0.5 : 1.0;
+        if ((rc = add(K(AK_XRAD, n[0], {xe, k, double(d - 3), S_d(d - 1) * 0.5 * k * k * half / powi(tp, d - 1)}), R_Q)))
+          break;
+        if (g.family == GB_FAM_ANGLE_FTX0) {
+          if ((rc = add(K(AK_COS, n[1], {0, 1}), R_C1))) break;
+          tail = n[2];
+        } else
+          tail = n[1];
+      }
+      tail += g.x0_summands - ns;  // at T = 0 the summands join the tail (integrator_finiteTx0_cpu.hh:41-50)
+      if (tail < 0 || tail > 4096) return set_error(ctx, GB_EINVAL, "x0 quadrature order out of range");
+      rc = add(K(AK_FTX0, tail, {Tzero ? 0.0 : g.T, k, g.x0_extent, (double)ns, k / tp}), R_Q0);
+      break;
+    }
+    case GB_FAM_CONST:
+      rc = add(K(AK_ONE, 1, {S_d(d) / powi(tp, d)}), R_NONE);
+      break;
+    case GB_FAM_QLOOP:
+      if ((rc = add(K(AK_QRAD, n[0], {xe, 3, 4 * kPi / powi(tp, 4)}), R_Q))) break;
+      rc = add(K(AK_COS, n[1], {0, 1}), R_C1);
+      break;
+    case GB_FAM_QLOOP_T: {
+      const int M = g.x0_summands;
+      if (M < 0 || M > 4095) return set_error(ctx, GB_EINVAL, "mode count out of range");
+      if ((rc = add(K(AK_MODES, M + 1, {g.T, g.T * tp / powi(tp, 3)}), R_Q0))) break;
+      if ((rc = add(K(AK_QRAD, n[0], {xe, 2, 1.0}), R_Q))) break;
+      rc = add(K(AK_COS, n[1], {0, 1}), R_C1);
+      break;
+    }
+    default:
+      return set_error(ctx, GB_EINVAL, "unknown family");
+    }
+    return rc;
+  }
+
+  int tables_needed(int integrand)
+  {
+    switch (integrand) {
+    case GB_IG_PROP1:
+    case GB_IG_FTLOOP:
+      return 1;
+    case GB_IG_PROP3:
+      return 4;
+    case GB_IG_VERT4:
+      return 2;
+    }
+    return 0;
+  }
+} // namespace
+
+// ============================================================================ batches
+namespace gbint
+{
+  void free_batch(gb_ctx *ctx, gb_batch *b)
+  {
+    if (!b) return;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    cudaFree(b->d_items);
+    cudaFree(b->d_units);
+    cudaFree(b->d_segs);
+    cudaFree(b->d_seg);
+    cudaFree(b->d_partials);
+    cudaFree(b->d_item_count);
+    cudaFree(b->d_counters);
+    cudaFree(b->d_out);
+    if (ctx) ctx->in_use -= b->bytes;
+    delete b;
+  }
+
+  int build_batch(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
+                  gb_batch **out)
+  {
+    if (!ctx || !out || n <= 0 || !items) return set_error(ctx, GB_EINVAL, "bad batch arguments");
+    if (precision != GB_PREC_FP32C && precision != GB_PREC_FP64) return set_error(ctx, GB_EINVAL, "bad precision");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    GB_CUDA(cudaSetDevice(ctx->device));
+    auto b = std::make_unique<gb_batch>();
+    b->n = n;
+    b->precision = precision;
+    b->src.assign(items, items + n);
+    b->items.resize(n);
+    std::map<std::tuple<int, int, int, int, double>, int> seg_index;  // dedupe
+    std::vector<int> item_kind(n);
+    for (int i = 0; i < n; ++i) {
+      const gb_integral &g = items[i];
+      ItemDev &it = b->items[i];
+      std::memset(&it, 0, sizeof(it));
+      it.integrand = g.integrand;
+      it.family = g.family;
+      it.k = g.k;
+      std::memcpy(it.args, g.args, sizeof(it.args));
+      if (g.integrand != GB_IG_POLY && g.integrand != GB_IG_PROP1 && g.integrand != GB_IG_PROP3 &&
+          g.integrand != GB_IG_VERT4 && g.integrand != GB_IG_FTLOOP)
+        return set_error(ctx, GB_EINVAL, "unknown integrand");
+      int rc = family_axes(ctx, g, it.ax, it.n_axes);
+      if (rc) return rc;
+      // tables
+      const int nt = tables_needed(g.integrand);
+      if (nt > n_tables) return set_error(ctx, GB_EINVAL, "integrand needs more tables than given");
+      for (int t = 0; t < 4; ++t) it.tab[t] = -1;
+      for (int t = 0; t < nt; ++t) {
+        if (!tables || !tables[t] || tables[t]->slot < 0) return set_error(ctx, GB_EINVAL, "null table");
+        it.tab[t] = tables[t]->slot;
+      }
+      if (g.integrand == GB_IG_FTLOOP && (tables[0]->spec.n1 < 2 || !(g.args[2] > 0)))
+        return set_error(ctx, GB_EINVAL, "FTLOOP needs a 2D table and T > 0");
+      if (g.integrand == GB_IG_VERT4) {
+        const gb_table_spec &a = tables[0]->spec, &c = tables[1]->spec;
+        if (a.n1 < 2 || std::memcmp(&a, &c, sizeof(a)) != 0)
+          return set_error(ctx, GB_EINVAL, "VERT4 needs two 2D tables with identical axes");
+      }
+      for (int t = 0; t < nt; ++t)
+        if (g.integrand != GB_IG_FTLOOP && g.integrand != GB_IG_VERT4 && tables[t]->spec.n1 != 0)
+          return set_error(ctx, GB_EINVAL, "integrand needs 1D tables");
+      // points (integrand evaluations, +-q0 counted twice)
+      uint64_t pts = 1;
+      for (int a = 0; a < it.n_axes; ++a) {
+        const AxisRef &A = it.ax[a];
+        const uint64_t single = (uint64_t)std::min(A.pm_from, A.n);
+        pts *= single + 2 * (uint64_t)(A.n - single);
+      }
+      b->points += pts;
+      // kind
+      int kind = K_GENERIC;
+      if (precision == GB_PREC_FP32C) {
+        if (g.integrand == GB_IG_PROP1 && it.n_axes == 2 && it.ax[0].role == R_Q && it.ax[1].role == R_C1 &&
+            it.ax[1].pm_from >= it.ax[1].n)
+          kind = K_S1;
+        else if (g.integrand == GB_IG_FTLOOP && g.family == GB_FAM_QLOOP_T)
+          kind = K_S2;
+        else if (g.integrand == GB_IG_PROP3 && g.family == GB_FAM_3D)
+          kind = K_S3;
+        else if (g.integrand == GB_IG_VERT4 && g.family == GB_FAM_4D)
+          kind = K_S5;
+      }
+      // table bytes of S kinds must fit shared memory
+      if (kind != K_GENERIC) {
+        int tb = 0;
+        for (int t = 0; t < nt; ++t) tb += tables[t]->bytes;
+        if (tb > 160 * 1024) kind = K_GENERIC;
+      }
+      it.kind = kind;
+      item_kind[i] = kind;
+      long long rows;
+      switch (kind) {
+      case K_S1: rows = it.ax[0].n; break;
+      case K_S2: rows = (long long)it.ax[0].n * it.ax[1].n; break;
+      case K_S3: rows = (long long)it.ax[0].n * it.ax[1].n; break;
+      case K_S5: rows = (long long)it.ax[0].n * it.ax[1].n; break;
+      default: {
+        rows = 1;
+        for (int a = 0; a < it.n_axes; ++a) rows *= it.ax[a].n;
+      }
+      }
+      if (rows > (1ll << 30)) return set_error(ctx, GB_EINVAL, "integral too large for one item (split it)");
+      it.rows = (int)rows;
+      // hoisted segment
+      if (kind != K_GENERIC) {
+        SegDev S{};
+        S.kind = kind;  // SEG_S* == K_S*
+        S.tab = it.tab[0];
+        S.ax0 = kind == K_S2 ? it.ax[0] : it.ax[0];
+        S.n0 = it.ax[0].n;
+        S.n1 = 1;
+        double par = 0;
+        if (kind == K_S1) par = g.args[2];
+        if (kind == K_S2) {
+          S.ax1 = it.ax[1];
+          S.n1 = it.ax[1].n;
+          par = g.args[2];
+        }
+        if (kind == K_S5) {
+          S.ax1 = it.ax[1];
+          S.n1 = it.ax[1].n;
+        }
+        S.par[0] = par;
+        auto key = std::make_tuple(kind, S.ax0.off, kind == K_S2 || kind == K_S5 ? S.ax1.off : -1, S.tab, par);
+        auto f = seg_index.find(key);
+        if (f == seg_index.end()) {
+          S.off = (int)b->seg_total;
+          b->seg_total += (size_t)S.n0 * S.n1;
+          b->seg_max_entries = std::max(b->seg_max_entries, S.n0 * S.n1);
+          seg_index[key] = (int)b->segs.size();
+          b->segs.push_back(S);
+          it.seg_off = S.off;
+        } else
+          it.seg_off = b->segs[f->second].off;
+      }
+      // reference-pattern geometry
+      int loop_axis = -1;
+      if (g.family == GB_FAM_4D) loop_axis = 2;
+      if (g.family == GB_FAM_4D_FTQ0 || g.family == GB_FAM_4D_FTX0) loop_axis = 3;
+      long long pt = 1;
+      for (int a = 0; a < it.n_axes; ++a)
+        if (a != loop_axis) pt *= it.ax[a].n;
+      b->plain_loop_axis.push_back(loop_axis);
+      b->plain_threads.push_back(pt);
+    }
+    // units grouped by kind
+    const int kinds[5] = {K_S1, K_S2, K_S3, K_S5, K_GENERIC};
+    for (int kind : kinds) {
+      gb_batch::KindRun run;
+      run.kind = kind;
+      run.unit_begin = (int)b->units.size();
+      const int rpu = kind_rows_per_unit(kind, ctx->threads_override[kind]);
+      int tab_cap = 0, rec_cap = 0;
+      bool any = false;
+      for (int i = 0; i < n; ++i) {
+        if (item_kind[i] != kind) continue;
+        any = true;
+        ItemDev &it = b->items[i];
+        const int nu = (it.rows + rpu - 1) / rpu;
+        it.unit_begin = (int)b->units.size() - run.unit_begin;
+        it.n_units = nu;
+        for (int u = 0; u < nu; ++u) {
+          UnitDev U{};
+          U.item = i;
+          U.row_begin = u * rpu;
+          U.row_count = std::min(rpu, it.rows - u * rpu);
+          b->units.push_back(U);
+        }
+        if (kind != K_GENERIC) {
+          int tb = 0;
+          for (int t = 0; t < tables_needed(it.integrand); ++t) tb += ctx->slots[it.tab[t]]->bytes;
+          tab_cap = std::max(tab_cap, tb);
+          int rc_n = 0;
+          if (kind == K_S1) rc_n = it.ax[1].n;
+          if (kind == K_S2 || kind == K_S3) rc_n = it.ax[2].n;
+          if (kind == K_S5) rc_n = it.ax[2].n + it.ax[3].n;
+          rec_cap = std::max(rec_cap, rc_n);
+        }
+      }
+      if (!any) continue;
+      run.n_units = (int)b->units.size() - run.unit_begin;
+      run.tab_cap = (tab_cap + 127) / 128 * 128;
+      run.rec_cap = (rec_cap + 3) / 4 * 4;
+      if (kind == K_GENERIC) {
+        run.threads = kGenericThreads;
+        run.ctas = std::min(run.n_units, ctx->num_sms * 8);
+      } else {
+        run.threads = rpu;
+        const int occ = fp32c_occupancy(kind, rpu, run.tab_cap, run.rec_cap);
+        if (occ <= 0) return set_error(ctx, GB_EINVAL, "FP32 kernel cannot launch with this table/record size");
+        run.ctas = std::min(run.n_units, ctx->num_sms * occ);
+      }
+      b->runs.push_back(run);
+    }
+    // device buffers
+    const size_t nu = b->units.size();
+    size_t bytes = n * sizeof(ItemDev) + nu * sizeof(UnitDev) + b->segs.size() * sizeof(SegDev) +
+                   b->seg_total * sizeof(double) + nu * sizeof(double) + n * sizeof(int) +
+                   b->runs.size() * sizeof(int) + n * sizeof(double);
+    if (ctx->in_use + bytes > ctx->budget) return set_error(ctx, GB_EBUDGET, "batch exceeds the HBM budget");
+    auto alloc = [&](void **p, size_t sz) -> int {
+      GB_CUDA(cudaMalloc(p, std::max<size_t>(sz, 16)));
+      return GB_OK;
+    };
+    int rc;
+    if ((rc = alloc((void **)&b->d_items, n * sizeof(ItemDev)))) return rc;
+    if ((rc = alloc((void **)&b->d_units, nu * sizeof(UnitDev)))) { free_batch(nullptr, b.release()); return rc; }
+    if ((rc = alloc((void **)&b->d_segs, b->segs.size() * sizeof(SegDev)))) { free_batch(nullptr, b.release()); return rc; }
+    if ((rc = alloc((void **)&b->d_seg, b->seg_total * sizeof(double)))) { free_batch(nullptr, b.release()); return rc; }
+    if ((rc = alloc((void **)&b->d_partials, nu * sizeof(double)))) { free_batch(nullptr, b.release()); return rc; }
+    if ((rc = alloc((void **)&b->d_item_count, n * sizeof(int)))) { free_batch(nullptr, b.release()); return rc; }
+    if ((rc = alloc((void **)&b->d_counters, b->runs.size() * sizeof(int)))) { free_batch(nullptr, b.release()); return rc; }
+    if ((rc = alloc((void **)&b->d_out, n * sizeof(double)))) { free_batch(nullptr, b.release()); return rc; }
+    b->bytes = bytes;
+    ctx->in_use += bytes;
+    GB_CUDA(cudaMemcpy(b->d_items, b->items.data(), n * sizeof(ItemDev), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(b->d_units, b->units.data(), nu * sizeof(UnitDev), cudaMemcpyHostToDevice));
+    if (!b->segs.empty())
+      GB_CUDA(cudaMemcpy(b->d_segs, b->segs.data(), b->segs.size() * sizeof(SegDev), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemset(b->d_item_count, 0, n * sizeof(int)));
+    GB_CUDA(cudaMemset(b->d_out, 0, n * sizeof(double)));
+    *out = b.release();
+    return GB_OK;
+  }
+
+  int run_batch(gb_ctx *ctx, gb_batch *b, double *d_out, cudaStream_t s)
+  {
+    RunParams P{};
+    P.items = b->d_items;
+    P.n_items = b->n;
+    P.pv = ctx->pool.d_v;
+    P.pw = ctx->pool.d_w;
+    P.pa = ctx->pool.d_a;
+    P.prec = ctx->pool.d_rec;
+    P.tabs = ctx->d_dir;
+    P.seg = b->d_seg;
+    P.item_count = b->d_item_count;
+    P.out = d_out ? d_out : b->d_out;
+    P.err = ctx->d_err;
+    GB_CUDA(cudaMemsetAsync(b->d_counters, 0, b->runs.size() * sizeof(int), s));
+    if (!b->segs.empty())
+      GB_CUDA(launch_seg(b->d_segs, (int)b->segs.size(), b->seg_max_entries, P.pv, P.pw, P.pa, P.tabs, b->d_seg, s));
+    for (size_t r = 0; r < b->runs.size(); ++r) {
+      const auto &run = b->runs[r];
+      P.units = b->d_units + run.unit_begin;
+      P.n_units = run.n_units;
+      P.partials = b->d_partials + run.unit_begin;
+      P.unit_counter = b->d_counters + r;
+      if (run.kind == K_GENERIC)
+        GB_CUDA(launch_generic(P, run.ctas, s));
+      else
+        GB_CUDA(launch_fp32c(run.kind, P, run.threads, run.ctas, run.tab_cap, run.rec_cap, s));
+    }
+    return GB_OK;
+  }
+} // namespace gbint
+
+// ============================================================================ C ABI
+extern "C" {
+
+int gb_version(void) { return GBINT_ABI_VERSION; }
+
+const char *gb_status_string(int s)
+{
+  switch (s) {
+  case GB_OK: return "ok";
+  case GB_EINVAL: return "invalid argument";
+  case GB_ENOMEM: return "out of memory";
+  case GB_EBUDGET: return "HBM budget exceeded";
+  case GB_ETIMEDOUT: return "timed out";
+  case GB_ECUDA: return "CUDA error";
+  case GB_ENODEV: return "no CUDA device";
+  case GB_EAGAIN: return "not ready";
+  case GB_EDEVICE: return "device-side error flag";
+  case GB_ECANCELED: return "canceled";
+  }
+  return "unknown status";
+}
+
+int gb_ctx_create(int device, size_t budget, gb_ctx **out)
+{
+  if (!out) return GB_EINVAL;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GB_ENODEV;
+  if (device < 0 || device >= ndev) return GB_ENODEV;
+  auto ctx = std::make_unique<gb_ctx>();
+  ctx->device = device;
+  ctx->budget = budget ? budget : ((size_t)8 << 30);
+  gb_ctx *c = ctx.get();
+#define CK(call)                                       \
+  do {                                                 \
+    cudaError_t e__ = (call);                          \
+    if (e__ != cudaSuccess) return GB_ECUDA;           \
+  } while (0)
+  CK(cudaSetDevice(device));
+  CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
+  CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  c->pool_streams.resize(kPoolStreams);
+  for (auto &s : c->pool_streams) CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  c->pool.capacity = kPoolCapacity;
+  CK(cudaMalloc(&c->pool.d_v, kPoolCapacity * sizeof(double)));
+  CK(cudaMalloc(&c->pool.d_w, kPoolCapacity * sizeof(double)));
+  CK(cudaMalloc(&c->pool.d_a, kPoolCapacity * sizeof(double)));
+  CK(cudaMalloc(&c->pool.d_rec, kPoolCapacity * sizeof(NodeRec)));
+  CK(cudaMalloc(&c->d_dir, kMaxTables * sizeof(TableDev)));
+  CK(cudaMemset(c->d_dir, 0, kMaxTables * sizeof(TableDev)));
+  c->h_dir.assign(kMaxTables, TableDev{});
+  c->slots.assign(kMaxTables, nullptr);
+  CK(cudaMalloc(&c->d_err, sizeof(int)));
+  CK(cudaMemset(c->d_err, 0, sizeof(int)));
+  CK(cudaMalloc(&c->plain_res, kPoolStreams * sizeof(double)));
+  CK(cudaMallocHost(&c->plain_res_h, kPoolStreams * sizeof(double)));
+  c->plain_buf.assign(kPoolStreams, nullptr);
+  c->plain_buf_elems.assign(kPoolStreams, 0);
+  c->plain_tmp.assign(kPoolStreams, nullptr);
+  c->plain_tmp_bytes.assign(kPoolStreams, 0);
+#undef CK
+  *out = ctx.release();
+  return GB_OK;
+}
+
+int gb_ctx_destroy(gb_ctx *ctx)
+{
+  if (!ctx) return GB_EINVAL;
+  if (ctx->serve) serve_stop(ctx);
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  for (auto &kv : ctx->gl) {
+    cudaFree(kv.second.d64x);
+    cudaFree(kv.second.d64w);
+    cudaFree(kv.second.d32x);
+    cudaFree(kv.second.d32w);
+  }
+  for (auto &m : ctx->mats) {
+    cudaFree(m->d64x);
+    cudaFree(m->d64w);
+    cudaFree(m->d32x);
+    cudaFree(m->d32w);
+  }
+  for (auto *t : ctx->slots)
+    if (t) {
+      cudaFree(t->buf[0]);
+      cudaFree(t->buf[1]);
+      delete t;
+    }
+  for (size_t i = 0; i < ctx->plain_buf.size(); ++i) {
+    cudaFree(ctx->plain_buf[i]);
+    cudaFree(ctx->plain_tmp[i]);
+  }
+  cudaFree(ctx->plain_res);
+  cudaFreeHost(ctx->plain_res_h);
+  cudaFree(ctx->pool.d_v);
+  cudaFree(ctx->pool.d_w);
+  cudaFree(ctx->pool.d_a);
+  cudaFree(ctx->pool.d_rec);
+  cudaFree(ctx->d_dir);
+  cudaFree(ctx->d_err);
+  for (auto s : ctx->pool_streams) cudaStreamDestroy(s);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GB_OK;
+}
+
+int gb_last_error(gb_ctx *ctx, char *buf, size_t len)
+{
+  if (!ctx || !buf || len == 0) return GB_EINVAL;
+  std::snprintf(buf, len, "%s", ctx->last_error.c_str());
+  return GB_OK;
+}
+
+// ------------------------------------------------------------------ provider
+int gb_quad_gl(gb_ctx *ctx, int order, int dtype, const double **hx, const double **hw, const void **dx,
+               const void **dw)
+{
+  if (!ctx || order <= 0 || order > 4096) return set_error(ctx, GB_EINVAL, "bad GL order");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  GLRule &r = const_cast<GLRule &>(gl_host(ctx, order));
+  if (hx) *hx = r.x.data();
+  if (hw) *hw = r.w.data();
+  if (dx || dw) {
+    GB_CUDA(cudaSetDevice(ctx->device));
+    if (dtype == GB_DTYPE_F64) {
+      if (!r.d64x) {
+        GB_CUDA(cudaMalloc(&r.d64x, order * sizeof(double)));
+        GB_CUDA(cudaMalloc(&r.d64w, order * sizeof(double)));
+        GB_CUDA(cudaMemcpy(r.d64x, r.x.data(), order * sizeof(double), cudaMemcpyHostToDevice));
+        GB_CUDA(cudaMemcpy(r.d64w, r.w.data(), order * sizeof(double), cudaMemcpyHostToDevice));
+      }
+      if (dx) *dx = r.d64x;
+      if (dw) *dw = r.d64w;
+    } else {
+      if (!r.d32x) {
+        std::vector<float> fx(r.x.begin(), r.x.end()), fw(r.w.begin(), r.w.end());
+        GB_CUDA(cudaMalloc(&r.d32x, order * sizeof(float)));
+        GB_CUDA(cudaMalloc(&r.d32w, order * sizeof(float)));
+        GB_CUDA(cudaMemcpy(r.d32x, fx.data(), order * sizeof(float), cudaMemcpyHostToDevice));
+        GB_CUDA(cudaMemcpy(r.d32w, fw.data(), order * sizeof(float), cudaMemcpyHostToDevice));
+      }
+      if (dx) *dx = r.d32x;
+      if (dw) *dw = r.d32w;
+    }
+  }
+  return GB_OK;
+}
+
+int gb_quad_matsubara(gb_ctx *ctx, double T, double E, int dtype, int *size, const double **hx, const double **hw,
+                      const void **dx, const void **dw, double *T_rule)
+{
+  if (!ctx || !(T >= 0) || !(E >= 0)) return set_error(ctx, GB_EINVAL, "bad Matsubara parameters");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  MatsEntry &m = mats_host(ctx, T, E);
+  const int n = (int)m.rule.x.size();
+  if (size) *size = n;
+  if (hx) *hx = m.rule.x.data();
+  if (hw) *hw = m.rule.w.data();
+  if (T_rule) *T_rule = m.rule.T_rule;
+  if (dx || dw) {
+    GB_CUDA(cudaSetDevice(ctx->device));
+    if (dtype == GB_DTYPE_F64) {
+      if (!m.d64x) {
+        GB_CUDA(cudaMalloc(&m.d64x, n * sizeof(double)));
+        GB_CUDA(cudaMalloc(&m.d64w, n * sizeof(double)));
+        GB_CUDA(cudaMemcpy(m.d64x, m.rule.x.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+        GB_CUDA(cudaMemcpy(m.d64w, m.rule.w.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+      }
+      if (dx) *dx = m.d64x;
+      if (dw) *dw = m.d64w;
+    } else {
+      if (!m.d32x) {
+        std::vector<float> fx(m.rule.x.begin(), m.rule.x.end()), fw(m.rule.w.begin(), m.rule.w.end());
+        GB_CUDA(cudaMalloc(&m.d32x, n * sizeof(float)));
+        GB_CUDA(cudaMalloc(&m.d32w, n * sizeof(float)));
+        GB_CUDA(cudaMemcpy(m.d32x, fx.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+        GB_CUDA(cudaMemcpy(m.d32w, fw.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+      }
+      if (dx) *dx = m.d32x;
+      if (dw) *dw = m.d32w;
+    }
+  }
+  return GB_OK;
+}
+
+int gb_quad_config(gb_ctx *ctx, int min_size, int vacuum, int add)
+{
+  if (!ctx) return GB_EINVAL;
+  // QuadratureProvider(json) / MatsubaraStorage setters (quadrature_provider.cu:112-126,220-227)
+  if (min_size <= 0) return set_error(ctx, GB_EINVAL, "min_matsubara_size must be positive");
+  if (vacuum <= 0) return set_error(ctx, GB_EINVAL, "vacuum_quad_size must be positive");
+  if (add < 0) return set_error(ctx, GB_EINVAL, "add_matsubara_size must be non-negative");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  ctx->mats_min = min_size;
+  ctx->mats_vacuum = vacuum;
+  ctx->mats_add = add;
+  return GB_OK;
+}
+
+// ------------------------------------------------------------------ tables
+int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
+{
+  if (!ctx || !spec || !out) return set_error(ctx, GB_EINVAL, "bad table arguments");
+  if (spec->n0 < 2 || (spec->n1 != 0 && spec->n1 < 2)) return set_error(ctx, GB_EINVAL, "table axes need >= 2 points");
+  if ((spec->log0 && !(spec->lo0 > 0 && spec->hi0 > spec->lo0)) || (!spec->log0 && !(spec->hi0 > spec->lo0)))
+    return set_error(ctx, GB_EINVAL, "bad table axis 0 range");
+  if (spec->n1 && ((spec->log1 && !(spec->lo1 > 0 && spec->hi1 > spec->lo1)) || (!spec->log1 && !(spec->hi1 > spec->lo1))))
+    return set_error(ctx, GB_EINVAL, "bad table axis 1 range");
+  const long long elems = (long long)spec->n0 * std::max(spec->n1, 1);
+  if (elems > (1 << 24)) return set_error(ctx, GB_EINVAL, "table too large");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  int slot = -1;
+  for (int i = 0; i < kMaxTables; ++i)
+    if (!ctx->slots[i]) {
+      slot = i;
+      break;
+    }
+  if (slot < 0) return set_error(ctx, GB_ENOMEM, "table directory full");
+  auto t = std::make_unique<gb_table>();
+  t->spec = *spec;
+  t->elems = (int)elems;
+  t->bytes = (int)((elems * 4 + 15) / 16 * 16);
+  GB_CUDA(cudaSetDevice(ctx->device));
+  GB_CUDA(cudaMalloc(&t->buf[0], t->bytes));
+  GB_CUDA(cudaMalloc(&t->buf[1], t->bytes));
+  GB_CUDA(cudaMemset(t->buf[0], 0, t->bytes));
+  GB_CUDA(cudaMemset(t->buf[1], 0, t->bytes));
+  TableDev &D = ctx->h_dir[slot];
+  D = TableDev{};
+  D.data = t->buf[0];
+  D.n0 = spec->n0;
+  D.n1 = spec->n1;
+  D.bytes = t->bytes;
+  D.a0 = make_axis(spec->n0, spec->log0, spec->lo0, spec->hi0);
+  D.a1 = spec->n1 ? make_axis(spec->n1, spec->log1, spec->lo1, spec->hi1) : dev::AxisDev{};
+  GB_CUDA(cudaMemcpy(ctx->d_dir + slot, &D, sizeof(TableDev), cudaMemcpyHostToDevice));
+  t->slot = slot;
+  ctx->slots[slot] = t.get();
+  *out = t.release();
+  return GB_OK;
+}
+
+static int table_update_impl(gb_ctx *ctx, gb_table *t, const float *src, cudaMemcpyKind kind, void *stream)
+{
+  if (!ctx || !t || !src || t->slot < 0) return set_error(ctx, GB_EINVAL, "bad table update");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  GB_CUDA(cudaSetDevice(ctx->device));
+  const int back = t->front ^ 1;
+  GB_CUDA(cudaMemcpyAsync(t->buf[back], src, (size_t)t->elems * 4, kind, s));
+  // publish the new buffer in the directory, ordered after the data on the same stream
+  TableDev &D = ctx->h_dir[t->slot];
+  D.data = t->buf[back];
+  GB_CUDA(cudaMemcpyAsync(ctx->d_dir + t->slot, &D, sizeof(TableDev), cudaMemcpyHostToDevice, s));
+  // the pageable host source (h_dir entry) is staged by the runtime before the call returns
+  t->front = back;
+  t->epoch++;
+  return GB_OK;
+}
+
+int gb_table_update(gb_ctx *ctx, gb_table *t, const float *host_data, void *stream)
+{
+  return table_update_impl(ctx, t, host_data, cudaMemcpyHostToDevice, stream);
+}
+
+int gb_table_update_device(gb_ctx *ctx, gb_table *t, const float *device_data, void *stream)
+{
+  return table_update_impl(ctx, t, device_data, cudaMemcpyDeviceToDevice, stream);
+}
+
+int gb_table_epoch(gb_ctx *ctx, gb_table *t, uint64_t *epoch)
+{
+  if (!ctx || !t || !epoch) return GB_EINVAL;
+  *epoch = t->epoch;
+  return GB_OK;
+}
+
+int gb_table_destroy(gb_ctx *ctx, gb_table *t)
+{
+  if (!ctx || !t) return GB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  if (t->slot >= 0) ctx->slots[t->slot] = nullptr;
+  cudaFree(t->buf[0]);
+  cudaFree(t->buf[1]);
+  delete t;
+  return GB_OK;
+}
+
+// ------------------------------------------------------------------ batches
+int gb_batch_create(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
+                    gb_batch **out)
+{
+  return build_batch(ctx, items, n, tables, n_tables, precision, out);
+}
+
+int gb_batch_run(gb_ctx *ctx, gb_batch *b, double *d_out, void *stream)
+{
+  if (!ctx || !b) return GB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  GB_CUDA(cudaSetDevice(ctx->device));
+  return run_batch(ctx, b, d_out, stream ? (cudaStream_t)stream : ctx->stream);
+}
+
+int gb_batch_run_graph(gb_ctx *ctx, gb_batch *b, void *stream)
+{
+  if (!ctx || !b) return GB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  GB_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  if (!b->graph) {
+    cudaStream_t cap;
+    GB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t g;
+    GB_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    const int rc = run_batch(ctx, b, nullptr, cap);
+    cudaError_t e = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
+  }
+  GB_CUDA(cudaGraphLaunch(b->graph, s));
+  return GB_OK;
+}
+
+int gb_batch_results(gb_ctx *ctx, gb_batch *b, double *host_out, void *stream)
+{
+  if (!ctx || !b || !host_out) return GB_EINVAL;
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  GB_CUDA(cudaSetDevice(ctx->device));
+  GB_CUDA(cudaMemcpyAsync(host_out, b->d_out, b->n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  int err = 0;
+  GB_CUDA(cudaMemcpy(&err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) {
+    cudaMemset(ctx->d_err, 0, sizeof(int));
+    return set_error(ctx, GB_EDEVICE, "kernel reported error flags " + std::to_string(err));
+  }
+  return GB_OK;
+}
+
+int gb_batch_get(gb_ctx *ctx, gb_batch *b, double *host_out, void *stream)
+{
+  int rc = gb_batch_run(ctx, b, nullptr, stream);
+  if (rc) return rc;
+  return gb_batch_results(ctx, b, host_out, stream);
+}
+
+int gb_batch_info(gb_ctx *ctx, gb_batch *b, uint64_t *points, int *n_units, int *n_items)
+{
+  if (!ctx || !b) return GB_EINVAL;
+  if (points) *points = b->points;
+  if (n_units) *n_units = (int)b->units.size();
+  if (n_items) *n_items = b->n;
+  return GB_OK;
+}
+
+int gb_batch_destroy(gb_ctx *ctx, gb_batch *b)
+{
+  if (!ctx || !b) return GB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  free_batch(ctx, b);
+  return GB_OK;
+}
+
+// Reference execution pattern: request() launches the per-point kernel for every integral on a
+// pooled stream; get() then reduces each integral's buffer with CUB, copies the value to the
+// host and synchronises (integrator_4D_gpu.hh:141-197).  In-flight buffers are bounded to 4 GiB.
+int gb_batch_run_plain(gb_ctx *ctx, gb_batch *b, double *host_out, int n_streams)
+{
+  if (!ctx || !b || !host_out) return GB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  GB_CUDA(cudaSetDevice(ctx->device));
+  const int S = std::max(1, std::min(n_streams, (int)ctx->pool_streams.size()));
+  const size_t cap_bytes = (size_t)4 << 30;
+  int i0 = 0;
+  std::vector<double *> bufs;
+  std::vector<size_t> buf_elems;
+  std::vector<void *> tmps;
+  std::vector<size_t> tmp_bytes;
+  int rc = GB_OK;
+  while (i0 < b->n && rc == GB_OK) {
+    // chunk of integrals whose buffers fit the cap
+    int i1 = i0;
+    size_t bytes = 0;
+    while (i1 < b->n && (i1 == i0 || bytes + b->plain_threads[i1] * sizeof(double) <= cap_bytes)) {
+      bytes += b->plain_threads[i1] * sizeof(double);
+      ++i1;
+    }
+    const int m = i1 - i0;
+    if ((int)bufs.size() < m) {
+      bufs.resize(m, nullptr);
+      buf_elems.resize(m, 0);
+      tmps.resize(m, nullptr);
+      tmp_bytes.resize(m, 0);
+    }
+    // request(): allocate + launch
+    for (int j = 0; j < m && rc == GB_OK; ++j) {
+      const int i = i0 + j;
+      cudaStream_t s = ctx->pool_streams[i % S];
+      const size_t ne = (size_t)b->plain_threads[i];
+      if (buf_elems[j] < ne) {
+        cudaFree(bufs[j]);
+        if (cudaMalloc(&bufs[j], ne * sizeof(double)) != cudaSuccess) {
+          rc = set_error(ctx, GB_ENOMEM, "plain buffer");
+          break;
+        }
+        buf_elems[j] = ne;
+      }
+      cudaError_t e = launch_plain(b->d_items + i, (long long)ne, b->plain_loop_axis[i], ctx->pool.d_v,
+                                   ctx->pool.d_w, ctx->d_dir, bufs[j], s);
+      if (e != cudaSuccess) rc = cuda_fail(ctx, e, "plain kernel");
+    }
+    // get(): reduce + D2H + sync, one integral at a time
+    for (int j = 0; j < m && rc == GB_OK; ++j) {
+      const int i = i0 + j;
+      const int si = i % S;
+      cudaStream_t s = ctx->pool_streams[si];
+      const size_t ne = (size_t)b->plain_threads[i];
+      size_t need = 0;
+      cub::DeviceReduce::Sum(nullptr, need, bufs[j], ctx->plain_res + si, (int)ne, s);
+      if (tmp_bytes[j] < need) {
+        cudaFree(tmps[j]);
+        if (cudaMalloc(&tmps[j], need) != cudaSuccess) {
+          rc = set_error(ctx, GB_ENOMEM, "cub temp");
+          break;
+        }
+        tmp_bytes[j] = need;
+      }
+      cudaError_t e = cub::DeviceReduce::Sum(tmps[j], need, bufs[j], ctx->plain_res + si, (int)ne, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->plain_res_h + si, ctx->plain_res + si, sizeof(double),
+                                                cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) {
+        rc = cuda_fail(ctx, e, "plain reduce");
+        break;
+      }
+      host_out[i] = b->src[i].args[0] + ctx->plain_res_h[si];
+    }
+    i0 = i1;
+  }
+  cudaDeviceSynchronize();
+  for (size_t j = 0; j < bufs.size(); ++j) {
+    cudaFree(bufs[j]);
+    cudaFree(tmps[j]);
+  }
+  return rc;
+}
+
+int gb_get(gb_ctx *ctx, const gb_integral *item, gb_table *const *tables, int n_tables, int precision, double *out)
+{
+  if (!ctx || !item || !out) return GB_EINVAL;
+  gb_batch *b = nullptr;
+  int rc = build_batch(ctx, item, 1, tables, n_tables, precision, &b);
+  if (rc) return rc;
+  rc = gb_batch_get(ctx, b, out, nullptr);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaStreamSynchronize(ctx->stream);
+  free_batch(ctx, b);
+  return rc;
+}
+
+// ------------------------------------------------------------------ serving
+int gb_serve_start(gb_ctx *ctx, int max_inflight, int max_items) { return serve_start(ctx, max_inflight, max_items); }
+int gb_serve_stop(gb_ctx *ctx) { return serve_stop(ctx); }
+int gb_submit(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
+              gb_ticket *out)
+{
+  return serve_submit(ctx, items, n, tables, n_tables, precision, out);
+}
+int gb_poll(gb_ctx *ctx, gb_ticket t, double *out) { return serve_poll(ctx, t, out, false, 0.0); }
+int gb_wait(gb_ctx *ctx, gb_ticket t, double *out, double timeout_s) { return serve_poll(ctx, t, out, true, timeout_s); }
+int gb_cancel(gb_ctx *ctx, gb_ticket t) { return serve_cancel(ctx, t); }
+int gb_get_stats(gb_ctx *ctx, gb_stats *out) { return serve_stats(ctx, out); }
+int gb_reset_stats(gb_ctx *ctx) { return serve_reset_stats(ctx); }
+
+int gb_measure_peaks(gb_ctx *ctx, double *fp32_tflops, double *mufu_gops, double *fp64_tflops)
+{
+  if (!ctx) return GB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  GB_CUDA(cudaSetDevice(ctx->device));
+  void *buf = nullptr;
+  GB_CUDA(cudaMalloc(&buf, 64));
+  cudaEvent_t e0, e1;
+  GB_CUDA(cudaEventCreate(&e0));
+  GB_CUDA(cudaEventCreate(&e1));
+  cudaStream_t s = ctx->stream;
+  const int threads = 256, ctas = ctx->num_sms * 8;
+  auto timeit = [&](int which, int iters, double &ms) -> int {
+    for (int rep = 0; rep < 2; ++rep) {  // warm-up + timed
+      GB_CUDA(cudaEventRecord(e0, s));
+      cudaError_t e = which == 0   ? launch_peak_ffma((float *)buf, ctas, threads, iters, s)
+                      : which == 1 ? launch_peak_mufu((float *)buf, ctas, threads, iters, s)
+                                   : launch_peak_dfma((double *)buf, ctas, threads, iters, s);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "peak probe");
+      GB_CUDA(cudaEventRecord(e1, s));
+      GB_CUDA(cudaEventSynchronize(e1));
+      float f = 0;
+      GB_CUDA(cudaEventElapsedTime(&f, e0, e1));
+      ms = f;
+    }
+    return GB_OK;
+  };
+  const double nthreads = (double)threads * ctas;
+  double ms = 0;
+  int rc = timeit(0, 4096, ms);
+  if (!rc && fp32_tflops) *fp32_tflops = nthreads * 4096.0 * 16 * 8 * 2 / (ms * 1e-3) / 1e12;
+  if (!rc) rc = timeit(1, 2048, ms);
+  if (!rc && mufu_gops) *mufu_gops = nthreads * 2048.0 * 4 * 8 / (ms * 1e-3) / 1e9;
+  if (!rc) rc = timeit(2, 64, ms);
+  if (!rc && fp64_tflops) *fp64_tflops = nthreads * 64.0 * 4 * 8 * 2 / (ms * 1e-3) / 1e12;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  return rc;
+}
+
+} // extern "C"

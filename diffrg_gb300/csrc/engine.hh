@@ -1,0 +1,158 @@
+// engine.hh -- host-side internals of libgbint (context, provider caches, node pool, batches).
+#pragma once
+
+#include <atomic>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "engine_types.hh"
+#include "gbint.h"
+#include "host_quadrature.hh"
+
+namespace gbint
+{
+  // cache key of one quadrature axis (kind + order + the parameters its nodes depend on)
+  struct AxisKey {
+    int kind = 0;
+    int n = 0;
+    double p[7] = {0, 0, 0, 0, 0, 0, 0};
+    bool operator<(const AxisKey &o) const
+    {
+      if (kind != o.kind) return kind < o.kind;
+      if (n != o.n) return n < o.n;
+      return std::memcmp(p, o.p, sizeof(p)) < 0;
+    }
+  };
+
+  struct HostAxis {
+    std::vector<double> v, w, a;
+    int pm_from = 1 << 30;
+  };
+
+  struct GLRule {
+    std::vector<double> x, w;
+    double *d64x = nullptr, *d64w = nullptr;
+    float *d32x = nullptr, *d32w = nullptr;
+  };
+  struct MatsEntry {
+    double T, E;
+    MatsRule rule;
+    double *d64x = nullptr, *d64w = nullptr;
+    float *d32x = nullptr, *d32w = nullptr;
+  };
+
+  // device pool of axis nodes (FP64 arrays + 32-byte FP32 records); offsets never move
+  struct NodePool {
+    int capacity = 0, used = 0;
+    double *d_v = nullptr, *d_w = nullptr, *d_a = nullptr;
+    NodeRec *d_rec = nullptr;
+  };
+
+  struct Ticket;
+  struct ServeState;
+} // namespace gbint
+
+struct gb_table {
+  int slot = -1;
+  gb_table_spec spec{};
+  float *buf[2] = {nullptr, nullptr};
+  int front = 0;
+  uint64_t epoch = 0;
+  int elems = 0;
+  int bytes = 0;  // padded to 16
+};
+
+struct gb_batch {
+  int n = 0;
+  int precision = GB_PREC_FP32C;
+  std::vector<gb_integral> src;
+  std::vector<gbint::ItemDev> items;
+  std::vector<gbint::UnitDev> units;
+  std::vector<gbint::SegDev> segs;
+  struct KindRun {
+    int kind = 0;
+    int unit_begin = 0, n_units = 0;
+    int threads = 0, ctas = 0, tab_cap = 0, rec_cap = 0;
+  };
+  std::vector<KindRun> runs;
+  std::vector<int> plain_loop_axis;
+  std::vector<long long> plain_threads;
+  int seg_max_entries = 0;
+  size_t seg_total = 0;
+  uint64_t points = 0;
+  // device
+  gbint::ItemDev *d_items = nullptr;
+  gbint::UnitDev *d_units = nullptr;
+  gbint::SegDev *d_segs = nullptr;
+  double *d_seg = nullptr;
+  double *d_partials = nullptr;
+  int *d_item_count = nullptr;
+  int *d_counters = nullptr;  // one per kind run
+  double *d_out = nullptr;
+  size_t bytes = 0;
+  // graph replay
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+};
+
+struct gb_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<cudaStream_t> pool_streams;
+  std::recursive_mutex mu;
+  size_t budget = 0;
+  std::atomic<size_t> in_use{0};
+  std::string last_error;
+  // provider
+  int mats_min = 32, mats_vacuum = 48, mats_add = 0;
+  std::map<int, gbint::GLRule> gl;
+  std::vector<std::unique_ptr<gbint::MatsEntry>> mats;
+  // nodes
+  gbint::NodePool pool;
+  std::map<gbint::AxisKey, gbint::AxisRef> axis_cache;
+  // tables
+  gbint::TableDev *d_dir = nullptr;
+  std::vector<gbint::TableDev> h_dir;
+  std::vector<gb_table *> slots;
+  int *d_err = nullptr;
+  // kind -> thread override (autotuner)
+  int threads_override[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // plain-path scratch
+  std::vector<double *> plain_buf;
+  std::vector<size_t> plain_buf_elems;
+  std::vector<void *> plain_tmp;
+  std::vector<size_t> plain_tmp_bytes;
+  double *plain_res = nullptr;     // device, per stream
+  double *plain_res_h = nullptr;   // pinned host
+  // serving
+  gbint::ServeState *serve = nullptr;
+};
+
+namespace gbint
+{
+  int set_error(gb_ctx *ctx, int code, const std::string &msg);
+  int cuda_fail(gb_ctx *ctx, cudaError_t e, const char *what);
+  int build_batch(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
+                  gb_batch **out);
+  int run_batch(gb_ctx *ctx, gb_batch *b, double *d_out, cudaStream_t s);
+  void free_batch(gb_ctx *ctx, gb_batch *b);
+  // serving
+  int serve_start(gb_ctx *ctx, int max_inflight, int max_items);
+  int serve_stop(gb_ctx *ctx);
+  int serve_submit(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
+                   gb_ticket *out);
+  int serve_poll(gb_ctx *ctx, gb_ticket t, double *out, bool wait, double timeout_s);
+  int serve_cancel(gb_ctx *ctx, gb_ticket t);
+  int serve_stats(gb_ctx *ctx, gb_stats *out);
+  int serve_reset_stats(gb_ctx *ctx);
+} // namespace gbint

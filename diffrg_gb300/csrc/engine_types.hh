@@ -1,0 +1,109 @@
+// engine_types.hh -- device-visible data layout of the gbint engine.
+//
+// Every integrator family of the reference is a tensor product of at most four quadrature
+// axes.  The host turns each axis into a node array (value, weight) with the reference's
+// maps and Jacobians folded in (x -> q = k sqrt(x x_extent), cos = 2(t-1/2), phi = 2 pi t,
+// int_element, Matsubara or explicit-sum weights), so the device evaluates
+//     constant + sum_{i0..i3} w0[i0] w1[i1] w2[i2] w3[i3] * KERNEL(v0[i0], v1[i1], ...)
+// with every "q0" axis evaluated at +-v (nodes before pm_from are evaluated once).
+#pragma once
+
+#include <cstdint>
+
+#include "gbint.h"
+#include "gbint/device/numerics.cuh"
+
+namespace gbint
+{
+  // coordinate an axis feeds into the kernel
+  enum Role : int { R_NONE = 0, R_Q = 1, R_C1 = 2, R_C2 = 3, R_PHI = 4, R_Q0 = 5, R_QX = 6, R_QY = 7, R_QZ = 8 };
+
+  // 32-byte node record for FP32 kernels, every field a double-float pair:
+  // v = coordinate, w = weight, a = auxiliary value (sqrt(1 - v^2) on cos axes, cos(v) on phi
+  // axes, v^2 on radial axes), aw = w * a.
+  struct alignas(32) NodeRec {
+    float v_hi, v_lo, w_hi, w_lo, a_hi, a_lo, aw_hi, aw_lo;
+  };
+
+  struct AxisRef {
+    int off;      // node index into the pools
+    int n;        // nodes
+    int role;     // Role
+    int pm_from;  // nodes >= pm_from are evaluated at +v and -v
+  };
+
+  // kernel kinds
+  enum Kind : int {
+    K_GENERIC = 0,  // any family x any integrand, FP64, thread per point
+    K_S1 = 1,       // 2-axis (q, c) + PROP1, FP32c: rows q, inner c
+    K_S2 = 2,       // (mode, q, c) + FTLOOP, FP32c: rows (mode, q), inner c
+    K_S3 = 3,       // (q, c, phi) + PROP3, FP32c: rows (q, c), inner phi
+    K_S5 = 5        // (q, c1, c2, phi) + VERT4, FP32c: rows (q, c1), mid c2, inner phi
+  };
+
+  struct ItemDev {
+    int kind;
+    int integrand;
+    int family;
+    int n_axes;
+    int rows;        // rows (S kinds) or points (generic)
+    AxisRef ax[4];
+    int unit_begin;
+    int n_units;
+    int seg_off;     // hoisted FP64 factors (S kinds)
+    int seg_stride;  // row stride inside the segment
+    int tab[4];      // table directory slots
+    int pad;
+    double k;
+    double args[GB_MAX_ARGS];
+  };
+
+  struct UnitDev {
+    int item;
+    int row_begin;
+    int row_count;
+    int pad;
+  };
+
+  // table directory entry (device): current FP32 data + axes
+  struct TableDev {
+    const float *data;
+    int n0, n1;  // n1 == 0: 1D
+    int bytes;   // data bytes (multiple of 16)
+    int pad;
+    dev::AxisDev a0, a1;
+  };
+
+  constexpr int kMaxTables = 256;
+
+  struct RunParams {
+    const ItemDev *items;
+    const UnitDev *units;
+    int n_units;
+    int n_items;
+    const double *pv;      // FP64 node values
+    const double *pw;      // FP64 node weights
+    const double *pa;      // FP64 aux values
+    const NodeRec *prec;   // FP32 records
+    const TableDev *tabs;  // directory
+    const double *seg;     // hoisted factors
+    double *partials;      // per unit
+    int *item_count;       // per item arrival counters (reset by the finisher)
+    int *unit_counter;     // work-stealing counter (reset by the finisher of the run)
+    int *done_counter;     // items finished in this run
+    double *out;           // per item results
+    int *err;              // device error word
+  };
+
+  // hoisted-factor segment kinds
+  enum SegKind : int { SEG_S1 = 1, SEG_S2 = 2, SEG_S3 = 3, SEG_S5 = 5 };
+  struct SegDev {
+    int kind;
+    int off;       // output offset
+    int n0, n1;    // entries = n0 * n1
+    AxisRef ax0, ax1;
+    int tab;       // table slot
+    int pad;
+    double par[4];
+  };
+} // namespace gbint

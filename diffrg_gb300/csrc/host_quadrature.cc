@@ -1,0 +1,168 @@
+// host_quadrature.cc -- see host_quadrature.hh.
+#include "host_quadrature.hh"
+
+#include <algorithm>
+#include <cmath>
+#include <stdexcept>
+
+namespace gbint
+{
+  namespace
+  {
+    const long double kPiL = 3.141592653589793238462643383279502884L;
+
+    // P_n(z) and P_{n-1}(z) by the Bonnet recurrence
+    inline void legendre_pair(int n, long double z, long double &pn, long double &pn1)
+    {
+      long double p0 = 1, p1 = z;
+      if (n == 0) {
+        pn = 1;
+        pn1 = 0;
+        return;
+      }
+      for (int j = 2; j <= n; ++j) {
+        const long double p2 = ((2 * j - 1) * z * p1 - (j - 1) * p0) / j;
+        p0 = p1;
+        p1 = p2;
+      }
+      pn = p1;
+      pn1 = p0;
+    }
+
+    // number of eigenvalues of the Jacobi matrix below lambda (Sturm count of the LDL^T pivots)
+    int sturm_count(const std::vector<long double> &a, const std::vector<long double> &b, long double lambda)
+    {
+      const int n = (int)a.size();
+      int cnt = 0;
+      long double d = 1;
+      for (int i = 0; i < n; ++i) {
+        const long double off = i > 0 ? b[i - 1] : 0.0L;
+        d = (a[i] - lambda) - (i > 0 ? off / d : 0.0L);
+        if (d == 0) d = -1e-300L;
+        if (d < 0) ++cnt;
+      }
+      return cnt;
+    }
+  } // namespace
+
+  void gl_rule01(int n, std::vector<double> &x, std::vector<double> &w)
+  {
+    if (n <= 0) throw std::invalid_argument("Gauss-Legendre order must be positive");
+    x.assign(n, 0.0);
+    w.assign(n, 0.0);
+    const int half = (n + 1) / 2;
+    for (int i = 0; i < half; ++i) {
+      // i-th largest root; initial guess from the asymptotic formula
+      long double z = std::cos(kPiL * (4 * i + 3) / (4 * n + 2));
+      long double pn = 0, pn1 = 0;
+      for (int it = 0; it < 64; ++it) {
+        legendre_pair(n, z, pn, pn1);
+        const long double dp = n * (pn1 - z * pn) / (1 - z * z);
+        const long double step = pn / dp;
+        z -= step;
+        if (std::fabs(step) <= 4 * std::numeric_limits<long double>::epsilon()) break;
+      }
+      legendre_pair(n, z, pn, pn1);
+      const long double dp = n * (pn1 - z * pn) / (1 - z * z);
+      const long double wt = 1 / ((1 - z * z) * dp * dp);  // weight on [0,1] = half of [-1,1]'s
+      x[n - 1 - i] = (double)((1 + z) / 2);
+      x[i] = (double)((1 - z) / 2);
+      w[n - 1 - i] = (double)wt;
+      w[i] = (double)wt;
+    }
+    if (n % 2 == 1) x[n / 2] = 0.5;
+  }
+
+  void jacobi_gauss(const std::vector<long double> &a, const std::vector<long double> &b, long double mu0,
+                    std::vector<long double> &x, std::vector<long double> &w)
+  {
+    const int n = (int)a.size();
+    if ((int)b.size() != n) throw std::invalid_argument("jacobi_gauss: size mismatch");
+    x.assign(n, 0);
+    w.assign(n, 0);
+    // Gershgorin interval
+    long double lo = a[0], hi = a[0];
+    for (int i = 0; i < n; ++i) {
+      long double r = 0;
+      if (i > 0) r += std::sqrt(b[i - 1]);
+      if (i + 1 < n) r += std::sqrt(b[i]);
+      lo = std::min(lo, a[i] - r);
+      hi = std::max(hi, a[i] + r);
+    }
+    for (int k = 0; k < n; ++k) {
+      long double l = lo, h = hi;
+      for (int it = 0; it < 200; ++it) {
+        const long double m = (l + h) / 2;
+        if (m == l || m == h) break;
+        if (sturm_count(a, b, m) > k)
+          h = m;
+        else
+          l = m;
+      }
+      const long double lam = (l + h) / 2;
+      x[k] = lam;
+      // Christoffel weights from the orthonormal recurrence
+      long double p_prev = 0, p = 1, s = 1;
+      for (int j = 0; j + 1 < n; ++j) {
+        const long double beta = std::sqrt(b[j]);
+        const long double pn = ((lam - a[j]) * p - (j > 0 ? std::sqrt(b[j - 1]) : 0.0L) * p_prev) / beta;
+        p_prev = p;
+        p = pn;
+        s += p * p;
+      }
+      w[k] = mu0 / s;
+    }
+  }
+
+  MatsRule matsubara_rule(double T, double E, int step, int min_size, int max_size, int vacuum_quad_size,
+                          int precision_factor)
+  {
+    MatsRule r;
+    if (precision_factor < 0) precision_factor = 1;
+    if (vacuum_quad_size <= 6) vacuum_quad_size = 6;
+    const bool T_zero = std::fabs(T) <= 1e-12;
+    const double rel = std::fabs(E) / std::fabs(T + 1e-16);
+    if (T_zero || rel > 1e2) {
+      // vacuum: GL split into a linear part on [0, 2|E|] and a log part on [2|E|, 1e6 |E|]
+      int m = vacuum_quad_size;
+      if (m % 2) ++m;
+      const double Ee = std::fabs(E) <= 1e-300 ? 1.0 : std::fabs(E);
+      std::vector<double> gx, gw;
+      gl_rule01(m / 2, gx, gw);
+      r.T_rule = 0;
+      r.x.resize(m);
+      r.w.resize(m);
+      const long double div = 2.0L * Ee, ext = 1e6L * Ee;
+      const long double ls = std::log(div), le = std::log(ext / div);
+      const double tp = 2.0 * (double)kPiL;
+      for (int i = 0; i < m / 2; ++i) {
+        r.x[i] = gx[i] * (double)div;
+        r.w[i] = gw[i] * (double)div / tp;
+        const double xv = (double)std::exp(ls + le * (long double)gx[i]);
+        r.x[i + m / 2] = xv;
+        r.w[i + m / 2] = gw[i] * (double)le * xv / tp;
+      }
+      return r;
+    }
+    const double E_max = (precision_factor + 100) * std::fabs(E);
+    int m = 5 + int(std::sqrt(4 * E_max / ((double)(kPiL * kPiL) * std::fabs(T))));
+    m = (int)std::ceil(m / (double)step) * step;
+    m = std::max(min_size, std::min(max_size, m));
+    std::vector<long double> a(m), b(m), xs, ws;
+    for (int j = 0; j < m; ++j) {
+      const long double j1 = j + 1;
+      a[j] = 2 * kPiL * kPiL / ((4 * j + 1) * (long double)(4 * j + 5));
+      b[j] = kPiL * kPiL * kPiL * kPiL / ((4 * j1 - 1) * (4 * j1 + 3)) / ((4 * j1 + 1) * (4 * j1 + 1));
+    }
+    a[0] = kPiL * kPiL / 15;
+    jacobi_gauss(a, b, kPiL * kPiL / 6, xs, ws);
+    r.T_rule = T;
+    r.x.resize(m);
+    r.w.resize(m);
+    for (int i = 0; i < m; ++i) {
+      r.w[i] = (double)((long double)T * ws[i] / xs[i]);
+      r.x[i] = (double)(2 * kPiL * (long double)T / std::sqrt(xs[i]));
+    }
+    return r;
+  }
+} // namespace gbint

@@ -1,0 +1,43 @@
+// kernels.hh -- host-side launchers of the gbint kernels (implemented in kernels_*.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "engine_types.hh"
+
+namespace gbint
+{
+  struct KernelShape {
+    int threads;  // CTA size (= rows per unit for S kinds)
+    int ctas;     // persistent grid size
+    size_t smem;  // dynamic shared memory bytes
+  };
+
+  // generic FP64 kernel: points per unit
+  constexpr int kGenericThreads = 256;
+  constexpr int kGenericPPT = 4;
+  constexpr int kGenericUnitPoints = kGenericThreads * kGenericPPT;
+
+  // shape of a kind for this device (num SMs, smem opt-in); threads may be overridden (autotuner)
+  KernelShape kernel_shape(int kind, int num_sms, int threads_override);
+  int kind_rows_per_unit(int kind, int threads_override);
+
+  cudaError_t launch_generic(const RunParams &P, int ctas, cudaStream_t s);
+  cudaError_t launch_seg(const SegDev *segs, int n_segs, int total_entries, const double *pv, const double *pw,
+                         const double *pa, const TableDev *tabs, double *seg_out, cudaStream_t s);
+  // FP32-compensated persistent kernels (kinds K_S1..K_S5); threads in {128, 256, 512}
+  cudaError_t launch_fp32c(int kind, const RunParams &P, int threads, int ctas, int tab_bytes_cap, int rec_cap,
+                           cudaStream_t s);
+  // resident CTAs per SM for that configuration (0 if it cannot launch)
+  int fp32c_occupancy(int kind, int threads, int tab_bytes_cap, int rec_cap);
+  int kind_default_threads(int kind);
+
+  // reference execution pattern: one value per (row of) point(s) into dest
+  cudaError_t launch_plain(const ItemDev *item_dev, long long n_threads, int loop_axis, const double *pv,
+                           const double *pw, const TableDev *tabs, double *dest, cudaStream_t s);
+
+  // plain FFMA / MUFU throughput probes (peaks for the roofline)
+  cudaError_t launch_peak_ffma(float *out, int ctas, int threads, int iters, cudaStream_t s);
+  cudaError_t launch_peak_mufu(float *out, int ctas, int threads, int iters, cudaStream_t s);
+  cudaError_t launch_peak_dfma(double *out, int ctas, int threads, int iters, cudaStream_t s);
+} // namespace gbint

@@ -1,0 +1,470 @@
+// kernels_fp32c.cu -- FP32-compensated persistent kernels for the catalogue workloads.
+//
+// Structure shared by all kinds (one CTA per SM slot, persistent):
+//   * the CTA's dressing tables are staged into shared memory once by non-tensor TMA bulk
+//     copies (cp.async.bulk + mbarrier complete_tx) and restaged only when an item uses others;
+//   * work units (item, 'rows' range) are taken from an atomic counter; the node records of the
+//     unit's inner axes are TMA-prefetched into a second buffer while the current unit computes;
+//   * one thread per row loops over the inner axes in FP32 with double-float constants and a
+//     Kahan sum, multiplies by the row's hoisted FP64 factor and the unit is reduced in FP64;
+//   * the last unit of an item sums the item's unit partials in a fixed order (deterministic).
+// Tensor cores are not used: this is a reduction, not a dense contraction.
+#include "device_common.cuh"
+#include "integrands.cuh"
+#include "kernels.hh"
+
+#include <algorithm>
+
+namespace gbint
+{
+  using namespace dev;
+
+  namespace
+  {
+    // A + B*c with A, B, c double-float, rounded once to FP32
+    __device__ __forceinline__ float lin_df(df A, df B, float c_hi, float c_lo)
+    {
+      const df p = two_prod(B.hi, c_hi);
+      const df s = two_sum(A.hi, p.hi);
+      const float corr = __fadd_rn(__fadd_rn(s.lo, A.lo), __fmaf_rn(B.hi, c_lo, __fmaf_rn(B.lo, c_hi, p.lo)));
+      return __fadd_rn(s.hi, corr);
+    }
+    __device__ __forceinline__ df df_neg(df a) { return df{-a.hi, -a.lo}; }
+    __device__ __forceinline__ df df_scale2(df a, float s) { return df{a.hi * s, a.lo * s}; }  // s a power of 2
+    __device__ __forceinline__ df dfc(double v) { return df_from(v); }
+
+    // fractional index on a linear axis for a double-float coordinate
+    __device__ __forceinline__ float axis_frac_lin_df(const AxisDev &a, df v, int &i)
+    {
+      const df u = df_add(df_mul(a.scale, v), a.shift);
+      const float ur = __fadd_rn(u.hi, u.lo);
+      if (!(ur > 0.f)) {
+        i = 0;
+        return 0.f;
+      }
+      if (ur >= (float)(a.n - 1)) {
+        i = a.n - 2;
+        return 1.f;
+      }
+      int ii = (int)floorf(ur);
+      float f = __fadd_rn(__fsub_rn(u.hi, (float)ii), u.lo);
+      if (f < 0.f) {
+        ii -= 1;
+        f = __fadd_rn(__fsub_rn(u.hi, (float)ii), u.lo);
+      }
+      if (ii > a.n - 2) {
+        ii = a.n - 2;
+        f = 1.f;
+      }
+      i = ii;
+      return fminf(fmaxf(f, 0.f), 1.f);
+    }
+
+    __device__ __forceinline__ float tab1_32(const float *d, const AxisDev &a, float x)
+    {
+      int i;
+      const float f = axis_frac(a, x, i);
+      return lerp32(d[i], d[i + 1], f);
+    }
+    // bilinear: lerp along axis 0 at columns j, j+1, then along axis 1
+    __device__ __forceinline__ float bil32(const float *d, int n1, int i, float fx, int j, float fy)
+    {
+      const float *r0 = d + i * n1 + j;
+      const float *r1 = r0 + n1;
+      const float lo = lerp32(r0[0], r1[0], fx);
+      const float hi = lerp32(r0[1], r1[1], fx);
+      return lerp32(lo, hi, fy);
+    }
+    __device__ __forceinline__ float rcp32(float x) { return __frcp_rn(x); }
+
+    // ---------------------------------------------------------------- per-kind traits
+    template <int KIND> struct Traits;
+    template <> struct Traits<K_S1> {
+      static constexpr int kTables = 1;
+    };
+    template <> struct Traits<K_S2> {
+      static constexpr int kTables = 1;
+    };
+    template <> struct Traits<K_S3> {
+      static constexpr int kTables = 4;
+    };
+    template <> struct Traits<K_S5> {
+      static constexpr int kTables = 2;
+    };
+
+    // records a unit needs: (axis index, count) pairs staged back to back
+    __device__ __forceinline__ int rec_axes(int kind, const ItemDev &it, int &a0, int &a1)
+    {
+      switch (kind) {
+      case K_S1:
+        a0 = 1;
+        a1 = -1;
+        return it.ax[1].n;
+      case K_S2:
+        a0 = 2;
+        a1 = -1;
+        return it.ax[2].n;
+      case K_S3:
+        a0 = 2;
+        a1 = -1;
+        return it.ax[2].n;
+      case K_S5:
+        a0 = 2;
+        a1 = 3;
+        return it.ax[2].n + it.ax[3].n;
+      }
+      a0 = a1 = -1;
+      return 0;
+    }
+
+    __device__ __forceinline__ void issue_records(int kind, const RunParams &P, int unit, NodeRec *dst,
+                                                  uint64_t *bar)
+    {
+      const ItemDev &it = P.items[P.units[unit].item];
+      int a0, a1;
+      const int n = rec_axes(kind, it, a0, a1);
+      mbar_expect_tx(bar, (uint32_t)(n * sizeof(NodeRec)));
+      tma_bulk_g2s(dst, P.prec + it.ax[a0].off, (uint32_t)(it.ax[a0].n * sizeof(NodeRec)), bar);
+      if (a1 >= 0) tma_bulk_g2s(dst + it.ax[a0].n, P.prec + it.ax[a1].off, (uint32_t)(it.ax[a1].n * sizeof(NodeRec)), bar);
+    }
+
+    __device__ __forceinline__ df rec_v(const NodeRec &r) { return df{r.v_hi, r.v_lo}; }
+    __device__ __forceinline__ df rec_a(const NodeRec &r) { return df{r.a_hi, r.a_lo}; }
+    __device__ __forceinline__ df rec_w(const NodeRec &r) { return df{r.w_hi, r.w_lo}; }
+
+    // ---------------------------------------------------------------- S1: (q, c) x PROP1
+    // row = q node i; inner = c nodes; hoisted F_i = w_q kfac G(q^2) Rdot(q^2) (FP64)
+    __device__ __forceinline__ double row_s1(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
+                                             const float *tab, const TableDev *sT)
+    {
+      const NodeRec qr = P.prec[it.ax[0].off + row];
+      const double p = it.args[1];
+      const df A = df_add(rec_a(qr), dfc(p * p));
+      const df B = df_mul(dfc(2.0 * p), rec_v(qr));
+      const AxisDev ax = sT[0].a0;
+      Kahan k;
+      const int nc = it.ax[1].n;
+#pragma unroll 2
+      for (int l = 0; l < nc; ++l) {
+        const NodeRec r = rc[l];
+        const float x2 = fmaxf(lin_df(A, B, r.v_hi, r.v_lo), 1e-30f);
+        const float z = tab1_32(tab, ax, x2);
+        const float g = rcp32(__fmaf_rn(z, x2, reg_R(x2)));
+        k.add(__fmaf_rn(r.aw_hi, g, __fmul_rn(r.aw_lo, g)));
+      }
+      return P.seg[it.seg_off + row] * k.value();
+    }
+
+    // ---------------------------------------------------------------- S2: (mode, q, c) x FTLOOP
+    // row = (mode m, q node i); inner = c nodes, each at +w_m and (m >= pm_from) -w_m;
+    // hoisted F_{m,i} = w_m w_q Rdot(q^2) G(w_m, q^2) (FP64)
+    __device__ __forceinline__ double row_s2(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
+                                             const float *tab, const TableDev *sT)
+    {
+      const int nq = it.ax[1].n;
+      const int m = row / nq, i = row - m * nq;
+      const NodeRec qr = P.prec[it.ax[1].off + i];
+      const double p = it.args[1], T = it.args[2], Om = it.args[3];
+      const double w = P.pv[it.ax[0].off + m];
+      const bool pm = m >= it.ax[0].pm_from;
+      const df A = df_add(rec_a(qr), dfc(p * p));
+      const df B = df_mul(dfc(2.0 * p), rec_v(qr));
+      const TableDev &Z = sT[0];
+      AxisDev axq = Z.a1;  // |q| axis, fed with log2(x2) -> halve the scale
+      axq.scale.hi *= 0.5f;
+      axq.scale.lo *= 0.5f;
+      const int n1 = Z.n1;
+      const double inv2piT = 1.0 / (2.0 * 3.14159265358979323846 * T);
+      // per sign: table row index/fraction (FP64 -> exact enough), w^2 as double-float
+      int j0[2];
+      float fy0[2];
+      df w2[2];
+      const int ns = pm ? 2 : 1;
+      for (int s = 0; s < 2; ++s) {
+        const double ws = (s == 0 ? w : -w) + Om;
+        int jj;
+        fy0[s] = (float)axis_frac64(Z.a0, fabs(ws) * inv2piT, jj);
+        j0[s] = jj;
+        w2[s] = dfc(ws * ws);
+      }
+      Kahan k;
+      const int nc = it.ax[2].n;
+#pragma unroll 1
+      for (int l = 0; l < nc; ++l) {
+        const NodeRec r = rc[l];
+        const float x2 = fmaxf(lin_df(A, B, r.v_hi, r.v_lo), 1e-30f);
+        int jq;
+        const float fq = axis_frac(axq, x2, jq);
+        const float R = reg_R(x2);
+        float gsum = 0.f;
+        for (int s = 0; s < ns; ++s) {
+          // Z[(mode cell j0) .. +1][(|q| cell jq) .. +1]
+          const float z = bil32(tab, n1, j0[s], fy0[s], jq, fq);
+          const float den = __fmaf_rn(z, __fadd_rn(__fadd_rn(w2[s].hi, x2), w2[s].lo), R);
+          gsum = __fadd_rn(gsum, rcp32(den));
+        }
+        k.add(__fmaf_rn(r.w_hi, gsum, __fmul_rn(r.w_lo, gsum)));
+      }
+      return P.seg[it.seg_off + row] * k.value();
+    }
+
+    // ---------------------------------------------------------------- S3: (q, c, phi) x PROP3
+    // row = (q node i, c node j); inner = phi nodes; hoisted F_i = w_q Rdot(q^2) G_A(q^2) (FP64)
+    __device__ __forceinline__ double row_s3(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
+                                             const float *tab, const TableDev *sT, const int *toff)
+    {
+      const int nc = it.ax[1].n;
+      const int i = row / nc, j = row - i * nc;
+      const NodeRec qr = P.prec[it.ax[0].off + i];
+      const NodeRec cr = P.prec[it.ax[1].off + j];
+      const double Pm = it.args[1], ct = it.args[2], st = it.args[3];
+      const df q2 = rec_a(qr);
+      const df qP = df_mul(rec_v(qr), dfc(Pm));
+      const df X = df_mul(qP, df_mul(rec_v(cr), dfc(ct)));      // q P c cos(th)
+      const df q2pp = df_add(q2, dfc(Pm * Pm));
+      const df A = df_add(q2pp, df_scale2(df_neg(X), 2.f));       // |q-p|^2 at cos(phi) = 0
+      const df Ap = df_add(df_add(q2, dfc(0.25 * Pm * Pm)), df_neg(X));
+      const df B = df_scale2(df_neg(df_mul(qP, df_mul(rec_a(cr), dfc(st)))), 2.f);  // -2 q P s sin(th)
+      const df Bh = df_scale2(B, 0.5f);
+      const df third = dfc(1.0 / 3.0);
+      const float sb = df_round(df_mul(q2pp, third));
+      const float *TB = tab + toff[1], *TC = tab + toff[2], *TD = tab + toff[3];
+      const AxisDev aB = sT[1].a0, aC = sT[2].a0, aD = sT[3].a0;
+      Kahan k;
+      const int nf = it.ax[2].n;
+#pragma unroll 1
+      for (int l = 0; l < nf; ++l) {
+        const NodeRec r = rc[l];  // a = cos(phi), w = 2 pi w_phi
+        const float r2 = fmaxf(lin_df(A, B, r.a_hi, r.a_lo), 1e-30f);
+        const float t2 = fmaxf(lin_df(Ap, Bh, r.a_hi, r.a_lo), 1e-30f);
+        const float sv = __fmaf_rn(r2, third.hi, __fmaf_rn(r2, third.lo, sb));
+        const float gB = rcp32(__fmaf_rn(tab1_32(TB, aB, r2), r2, reg_R(r2)));
+        const float g = gB * tab1_32(TC, aC, sv) * tab1_32(TD, aD, t2);
+        k.add(__fmaf_rn(r.w_hi, g, __fmul_rn(r.w_lo, g)));
+      }
+      return P.seg[it.seg_off + i] * P.pw[it.ax[1].off + j] * k.value();
+    }
+
+    // ---------------------------------------------------------------- S5: (q, c1, c2, phi) x VERT4
+    // row = (q node i, c1 node j); mid = c2 nodes; inner = phi nodes;
+    // hoisted F_ij = w_q w_c1 Rdot(q^2) G(q^2, c1) (FP64)
+    __device__ __forceinline__ double row_s5(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
+                                             const float *tab, const TableDev *sT, const int *toff)
+    {
+      const int n1 = it.ax[1].n;
+      const int i = row / n1, j = row - i * n1;
+      const NodeRec qr = P.prec[it.ax[0].off + i];
+      const NodeRec cr = P.prec[it.ax[1].off + j];
+      const double Pm = it.args[1], ca = it.args[2], sa = it.args[3];
+      const df qP = df_mul(rec_v(qr), dfc(Pm));
+      const df q2pp = df_add(rec_a(qr), dfc(Pm * Pm));
+      const df c1 = rec_v(cr);
+      const df qPc1 = df_mul(qP, c1);
+      const float r1 = fmaxf(df_round(df_add(q2pp, df_scale2(df_neg(qPc1), 2.f))), 1e-30f);  // |q-p1|^2
+      const df A2 = df_add(q2pp, df_scale2(df_mul(qPc1, dfc(ca)), 2.f));
+      const df B2 = df_scale2(df_mul(qP, df_mul(rec_a(cr), dfc(sa))), 2.f);
+      const TableDev &TA = sT[0];
+      const float *DA = tab + toff[0], *DB = tab + toff[1];
+      const int tn1 = TA.n1;
+      // row-level table coordinates: x-cell of r1^2, t-cell of c1
+      int ir1;
+      const float fr1 = axis_frac(TA.a0, r1, ir1);
+      const float Rr1 = reg_R(r1);
+      int jc1;
+      const float fc1 = axis_frac_lin_df(TA.a1, c1, jc1);
+      const int n2 = it.ax[2].n, n3 = it.ax[3].n;
+      const NodeRec *rphi = rc + n2;
+      Kahan kmid;
+#pragma unroll 1
+      for (int l = 0; l < n2; ++l) {
+        const NodeRec r2r = rc[l];  // c2: v = c2, a = s2, w = 2 w_c2
+        int jc2;
+        const float fc2 = axis_frac_lin_df(TA.a1, rec_v(r2r), jc2);
+        const float gr1 = rcp32(__fmaf_rn(bil32(DA, tn1, ir1, fr1, jc2, fc2), r1, Rr1));
+        const df Bs = df_mul(B2, rec_a(r2r));
+        Kahan kin;
+#pragma unroll 2
+        for (int m = 0; m < n3; ++m) {
+          const NodeRec rp = rphi[m];  // a = cos(phi), w = 2 pi w_phi
+          const float x = fmaxf(lin_df(A2, Bs, rp.a_hi, rp.a_lo), 1e-30f);
+          int ix;
+          const float fx = axis_frac(TA.a0, x, ix);
+          const float gv = rcp32(__fmaf_rn(bil32(DA, tn1, ix, fx, jc1, fc1), x, reg_R(x)));
+          const float vv = bil32(DB, tn1, ix, fx, jc2, fc2);
+          const float g = gv * vv;
+          kin.add(__fmaf_rn(rp.w_hi, g, __fmul_rn(rp.w_lo, g)));
+        }
+        const float mt = __fmul_rn((float)kin.value(), gr1);
+        kmid.add(__fmaf_rn(r2r.w_hi, mt, __fmul_rn(r2r.w_lo, mt)));
+      }
+      return P.seg[it.seg_off + row] * kmid.value();
+    }
+
+    template <int KIND>
+    __device__ __forceinline__ double row_value(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
+                                                const float *tab, const TableDev *sT, const int *toff)
+    {
+      if constexpr (KIND == K_S1) return row_s1(P, it, row, rc, tab + toff[0], sT);
+      if constexpr (KIND == K_S2) return row_s2(P, it, row, rc, tab + toff[0], sT);
+      if constexpr (KIND == K_S3) return row_s3(P, it, row, rc, tab, sT, toff);
+      if constexpr (KIND == K_S5) return row_s5(P, it, row, rc, tab, sT, toff);
+      return 0.0;
+    }
+  } // namespace
+
+  template <int KIND, int THREADS>
+  __global__ void __launch_bounds__(THREADS) k_fp32c(const RunParams P, int tab_bytes_cap, int rec_cap)
+  {
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr int NT = Traits<KIND>::kTables;
+    float *tab_s = reinterpret_cast<float *>(smem);
+    NodeRec *rec_s0 = reinterpret_cast<NodeRec *>(smem + tab_bytes_cap);
+    NodeRec *rec_s1 = rec_s0 + rec_cap;
+    __shared__ __align__(8) uint64_t bar[3];
+    __shared__ TableDev sT[4];
+    __shared__ int s_slot[4], s_toff[4], s_next[2], s_flag;
+    __shared__ double red[32];
+
+    if (threadIdx.x == 0) {
+      mbar_init(&bar[0], 1);
+      mbar_init(&bar[1], 1);
+      mbar_init(&bar[2], 1);
+      mbar_fence_init();
+      for (int i = 0; i < 4; ++i) s_slot[i] = -2;
+      const int u = atomicAdd(P.unit_counter, 1);
+      s_next[0] = u;
+      if (u < P.n_units) issue_records(KIND, P, u, rec_s0, &bar[0]);
+    }
+    __syncthreads();
+    uint32_t ph0 = 0, ph1 = 0, ph_tab = 0;
+    int buf = 0;
+    for (;;) {
+      const int u = s_next[buf];
+      if (u >= P.n_units) break;
+      const UnitDev U = P.units[u];
+      const ItemDev &it = P.items[U.item];
+      bool ok = true;
+      bool need = false;
+#pragma unroll
+      for (int t = 0; t < NT; ++t) need |= (it.tab[t] != s_slot[t]);
+      if (need) {
+        __syncthreads();  // everyone has read s_slot
+        if (threadIdx.x == 0) {
+          int total = 0;
+          for (int t = 0; t < NT; ++t) {
+            const int slot = it.tab[t];
+            sT[t] = P.tabs[slot];
+            s_slot[t] = slot;
+            s_toff[t] = total / 4;
+            total += sT[t].bytes;
+          }
+          if (total > tab_bytes_cap) {
+            atomicOr(P.err, ERR_BAD_INDEX);
+            total = 0;
+          }
+          mbar_expect_tx(&bar[2], (uint32_t)total);
+          if (total > 0)
+            for (int t = 0; t < NT; ++t) tma_bulk_g2s(tab_s + s_toff[t], sT[t].data, (uint32_t)sT[t].bytes, &bar[2]);
+        }
+        __syncthreads();
+        ok = mbar_wait_bounded(&bar[2], ph_tab, P.err) && ok;
+        ph_tab ^= 1;
+      }
+      // prefetch the next unit's records into the other buffer
+      if (threadIdx.x == 0) {
+        const int un = atomicAdd(P.unit_counter, 1);
+        s_next[buf ^ 1] = un;
+        if (un < P.n_units) issue_records(KIND, P, un, buf ? rec_s0 : rec_s1, &bar[buf ^ 1]);
+      }
+      if (buf == 0) {
+        ok = mbar_wait_bounded(&bar[0], ph0, P.err) && ok;
+        ph0 ^= 1;
+      } else {
+        ok = mbar_wait_bounded(&bar[1], ph1, P.err) && ok;
+        ph1 ^= 1;
+      }
+      double acc = 0.0;
+      if (ok && (int)threadIdx.x < U.row_count)
+        acc = row_value<KIND>(P, it, U.row_begin + threadIdx.x, buf ? rec_s1 : rec_s0, tab_s, sT, s_toff);
+      const double tot = block_sum(acc, red);
+      unit_finish(P, u, U.item, tot, red, &s_flag);
+      buf ^= 1;
+    }
+  }
+
+  // ------------------------------------------------------------------------------------------
+  // launch plumbing
+  // ------------------------------------------------------------------------------------------
+  namespace
+  {
+    template <int KIND, int THREADS> const void *kfun() { return (const void *)&k_fp32c<KIND, THREADS>; }
+
+    const void *select(int kind, int threads)
+    {
+#define GB_SEL(K)                                     \
+  case K:                                             \
+    if (threads == 128) return kfun<K, 128>();        \
+    if (threads == 256) return kfun<K, 256>();        \
+    if (threads == 512) return kfun<K, 512>();        \
+    return nullptr;
+      switch (kind) {
+        GB_SEL(K_S1)
+        GB_SEL(K_S2)
+        GB_SEL(K_S3)
+        GB_SEL(K_S5)
+      }
+#undef GB_SEL
+      return nullptr;
+    }
+  } // namespace
+
+  int kind_default_threads(int kind)
+  {
+    switch (kind) {
+    case K_S1:
+      return 128;
+    case K_S5:
+      return 512;
+    default:
+      return 256;
+    }
+  }
+
+  int kind_rows_per_unit(int kind, int threads_override)
+  {
+    if (kind == K_GENERIC) return kGenericUnitPoints;
+    return threads_override > 0 ? threads_override : kind_default_threads(kind);
+  }
+
+  KernelShape kernel_shape(int kind, int num_sms, int threads_override)
+  {
+    KernelShape s{0, 0, 0};
+    s.threads = kind_rows_per_unit(kind, threads_override);
+    s.ctas = num_sms;
+    return s;
+  }
+
+  cudaError_t launch_fp32c(int kind, const RunParams &P, int threads, int ctas, int tab_bytes_cap, int rec_cap,
+                           cudaStream_t s)
+  {
+    const void *fn = select(kind, threads);
+    if (!fn) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)tab_bytes_cap + 2 * (size_t)rec_cap * sizeof(NodeRec);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    RunParams p = P;
+    void *args[] = {(void *)&p, (void *)&tab_bytes_cap, (void *)&rec_cap};
+    return cudaLaunchKernel(fn, dim3(ctas), dim3(threads), args, smem, s);
+  }
+
+  int fp32c_occupancy(int kind, int threads, int tab_bytes_cap, int rec_cap)
+  {
+    const void *fn = select(kind, threads);
+    if (!fn) return 0;
+    const size_t smem = (size_t)tab_bytes_cap + 2 * (size_t)rec_cap * sizeof(NodeRec);
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess) return 0;
+    return nb;
+  }
+} // namespace gbint

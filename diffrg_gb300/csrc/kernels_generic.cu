@@ -1,0 +1,256 @@
+// kernels_generic.cu -- FP64 kernels: the generic fused kernel (any family x any catalogue
+// integrand), the reference-pattern per-point kernel, the hoisted-factor (segment) kernel and
+// the FFMA/MUFU/DFMA peak probes used as roofline denominators.
+#include "device_common.cuh"
+#include "integrands.cuh"
+#include "kernels.hh"
+
+namespace gbint
+{
+  using namespace dev;
+
+  // ------------------------------------------------------------------------------------------
+  // Generic fused FP64 kernel.  Persistent CTAs take work units (item, point range) from an
+  // atomic counter; each thread evaluates kGenericPPT points of the flattened tensor grid,
+  // partials are reduced in FP64 and the last unit of an item finishes it (unit_finish).
+  // Replaces gridreduce_* + thrust::reduce (e.g. integrator_4D_gpu.hh:21-49,141-158) with one
+  // launch for a whole batch and no per-point global buffer.
+  // ------------------------------------------------------------------------------------------
+  __device__ __forceinline__ double eval_point(const ItemDev &it, long long pt, const double *pv, const double *pw,
+                                               const TableDev *T)
+  {
+    Pt P{0, 0, 0, 0, 0, 0, 0, 0, it.k};
+    double w = 1.0;
+    bool pm = false;
+    long long rem = pt;
+    for (int a = it.n_axes - 1; a >= 0; --a) {
+      const AxisRef ax = it.ax[a];
+      const int idx = (int)(rem % ax.n);
+      rem /= ax.n;
+      const int node = ax.off + idx;
+      set_role(P, ax.role, pv[node]);
+      w *= pw[node];
+      if (idx >= ax.pm_from) pm = true;
+    }
+    double f = ig_eval64(it.integrand, it.family, P, it.args, T);
+    if (pm) {
+      P.q0 = -P.q0;
+      f += ig_eval64(it.integrand, it.family, P, it.args, T);
+    }
+    return w * f;
+  }
+
+  __global__ void __launch_bounds__(kGenericThreads) k_generic(const RunParams P)
+  {
+    __shared__ double red[32];
+    __shared__ int s_unit, s_flag;
+    __shared__ TableDev sT[4];
+    for (;;) {
+      if (threadIdx.x == 0) s_unit = atomicAdd(P.unit_counter, 1);
+      __syncthreads();
+      const int u = s_unit;
+      if (u >= P.n_units) break;
+      const UnitDev U = P.units[u];
+      const ItemDev &it = P.items[U.item];
+      if (threadIdx.x < 4) {
+        const int slot = it.tab[threadIdx.x];
+        if (slot >= 0) sT[threadIdx.x] = P.tabs[slot];
+      }
+      __syncthreads();
+      double acc = 0.0;
+#pragma unroll 1
+      for (int k = 0; k < kGenericPPT; ++k) {
+        const int local = threadIdx.x + k * blockDim.x;
+        if (local < U.row_count) acc += eval_point(it, (long long)U.row_begin + local, P.pv, P.pw, sT);
+      }
+      const double tot = block_sum(acc, red);
+      unit_finish(P, u, U.item, tot, red, &s_flag);
+    }
+  }
+
+  cudaError_t launch_generic(const RunParams &P, int ctas, cudaStream_t s)
+  {
+    k_generic<<<ctas, kGenericThreads, 0, s>>>(P);
+    return cudaGetLastError();
+  }
+
+  // ------------------------------------------------------------------------------------------
+  // Reference execution pattern (the FP64 denominator): one thread per point -- or per point of
+  // the other axes with an in-thread loop over `loop_axis`, as gridreduce_4d loops over cos2
+  // (integrator_4D_gpu.hh:42-47) and gridreduce_4d_finiteT* over q0 -- writing one FP64 value to
+  // global memory for a later device-wide reduction.
+  // ------------------------------------------------------------------------------------------
+  __global__ void __launch_bounds__(256) k_plain(const ItemDev *itp, long long n_threads, int loop_axis,
+                                                 const double *pv, const double *pw, const TableDev *tabs,
+                                                 double *dest)
+  {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_threads) return;
+    const ItemDev &it = *itp;
+    TableDev T[4];
+    for (int i = 0; i < 4; ++i)
+      if (it.tab[i] >= 0) T[i] = tabs[it.tab[i]];
+    const int nloop = loop_axis >= 0 ? it.ax[loop_axis].n : 1;
+    double acc = 0.0;
+    for (int l = 0; l < nloop; ++l) {
+      Pt P{0, 0, 0, 0, 0, 0, 0, 0, it.k};
+      double w = 1.0;
+      bool pm = false;
+      long long rem = t;
+      for (int a = it.n_axes - 1; a >= 0; --a) {
+        const AxisRef ax = it.ax[a];
+        int idx;
+        if (a == loop_axis)
+          idx = l;
+        else {
+          idx = (int)(rem % ax.n);
+          rem /= ax.n;
+        }
+        const int node = ax.off + idx;
+        set_role(P, ax.role, pv[node]);
+        w *= pw[node];
+        if (idx >= ax.pm_from) pm = true;
+      }
+      double f = ig_eval64(it.integrand, it.family, P, it.args, T);
+      if (pm) {
+        P.q0 = -P.q0;
+        f += ig_eval64(it.integrand, it.family, P, it.args, T);
+      }
+      acc += w * f;
+    }
+    dest[t] = acc;
+  }
+
+  cudaError_t launch_plain(const ItemDev *item_dev, long long n_threads, int loop_axis, const double *pv,
+                           const double *pw, const TableDev *tabs, double *dest, cudaStream_t s)
+  {
+    const long long blocks = (n_threads + 255) / 256;
+    k_plain<<<(unsigned)blocks, 256, 0, s>>>(item_dev, n_threads, loop_axis, pv, pw, tabs, dest);
+    return cudaGetLastError();
+  }
+
+  // ------------------------------------------------------------------------------------------
+  // Hoisted FP64 factors of the FP32-compensated kernels: one-axis (or two-axis) parts of the
+  // integrand that many points share, evaluated once per node in FP64.
+  // ------------------------------------------------------------------------------------------
+  __global__ void __launch_bounds__(256) k_seg(const SegDev *segs, const double *pv, const double *pw,
+                                               const TableDev *tabs, double *out)
+  {
+    const SegDev S = segs[blockIdx.y];
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= S.n0 * S.n1) return;
+    const TableDev &T = tabs[S.tab];
+    double F = 0.0;
+    switch (S.kind) {
+    case SEG_S1: {
+      const int i = S.ax0.off + e;
+      const double q = pv[i], q2 = q * q;
+      F = pw[i] * S.par[0] * G1_64(T, q2) * reg_Rdot(q2);
+      break;
+    }
+    case SEG_S2: {
+      const int m = e / S.n1, i = e % S.n1;
+      const int nm = S.ax0.off + m, nq = S.ax1.off + i;
+      const double q = pv[nq], q2 = q * q;
+      F = pw[nm] * pw[nq] * reg_Rdot(q2) * ft_G64(T, pv[nm], q2, S.par[0]);
+      break;
+    }
+    case SEG_S3: {
+      const int i = S.ax0.off + e;
+      const double q = pv[i], q2 = q * q;
+      F = pw[i] * reg_Rdot(q2) * G1_64(T, q2);
+      break;
+    }
+    case SEG_S5: {
+      const int i = e / S.n1, j = e % S.n1;
+      const int ni = S.ax0.off + i, nj = S.ax1.off + j;
+      const double q = pv[ni], q2 = q * q;
+      F = pw[ni] * pw[nj] * reg_Rdot(q2) * G2_64(T, q2, pv[nj]);
+      break;
+    }
+    }
+    out[S.off + e] = F;
+  }
+
+  cudaError_t launch_seg(const SegDev *segs, int n_segs, int max_entries, const double *pv, const double *pw,
+                         const double *pa, const TableDev *tabs, double *seg_out, cudaStream_t s)
+  {
+    (void)pa;
+    if (n_segs == 0) return cudaSuccess;
+    dim3 grid((max_entries + 255) / 256, n_segs);
+    k_seg<<<grid, 256, 0, s>>>(segs, pv, pw, tabs, seg_out);
+    return cudaGetLastError();
+  }
+
+  // ------------------------------------------------------------------------------------------
+  // Throughput probes: 8 independent dependency chains per thread.
+  // ------------------------------------------------------------------------------------------
+  __global__ void k_peak_ffma(float *out, int iters)
+  {
+    float a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = threadIdx.x * 1e-7f + i;
+    const float b = 0.9999f, c = 1e-6f;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = __fmaf_rn(a[i], b, c);
+      }
+    }
+    float s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += a[i];
+    if (s == 123.456f) out[0] = s;
+  }
+  __global__ void k_peak_mufu(float *out, int iters)
+  {
+    float a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = 1.0f + threadIdx.x * 1e-7f + i * 1e-3f;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = __log2f(a[i] + 2.0f);
+      }
+    }
+    float s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += a[i];
+    if (s == 123.456f) out[0] = s;
+  }
+  __global__ void k_peak_dfma(double *out, int iters)
+  {
+    double a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = threadIdx.x * 1e-7 + i;
+    const double b = 0.9999, c = 1e-6;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = fma(a[i], b, c);
+      }
+    }
+    double s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += a[i];
+    if (s == 123.456) out[0] = s;
+  }
+  cudaError_t launch_peak_ffma(float *out, int ctas, int threads, int iters, cudaStream_t s)
+  {
+    k_peak_ffma<<<ctas, threads, 0, s>>>(out, iters);
+    return cudaGetLastError();
+  }
+  cudaError_t launch_peak_mufu(float *out, int ctas, int threads, int iters, cudaStream_t s)
+  {
+    k_peak_mufu<<<ctas, threads, 0, s>>>(out, iters);
+    return cudaGetLastError();
+  }
+  cudaError_t launch_peak_dfma(double *out, int ctas, int threads, int iters, cudaStream_t s)
+  {
+    k_peak_dfma<<<ctas, threads, 0, s>>>(out, iters);
+    return cudaGetLastError();
+  }
+} // namespace gbint

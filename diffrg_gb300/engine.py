@@ -1,0 +1,208 @@
+"""Python host API above the C ABI (libgbint.so).
+
+Mirrors the reference objects a flow-equation code touches on the integration path:
+``QuadratureProvider`` (``Context.gl`` / ``Context.matsubara``), dressing-function tables
+(``Table``; TexLinearInterpolator* in the reference), one integrator evaluation
+(``Context.get``) and the fan-out of many integrals (``Batch``; request_data/update_data in
+DiFfRG/include/DiFfRG/physics/utils.hh:115-147).  Errors raise ``GbError`` like the reference
+throws std::runtime_error.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import capi
+from .capi import FAM, IG, PREC, GbError, Integral, TableSpec
+
+
+def integral(family, integrand="POLY", n=(0, 0, 0, 0), k=1.0, d=4, x_extent=1.0, x0_extent=0.0, x0_summands=0,
+             T=0.0, E=0.0, qmin=(-np.pi,) * 3, qmax=(np.pi,) * 3, args=()) -> Integral:
+    """Descriptor of one integral (gb_integral)."""
+    g = Integral()
+    g.family = FAM[family] if isinstance(family, str) else int(family)
+    g.integrand = IG[integrand] if isinstance(integrand, str) else int(integrand)
+    g.d = d
+    nn = list(n) + [0] * (4 - len(n))
+    for i in range(4):
+        g.n[i] = int(nn[i])
+    g.x_extent = x_extent
+    g.x0_extent = x0_extent
+    g.x0_summands = int(x0_summands)
+    g.T = T
+    g.E = E
+    g.k = k
+    for i in range(3):
+        g.qmin[i] = qmin[i]
+        g.qmax[i] = qmax[i]
+    a = np.zeros(capi.GB_MAX_ARGS)
+    a[:len(args)] = args
+    for i in range(capi.GB_MAX_ARGS):
+        g.args[i] = float(a[i])
+    return g
+
+
+class Table:
+    def __init__(self, ctx: "Context", spec: dict, data=None):
+        self.ctx = ctx
+        self.spec = dict(spec)
+        s = TableSpec(spec["n0"], int(spec["log0"]), spec["lo0"], spec["hi0"], spec.get("n1", 0),
+                      int(spec.get("log1", 0)), spec.get("lo1", 0.0), spec.get("hi1", 1.0))
+        h = C.c_void_p()
+        ctx.check(capi.lib().gb_table_create(ctx.h, C.byref(s), C.byref(h)))
+        self.h = h
+        self.shape = (spec["n0"],) if not spec.get("n1") else (spec["n0"], spec["n1"])
+        if data is not None:
+            self.update(data)
+
+    def update(self, data, stream=None):
+        d = np.ascontiguousarray(data, dtype=np.float32)
+        if d.size != int(np.prod(self.shape)):
+            raise ValueError("table data has %d values, expected %s" % (d.size, self.shape))
+        self.ctx.check(capi.lib().gb_table_update(self.ctx.h, self.h, d.ctypes.data_as(C.POINTER(C.c_float)),
+                                                   C.c_void_p(stream) if stream else None))
+
+    @property
+    def epoch(self) -> int:
+        e = C.c_uint64()
+        self.ctx.check(capi.lib().gb_table_epoch(self.ctx.h, self.h, C.byref(e)))
+        return int(e.value)
+
+    def close(self):
+        if self.h:
+            capi.lib().gb_table_destroy(self.ctx.h, self.h)
+            self.h = None
+
+
+def _table_array(tables: Sequence[Table]):
+    arr = (C.c_void_p * max(1, len(tables)))()
+    for i, t in enumerate(tables):
+        arr[i] = t.h
+    return arr
+
+
+class Batch:
+    def __init__(self, ctx: "Context", integrals: Sequence[Integral], tables: Sequence[Table] = (),
+                 precision: str = "fp32c"):
+        self.ctx = ctx
+        self.n = len(integrals)
+        arr = (Integral * self.n)(*integrals)
+        h = C.c_void_p()
+        ctx.check(capi.lib().gb_batch_create(ctx.h, arr, self.n, _table_array(tables), len(tables),
+                                             PREC[precision], C.byref(h)))
+        self.h = h
+        self.tables = list(tables)
+        self.precision = precision
+        pts = C.c_uint64()
+        nu = C.c_int()
+        ni = C.c_int()
+        ctx.check(capi.lib().gb_batch_info(ctx.h, h, C.byref(pts), C.byref(nu), C.byref(ni)))
+        self.points = int(pts.value)
+        self.n_units = int(nu.value)
+
+    def run(self, stream=None, d_out=None):
+        self.ctx.check(capi.lib().gb_batch_run(self.ctx.h, self.h, C.c_void_p(d_out) if d_out else None,
+                                               C.c_void_p(stream) if stream else None))
+
+    def run_graph(self, stream=None):
+        self.ctx.check(capi.lib().gb_batch_run_graph(self.ctx.h, self.h, C.c_void_p(stream) if stream else None))
+
+    def results(self, stream=None) -> np.ndarray:
+        out = np.zeros(self.n)
+        self.ctx.check(capi.lib().gb_batch_results(self.ctx.h, self.h, capi._dp(out),
+                                                   C.c_void_p(stream) if stream else None))
+        return out
+
+    def get(self, stream=None) -> np.ndarray:
+        out = np.zeros(self.n)
+        self.ctx.check(capi.lib().gb_batch_get(self.ctx.h, self.h, capi._dp(out),
+                                               C.c_void_p(stream) if stream else None))
+        return out
+
+    def run_plain(self, n_streams=16) -> np.ndarray:
+        out = np.zeros(self.n)
+        self.ctx.check(capi.lib().gb_batch_run_plain(self.ctx.h, self.h, capi._dp(out), n_streams))
+        return out
+
+    def close(self):
+        if self.h:
+            capi.lib().gb_batch_destroy(self.ctx.h, self.h)
+            self.h = None
+
+
+class Context:
+    """One device context (gb_ctx): provider caches, node pool, table directory, streams."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0):
+        L = capi.load()
+        h = C.c_void_p()
+        rc = L.gb_ctx_create(device, budget_bytes, C.byref(h))
+        if rc != 0:
+            raise GbError(rc, "gb_ctx_create(device=%d)" % device)
+        self.h = h
+
+    def last_error(self) -> str:
+        buf = C.create_string_buffer(512)
+        capi.lib().gb_last_error(self.h, buf, 512)
+        return buf.value.decode()
+
+    def check(self, rc: int):
+        if rc != 0:
+            raise GbError(rc, self.last_error())
+
+    # QuadratureProvider
+    def gl(self, order: int):
+        hx = C.POINTER(C.c_double)()
+        hw = C.POINTER(C.c_double)()
+        self.check(capi.lib().gb_quad_gl(self.h, order, 0, C.byref(hx), C.byref(hw), None, None))
+        return np.ctypeslib.as_array(hx, (order,)).copy(), np.ctypeslib.as_array(hw, (order,)).copy()
+
+    def gl_device(self, order: int, dtype=0):
+        dx = C.c_void_p()
+        dw = C.c_void_p()
+        self.check(capi.lib().gb_quad_gl(self.h, order, dtype, None, None, C.byref(dx), C.byref(dw)))
+        return dx.value, dw.value
+
+    def matsubara(self, T: float, E: float):
+        n = C.c_int()
+        hx = C.POINTER(C.c_double)()
+        hw = C.POINTER(C.c_double)()
+        tr = C.c_double()
+        self.check(capi.lib().gb_quad_matsubara(self.h, T, E, 0, C.byref(n), C.byref(hx), C.byref(hw), None, None,
+                                                C.byref(tr)))
+        m = n.value
+        return np.ctypeslib.as_array(hx, (m,)).copy(), np.ctypeslib.as_array(hw, (m,)).copy(), tr.value
+
+    def quad_config(self, min_matsubara_size=32, vacuum_quad_size=48, add_matsubara_size=0):
+        self.check(capi.lib().gb_quad_config(self.h, min_matsubara_size, vacuum_quad_size, add_matsubara_size))
+
+    def table(self, spec: dict, data=None) -> Table:
+        return Table(self, spec, data)
+
+    def batch(self, integrals, tables=(), precision="fp32c") -> Batch:
+        return Batch(self, integrals, tables, precision)
+
+    def get(self, g: Integral, tables=(), precision="fp64") -> float:
+        out = C.c_double()
+        self.check(capi.lib().gb_get(self.h, C.byref(g), _table_array(tables), len(tables), PREC[precision],
+                                     C.byref(out)))
+        return out.value
+
+    def measure_peaks(self):
+        """(FP32 TFLOP/s, MUFU G op/s, FP64 TFLOP/s) of this GPU from the library's probes."""
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        self.check(capi.lib().gb_measure_peaks(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def close(self):
+        if self.h:
+            capi.lib().gb_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

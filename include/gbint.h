@@ -1,0 +1,215 @@
+/* gbint.h -- C ABI of the GB300 momentum-loop integration engine (libgbint.so).
+ *
+ * DiFfRG evaluates every loop integral of a flow equation through C++ class templates
+ * (Integrator*GPU / Integrator*FiniteT*GPU + QuadratureProvider) that launch one CUDA
+ * grid per integral, write one FP64 value per quadrature point to global memory and
+ * reduce it with thrust/CUB.  This library replaces the runtime beneath those templates:
+ * quadrature storage, device-resident dressing tables, batched fused FP32-compensated
+ * (or FP64) evaluation with an in-kernel FP64 cross-block reduction, CUDA-graph replay,
+ * and a continuously batching request loop.  The C++ compatibility layer
+ * (include/gbint/integrators.hh) keeps the reference class names and calls only this ABI.
+ *
+ * Plain C types only: pointers, sizes, ints, doubles.  cudaStream_t is passed as void*.
+ * Every call returns a status code (GB_OK == 0).  The reference throws std::runtime_error
+ * on CUDA errors, bad sizes or a missing device (DiFfRG/src/DiFfRG/common/cuda_prefix.cu:9-14,
+ * DiFfRG/include/DiFfRG/physics/integration/integrator_4D_gpu.hh:81,92-93); the C++ layer
+ * maps non-zero codes back onto such exceptions.
+ */
+#ifndef GBINT_H
+#define GBINT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBINT_ABI_VERSION 1
+
+/* ------------------------------------------------------------------ status codes */
+enum {
+  GB_OK = 0,
+  GB_EINVAL = 1,     /* malformed argument or descriptor                           */
+  GB_ENOMEM = 2,     /* device or pinned allocation failed                          */
+  GB_EBUDGET = 3,    /* request refused: it can never fit the context's HBM budget  */
+  GB_ETIMEDOUT = 4,  /* gb_wait gave up, or a device-side bounded wait expired       */
+  GB_ECUDA = 5,      /* a CUDA runtime call failed (see gb_last_error)               */
+  GB_ENODEV = 6,     /* no CUDA device / device index out of range                   */
+  GB_EAGAIN = 7,     /* gb_poll: result not ready yet                                */
+  GB_EDEVICE = 8,    /* a kernel reported an error flag (bounded wait, bad index)    */
+  GB_ECANCELED = 9   /* request was cancelled before it ran                          */
+};
+
+/* ------------------------------------------------------------------ enumerations */
+/* integrator families -- one per reference class template */
+enum {
+  GB_FAM_1D = 1,          /* IntegratorGPU<d,NT,K>          integration/integrator_gpu.hh:21-128          */
+  GB_FAM_ANGLE = 2,       /* IntegratorAngleGPU<d,NT,K>     integration/integrator_angle_gpu.hh:21-219    */
+  GB_FAM_3D = 3,          /* Integrator3DGPU<NT,K>          integration/integrator_3D_gpu.hh:21-197       */
+  GB_FAM_4D2ANG = 4,      /* Integrator4D2AngGPU<NT,K>      integration/integrator_4D_2ang_gpu.hh:21-260  */
+  GB_FAM_4D = 5,          /* Integrator4DGPU<NT,K>          integration/integrator_4D_gpu.hh:21-263       */
+  GB_FAM_CART1 = 6,       /* Integrator1DCartesianGPU       integration/integrator_1D_cartesian_gpu.hh    */
+  GB_FAM_CART2 = 7,       /* Integrator2DCartesianGPU       integration/integrator_2D_cartesian_gpu.hh    */
+  GB_FAM_CART3 = 8,       /* Integrator3DCartesianGPU       integration/integrator_3D_cartesian_gpu.hh    */
+  GB_FAM_2DPQ0 = 9,       /* Integrator2Dpq0GPU             integration/integrator_2Dpq0_gpu.hh:21-243    */
+  GB_FAM_2DPX0 = 10,      /* Integrator2Dpx0GPU             integration/integrator_2Dpx0_gpu.hh           */
+  GB_FAM_3DPQ0 = 11,      /* Integrator3Dpq0GPU             integration/integrator_3Dpq0_gpu.hh           */
+  GB_FAM_3DPX0 = 12,      /* Integrator3Dpx0GPU             integration/integrator_3Dpx0_gpu.hh           */
+  GB_FAM_FTQ0 = 13,       /* IntegratorFiniteTq0GPU<d>      integration_finiteT/integrator_finiteTq0_gpu.hh:21-238 */
+  GB_FAM_ANGLE_FTQ0 = 14, /* IntegratorAngleFiniteTq0GPU<d> integration_finiteT/integrator_angle_finiteTq0_gpu.hh */
+  GB_FAM_4D_FTQ0 = 15,    /* Integrator4DFiniteTq0GPU       integration_finiteT/integrator_4D_finiteTq0_gpu.hh    */
+  GB_FAM_FTX0 = 16,       /* IntegratorFiniteTx0GPU<d>      integration_finiteT/integrator_finiteTx0_gpu.hh:21-225 */
+  GB_FAM_ANGLE_FTX0 = 17, /* IntegratorAngleFiniteTx0GPU<d> integration_finiteT/integrator_angle_finiteTx0_gpu.hh */
+  GB_FAM_4D_FTX0 = 18,    /* Integrator4DFiniteTx0GPU       integration_finiteT/integrator_4D_finiteTx0_gpu.hh:21-249 */
+  GB_FAM_CONST = 19,      /* IntegratorConstant<d>          integration/integrator_constant.hh:11-73      */
+  GB_FAM_QLOOP = 20,      /* d=4 loop, GL in q on [0,qmax] x cos (benchmark workload C1)            */
+  GB_FAM_QLOOP_T = 21     /* finite-T loop, explicit modes n=-M..M, GL in q x cos (workload C2)      */
+};
+
+/* catalogue integrands (device code compiled into the library) */
+enum {
+  GB_IG_POLY = 0,  /* product of polynomials per coordinate (reference test KERNEL)      */
+  GB_IG_PROP1 = 1, /* sqrt(1-c^2) G(q^2) G(q^2+p^2+2pqc) Rdot(q^2) * kfac                */
+  GB_IG_PROP3 = 3, /* Rdot G_A(q^2) G_B(|q-p|^2) V_C(s) V_D(|q-p/2|^2), 4 x 1D tables     */
+  GB_IG_VERT4 = 5, /* 4D vertex loop, two 2D (log x, t) tables                           */
+  GB_IG_FTLOOP = 6 /* q^2 G(w,q^2) G(w,|q+p|^2) Rdot(q^2), one 2D (mode, |q|) table       */
+};
+
+/* arithmetic of a batch */
+enum {
+  GB_PREC_FP32C = 0, /* FP32 evaluation, Kahan + double-float constants, FP64 reduction */
+  GB_PREC_FP64 = 1   /* FP64 evaluation in the same fused kernels                       */
+};
+
+enum { GB_DTYPE_F64 = 0, GB_DTYPE_F32 = 1 };
+
+/* ------------------------------------------------------------------ opaque handles */
+typedef struct gb_ctx gb_ctx;
+typedef struct gb_table gb_table;
+typedef struct gb_batch gb_batch;
+typedef uint64_t gb_ticket;
+
+/* ------------------------------------------------------------------ descriptors */
+/* Table axes: log-spaced (index linear in ln x) or linear; 2D tables are row-major [n0][n1].
+ * Replaces LinearCoordinates1D / LogarithmicCoordinates1D + TexLinearInterpolator{1D,2D}
+ * (discretization/grid/coordinates.hh:97-195, physics/interpolation/tex_linear_interpolation_1D.hh:86-106). */
+typedef struct {
+  int n0, log0;
+  double lo0, hi0;
+  int n1, log1; /* n1 == 0 for a 1D table */
+  double lo1, hi1;
+} gb_table_spec;
+
+#define GB_MAX_ARGS 24
+
+/* One integral.  Field meaning follows the reference constructors
+ * (QuadratureProvider&, grid_sizes, x_extent[, x0_extent|q0_extent, x0_summands, T]) and get(k, args...). */
+typedef struct {
+  int family;      /* GB_FAM_*                                                             */
+  int integrand;   /* GB_IG_*                                                              */
+  int d;           /* template dimension of IntegratorGPU<d>, IntegratorAngleGPU<d>, ...     */
+  int n[4];        /* grid_sizes (finite-T x0: spatial orders then the tail order)           */
+  double x_extent; /* x = q^2/k^2 in [0, x_extent]; qmax for GB_FAM_QLOOP*                   */
+  double x0_extent;/* q0_extent (pq0), x0_extent (px0, finite-T x0)                          */
+  int x0_summands; /* explicit Matsubara terms (finite-T x0); M for GB_FAM_QLOOP_T            */
+  double T;        /* temperature                                                          */
+  double E;        /* typical energy of the Matsubara rule (finite-T q0); 0: reference rule  */
+  double k;        /* RG scale                                                             */
+  double qmin[3], qmax[3]; /* Cartesian boxes                                              */
+  double args[GB_MAX_ARGS]; /* args[0] = constant(); integrand parameters follow             */
+} gb_integral;
+
+typedef struct {
+  uint64_t submitted, completed, rejected, batches_launched;
+  uint64_t points_evaluated;
+  double busy_seconds;
+  double p50_latency_s, p99_latency_s, max_latency_s;
+  uint64_t bytes_in_use, bytes_budget;
+} gb_stats;
+
+/* ------------------------------------------------------------------ context */
+int gb_version(void);
+const char *gb_status_string(int status);
+/* hbm_budget_bytes: admission cap for batch work memory (0 = 8 GiB default) */
+int gb_ctx_create(int device, size_t hbm_budget_bytes, gb_ctx **out);
+int gb_ctx_destroy(gb_ctx *ctx);
+int gb_last_error(gb_ctx *ctx, char *buf, size_t len);
+
+/* ------------------------------------------------------------------ QuadratureProvider
+ * get_points/get_weights (Gauss-Legendre on [0,1]) and get_matsubara_points/weights:
+ * common/quadrature/quadrature_provider.hh:138-248.  Host arrays are FP64; device arrays are
+ * of dtype.  Pointers stay valid until gb_ctx_destroy (the provider owns them for the
+ * process lifetime, as in the reference). */
+int gb_quad_gl(gb_ctx *ctx, int order, int dtype, const double **h_nodes, const double **h_weights,
+               const void **d_nodes, const void **d_weights);
+/* Monien rule for (T, E): MatsubaraStorage::get_matsubara_quadrature (quadrature_provider.cu:12-58).
+ * *size receives the rule size, *T_rule the rule's own T (0 for the vacuum form). */
+int gb_quad_matsubara(gb_ctx *ctx, double T, double E, int dtype, int *size, const double **h_nodes,
+                      const double **h_weights, const void **d_nodes, const void **d_weights, double *T_rule);
+/* /integration/{min_matsubara_size, vacuum_quad_size, add_matsubara_size} (quadrature_provider.cu:220-227) */
+int gb_quad_config(gb_ctx *ctx, int min_matsubara_size, int vacuum_quad_size, int add_matsubara_size);
+
+/* ------------------------------------------------------------------ dressing tables
+ * Device-resident FP32 tables, double-buffered with an epoch: an update writes the back
+ * buffer on `stream` and becomes visible to work enqueued after it on that stream.
+ * Replaces TexLinearInterpolator*::update() (tex_linear_interpolation_1D.cu:169-186), which
+ * copies and then calls cudaDeviceSynchronize. */
+int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out);
+int gb_table_update(gb_ctx *ctx, gb_table *t, const float *host_data, void *stream);
+int gb_table_update_device(gb_ctx *ctx, gb_table *t, const float *device_data, void *stream);
+int gb_table_epoch(gb_ctx *ctx, gb_table *t, uint64_t *epoch);
+int gb_table_destroy(gb_ctx *ctx, gb_table *t);
+
+/* ------------------------------------------------------------------ batches
+ * A batch is a fixed list of integrals planned once (work units, node arrays, scratch) and
+ * run many times: the request_data/update_data fan-out of physics/utils.hh:115-147 as one
+ * submission.  tables[] are referenced by position (integrand-specific: PROP1 t0 = Z;
+ * PROP3 t0..t3 = A,B,C,D; VERT4 t0 = A, t1 = B; FTLOOP t0 = Z(mode,|q|)). */
+int gb_batch_create(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables,
+                    int precision, gb_batch **out);
+/* Enqueue one evaluation on `stream` (NULL: the context stream).  d_out: device array of n
+ * doubles, or NULL to keep results in the batch's own device buffer. */
+int gb_batch_run(gb_ctx *ctx, gb_batch *b, double *d_out, void *stream);
+/* Same, replayed from a CUDA graph captured at the first call (fixed sweeps). */
+int gb_batch_run_graph(gb_ctx *ctx, gb_batch *b, void *stream);
+/* Copy the results of the last run to host (synchronises `stream`). */
+int gb_batch_results(gb_ctx *ctx, gb_batch *b, double *host_out, void *stream);
+/* End-to-end synchronous evaluation: run + D2H into host_out. */
+int gb_batch_get(gb_ctx *ctx, gb_batch *b, double *host_out, void *stream);
+/* Reference execution pattern in FP64: one launch per integral writing one value per point
+ * to global memory, CUB DeviceReduce, D2H and a sync per integral, integrals spread over
+ * n_streams pooled streams (integrator_4D_gpu.hh:141-197).  The 20x denominator. */
+int gb_batch_run_plain(gb_ctx *ctx, gb_batch *b, double *host_out, int n_streams);
+/* points of the tensor-product grids (as the reference counts them) */
+int gb_batch_info(gb_ctx *ctx, gb_batch *b, uint64_t *points, int *n_units, int *n_items);
+int gb_batch_destroy(gb_ctx *ctx, gb_batch *b);
+
+/* one-shot synchronous get(): constant(k,args) + integral, in `precision` */
+int gb_get(gb_ctx *ctx, const gb_integral *item, gb_table *const *tables, int n_tables, int precision,
+           double *out);
+
+/* ------------------------------------------------------------------ serving (request loop)
+ * request(): admit n integrals to the continuously batching loop; work that arrives while
+ * other batches are on the GPU is launched on another stream as soon as a slot and budget
+ * allow.  Tables are read at launch time (their latest epoch). */
+int gb_serve_start(gb_ctx *ctx, int max_inflight_batches, int max_batch_items);
+int gb_serve_stop(gb_ctx *ctx);
+int gb_submit(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
+              gb_ticket *out);
+int gb_poll(gb_ctx *ctx, gb_ticket t, double *out);
+int gb_wait(gb_ctx *ctx, gb_ticket t, double *out, double timeout_s);
+int gb_cancel(gb_ctx *ctx, gb_ticket t);
+int gb_get_stats(gb_ctx *ctx, gb_stats *out);
+int gb_reset_stats(gb_ctx *ctx);
+
+/* ------------------------------------------------------------------ diagnostics
+ * Throughput probes of this GPU (no reference counterpart): FP32 FMA (TFLOP/s, FMA = 2 flops),
+ * MUFU lg2 (G ops/s) and FP64 FMA (TFLOP/s), each timed with CUDA events over the whole
+ * device.  They are the denominators of the engine's roofline. */
+int gb_measure_peaks(gb_ctx *ctx, double *fp32_tflops, double *mufu_gops, double *fp64_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBINT_H */

@@ -1,0 +1,238 @@
+"""GPU parity: every path of libgbint against the FP64 CPU oracle, through the C ABI.
+
+Tolerances (relative, per integral):
+  * FP64 fused kernels and the reference-pattern FP64 path vs oracle: 1e-12 (same quadrature,
+    different summation order);
+  * FP32-compensated kernels vs oracle: TOL32 below, measured on GB300 and fixed here;
+  * polynomial known answers vs closed forms: the reference's own tolerances (kat.py).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from kat import CASES, analytic, random_args
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+# FP32-compensated vs FP64 oracle, max over the integrals of the test subset
+TOL32 = {"C1": 1e-8, "C2": 1e-9, "C3": 1e-9, "C5": 1e-9}
+
+
+@pytest.fixture(scope="module")
+def W():
+    from diffrg_gb300 import workloads
+
+    return workloads
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=float)
+    b = np.asarray(b, dtype=float)
+    return np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+
+
+# ------------------------------------------------------------------ QuadratureProvider
+@pytest.mark.parametrize("n", [1, 2, 5, 16, 64, 128, 256, 1000])
+def test_gl_provider_matches_oracle(ctx, oracle, n):
+    x, w = ctx.gl(n)
+    xo, wo = oracle.gauss_legendre(n)
+    assert np.max(np.abs(x - xo)) <= 2e-16
+    assert np.max(np.abs(w - wo)) <= 4e-16 * max(1, n / 64)
+
+
+@pytest.mark.parametrize("T,E", [(0.05, 1.0), (0.2, 1.0), (1.0, 1.0), (0.1, 0.3), (0.001, 1.0), (0.0, 2.0)])
+def test_matsubara_provider_matches_oracle(ctx, oracle, T, E):
+    x, w, tr = ctx.matsubara(T, E)
+    xo, wo, tro = oracle.matsubara(T, E, step=2, min_size=32, max_size=128, vacuum=48, precision_factor=0)
+    assert tr == tro and x.size == xo.size
+    assert np.max(rel(x, xo)) < 1e-13
+    assert np.max(rel(w, wo)) < 1e-12
+
+
+def test_matsubara_provider_closed_form(ctx):
+    for T in (0.03, 0.3, 0.9):
+        x, w, tr = ctx.matsubara(T, 1.0)
+        s = tr * 1.0 + np.sum(w * 2.0 / (1.0 + x * x))
+        assert abs(s - 0.5 / math.tanh(0.5 / T)) < 1e-13 * s
+
+
+# ------------------------------------------------------------------ families, polynomial KERNEL
+def engine_poly(fam, seed):
+    from diffrg_gb300.engine import integral
+
+    rng = np.random.default_rng(seed)
+    kw = dict(CASES[fam])
+    n = kw.pop("n")
+    d = kw.pop("d")
+    k = rng.uniform(0.3, 1.0)
+    xe = rng.uniform(1.0, 2.0)
+    T = kw.get("T", 0.0)
+    args = random_args(rng, q0_rational=(T, rng.uniform(0.8, 1.2))) if fam.endswith("FTQ0") else random_args(rng)
+    if fam.endswith("FTX0"):
+        kw["x0_extent"] = kw["x0_summands"] * 10 * 2 * math.pi * T / k * 1.5 + 1000.0 / k
+    g = integral(fam, "POLY", n=n, k=k, d=d, x_extent=xe, x0_extent=kw.get("x0_extent", 0.0),
+                 x0_summands=kw.get("x0_summands", 0), T=T, qmin=kw.get("qmin", (-math.pi,) * 3),
+                 qmax=kw.get("qmax", (math.pi,) * 3), args=args)
+    return g, n, d, k, xe, args, kw
+
+
+@pytest.mark.parametrize("fam", list(CASES))
+def test_family_poly_fp64(ctx, oracle, fam):
+    from test_oracle_families import oracle_family
+
+    for seed in (11, 12):
+        g, n, d, k, xe, args, kw = engine_poly(fam, seed)
+        got = ctx.get(g, (), "fp64")
+        ref = oracle_family(oracle, fam, n, d, k, xe, args, kw)
+        assert abs(got - ref) <= TOL64 * max(abs(ref), 1e-3), (fam, got, ref)
+        ana = analytic(fam, args, k, d=d, x_extent=xe, **kw)
+        tol = 5e-5 if fam.endswith("FTQ0") else 1e-4
+        assert abs(got - ana) <= tol * max(1.0, abs(ana))
+
+
+def test_family_batch_matches_single_gets(ctx):
+    gs = [engine_poly(f, 5)[0] for f in ("ANGLE", "4D", "3DPX0", "FTX0", "4D_FTQ0", "CART3")]
+    b = ctx.batch(gs, (), "fp64")
+    many = b.get()
+    b.close()
+    one = np.array([ctx.get(g, (), "fp64") for g in gs])
+    assert np.array_equal(many, one)
+
+
+# ------------------------------------------------------------------ benchmark workloads
+def subset(W, name):
+    w = getattr(W, name.lower())()
+    if name == "C2":
+        sel = np.concatenate([np.arange(0, 128, 16), 128 + np.arange(0, 128, 16), 256 + np.arange(0, 128, 16)])
+        w["p"], w["T"] = w["p"][sel], w["T"][sel]
+    elif name == "C3":
+        rng = np.random.default_rng(3)
+        sel = rng.choice(4096, 48, replace=False)
+        w["orders"], w["P"] = w["orders"][sel], w["P"][sel]
+    elif name == "C5":
+        sel = np.array([0, 21, 63, 64, 100, 127])
+        w["P"], w["alpha"] = w["P"][sel], w["alpha"][sel]
+    return w
+
+
+def run_engine(ctx, W, w, prec):
+    items, tabs = W.engine_items(w)
+    T = [ctx.table(s, d) for s, d in tabs]
+    b = ctx.batch(items, T, prec)
+    out = b.get()
+    b.close()
+    for t in T:
+        t.close()
+    return out
+
+
+@pytest.mark.parametrize("name", ["C1", "C2", "C3", "C5"])
+def test_workload_fp64_matches_oracle(ctx, oracle, W, name):
+    w = subset(W, name)
+    got = run_engine(ctx, W, w, "fp64")
+    ref = W.oracle_values(w, oracle)
+    assert np.max(rel(got, ref)) <= TOL64
+
+
+@pytest.mark.parametrize("name", ["C1", "C2", "C3", "C5"])
+def test_workload_fp32c_matches_oracle(ctx, oracle, W, name):
+    w = subset(W, name)
+    got = run_engine(ctx, W, w, "fp32c")
+    ref = W.oracle_values(w, oracle)
+    err = rel(got, ref)
+    print("%s fp32c max rel err %.3e  median %.3e" % (name, err.max(), np.median(err)))
+    assert np.all(np.isfinite(got))
+    assert err.max() <= TOL32[name]
+
+
+@pytest.mark.parametrize("name", ["C1", "C5"])
+def test_reference_pattern_matches_oracle(ctx, oracle, W, name):
+    w = subset(W, name)
+    items, tabs = W.engine_items(w)
+    T = [ctx.table(s, d) for s, d in tabs]
+    b = ctx.batch(items, T, "fp64")
+    got = b.run_plain(8)
+    b.close()
+    ref = W.oracle_values(w, oracle)
+    assert np.max(rel(got, ref)) <= TOL64
+
+
+# ------------------------------------------------------------------ batching semantics
+def test_alone_and_in_mix_are_bitwise_identical(ctx, W):
+    """Each integral's result is independent of what else is in the launch (deterministic
+    per-integral finish), for the FP32-compensated and FP64 kernels."""
+    w = subset(W, "C3")
+    items, tabs = W.engine_items(w)
+    T = [ctx.table(s, d) for s, d in tabs]
+    for prec in ("fp32c", "fp64"):
+        b = ctx.batch(items, T, prec)
+        mix = b.get()
+        b.close()
+        for i in (0, 7, 31):
+            b1 = ctx.batch([items[i]], T, prec)
+            alone = b1.get()[0]
+            b1.close()
+            assert alone == mix[i]
+    for t in T:
+        t.close()
+
+
+def test_graph_replay_matches_direct_run(ctx, W):
+    w = subset(W, "C2")
+    items, tabs = W.engine_items(w)
+    T = [ctx.table(s, d) for s, d in tabs]
+    b = ctx.batch(items, T, "fp32c")
+    direct = b.get()
+    for _ in range(3):
+        b.run_graph()
+        assert np.array_equal(b.results(), direct)
+    b.close()
+    for t in T:
+        t.close()
+
+
+def test_table_update_is_seen_by_next_run(ctx, oracle, W):
+    w = subset(W, "C1")
+    items, tabs = W.engine_items(w)
+    spec, Z = tabs[0]
+    t = ctx.table(spec, Z)
+    b = ctx.batch(items, [t], "fp32c")
+    first = b.get()
+    Z2 = (Z * 1.1).astype(np.float32)
+    t.update(Z2)
+    assert t.epoch == 2
+    second = b.get()
+    w2 = dict(w)
+    w2["tables"] = [(spec, Z2)]
+    ref = W.oracle_values(w2, oracle)
+    assert np.max(rel(second, ref)) <= TOL32["C1"]
+    assert np.max(rel(first, second)) > 1e-3
+    b.close()
+    t.close()
+
+
+def test_errors_are_status_codes(ctx, W):
+    from diffrg_gb300 import GbError
+    from diffrg_gb300.engine import Context, integral
+
+    with pytest.raises(GbError) as e:
+        ctx.get(integral(99, "POLY", n=(8,)))
+    assert e.value.code == 1
+    with pytest.raises(GbError) as e:  # PROP1 needs a table
+        ctx.get(integral("QLOOP", "PROP1", n=(8, 8), args=(0, 1.0, 1.0)), ())
+    assert e.value.code == 1
+    with pytest.raises(GbError) as e:
+        ctx.get(integral("ANGLE", "POLY", n=(0, 8)))
+    assert e.value.code == 1
+    small = Context(0, budget_bytes=1024)
+    try:
+        w = subset(W, "C1")
+        items, tabs = W.engine_items(w)
+        t = small.table(*tabs[0])
+        with pytest.raises(GbError) as e:
+            small.batch(items, [t])
+        assert e.value.code == 3
+    finally:
+        small.close()
