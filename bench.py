@@ -47,8 +47,8 @@ SPECIALS_PER_POINT = 4
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="C2", choices=["C1", "C2", "C3", "C5"])
     ap.add_argument("--no-cpu", action="store_true")
@@ -195,10 +195,15 @@ def main():
     b32 = ctx.batch(items, T, "fp32c")
     b64 = ctx.batch(items, T, "fp64")
     points = b32.points
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: the library launches on exactly this stream, so the CUDA
+    # events recorded on it bracket the kernels (handle 0 would mean "the context's own stream")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
+    assert sh != 0
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
-    launches_per_step = len([1 for _ in range(1)]) + 1  # hoisted-factor kernel + one fused kernel
+    # kernels per step: the hoisted-factor kernel + one fused persistent kernel per item kind
+    launches_per_step = 2
 
     def timed(batch, steps, warm):
         for _ in range(warm):

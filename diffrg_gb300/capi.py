@@ -22,7 +22,7 @@ FAM = {
     "FTX0": 16, "ANGLE_FTX0": 17, "4D_FTX0": 18, "CONST": 19, "QLOOP": 20, "QLOOP_T": 21,
 }
 IG = {"POLY": 0, "PROP1": 1, "PROP3": 3, "VERT4": 5, "FTLOOP": 6}
-PREC = {"fp32c": 0, "fp64": 1}
+PREC = {"fp32c": 0, "fp64": 1, "fp32f": 2, "fp32a": 3}
 GB_MAX_ARGS = 24
 
 # C ABI symbols declared in include/gbint.h (checked by the CPU test suite)

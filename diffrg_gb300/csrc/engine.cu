@@ -463,7 +463,7 @@ namespace gbint
                   gb_batch **out)
   {
     if (!ctx || !out || n <= 0 || !items) return set_error(ctx, GB_EINVAL, "bad batch arguments");
-    if (precision != GB_PREC_FP32C && precision != GB_PREC_FP64) return set_error(ctx, GB_EINVAL, "bad precision");
+    if (precision < GB_PREC_FP32C || precision > GB_PREC_FP32A) return set_error(ctx, GB_EINVAL, "bad precision");
     std::lock_guard<std::recursive_mutex> lk(ctx->mu);
     GB_CUDA(cudaSetDevice(ctx->device));
     auto b = std::make_unique<gb_batch>();
@@ -514,7 +514,7 @@ namespace gbint
       b->points += pts;
       // kind
       int kind = K_GENERIC;
-      if (precision == GB_PREC_FP32C) {
+      if (precision != GB_PREC_FP64) {
         if (g.integrand == GB_IG_PROP1 && it.n_axes == 2 && it.ax[0].role == R_Q && it.ax[1].role == R_C1 &&
             it.ax[1].pm_from >= it.ax[1].n)
           kind = K_S1;
@@ -524,6 +524,11 @@ namespace gbint
           kind = K_S3;
         else if (g.integrand == GB_IG_VERT4 && g.family == GB_FAM_4D)
           kind = K_S5;
+        // The fast form has ~5e-8 rms error per point and factor and a residual small-x bias of
+        // ~1e-9 (measured on GB300), so it can miss 1e-9 on integrals whose weight sits on a few
+        // thousand points; FP32C therefore uses the accurate double-float form (per-point error
+        // ~2e-9, no measurable bias).  FP32F selects the fast form explicitly.
+        if (kind != K_GENERIC && precision != GB_PREC_FP32F) kind |= K_ACC;
       }
       // table bytes of S kinds must fit shared memory
       if (kind != K_GENERIC) {
@@ -534,7 +539,8 @@ namespace gbint
       it.kind = kind;
       item_kind[i] = kind;
       long long rows;
-      switch (kind) {
+      const int kb = kind_base(kind);
+      switch (kb) {
       case K_S1: rows = it.ax[0].n; break;
       case K_S2: rows = (long long)it.ax[0].n * it.ax[1].n; break;
       case K_S3: rows = (long long)it.ax[0].n * it.ax[1].n; break;
@@ -549,24 +555,24 @@ namespace gbint
       // hoisted segment
       if (kind != K_GENERIC) {
         SegDev S{};
-        S.kind = kind;  // SEG_S* == K_S*
+        S.kind = kb;  // SEG_S* == K_S*
         S.tab = it.tab[0];
-        S.ax0 = kind == K_S2 ? it.ax[0] : it.ax[0];
+        S.ax0 = it.ax[0];
         S.n0 = it.ax[0].n;
         S.n1 = 1;
         double par = 0;
-        if (kind == K_S1) par = g.args[2];
-        if (kind == K_S2) {
+        if (kb == K_S1) par = g.args[2];
+        if (kb == K_S2) {
           S.ax1 = it.ax[1];
           S.n1 = it.ax[1].n;
           par = g.args[2];
         }
-        if (kind == K_S5) {
+        if (kb == K_S5) {
           S.ax1 = it.ax[1];
           S.n1 = it.ax[1].n;
         }
         S.par[0] = par;
-        auto key = std::make_tuple(kind, S.ax0.off, kind == K_S2 || kind == K_S5 ? S.ax1.off : -1, S.tab, par);
+        auto key = std::make_tuple(kb, S.ax0.off, kb == K_S2 || kb == K_S5 ? S.ax1.off : -1, S.tab, par);
         auto f = seg_index.find(key);
         if (f == seg_index.end()) {
           S.off = (int)b->seg_total;
@@ -589,12 +595,13 @@ namespace gbint
       b->plain_threads.push_back(pt);
     }
     // units grouped by kind
-    const int kinds[5] = {K_S1, K_S2, K_S3, K_S5, K_GENERIC};
+    const int kinds[9] = {K_S1, K_S2, K_S3, K_S5, K_S1 | K_ACC, K_S2 | K_ACC, K_S3 | K_ACC, K_S5 | K_ACC, K_GENERIC};
     for (int kind : kinds) {
       gb_batch::KindRun run;
       run.kind = kind;
       run.unit_begin = (int)b->units.size();
-      const int rpu = kind_rows_per_unit(kind, ctx->threads_override[kind]);
+      const int kb = kind_base(kind);
+      const int rpu = kind_rows_per_unit(kind, ctx->threads_override[kb + (kind_acc(kind) ? 8 : 0)]);
       int tab_cap = 0, rec_cap = 0;
       bool any = false;
       for (int i = 0; i < n; ++i) {
@@ -616,9 +623,9 @@ namespace gbint
           for (int t = 0; t < tables_needed(it.integrand); ++t) tb += ctx->slots[it.tab[t]]->bytes;
           tab_cap = std::max(tab_cap, tb);
           int rc_n = 0;
-          if (kind == K_S1) rc_n = it.ax[1].n;
-          if (kind == K_S2 || kind == K_S3) rc_n = it.ax[2].n;
-          if (kind == K_S5) rc_n = it.ax[2].n + it.ax[3].n;
+          if (kb == K_S1) rc_n = it.ax[1].n;
+          if (kb == K_S2 || kb == K_S3) rc_n = it.ax[2].n;
+          if (kb == K_S5) rc_n = it.ax[2].n + it.ax[3].n;
           rec_cap = std::max(rec_cap, rc_n);
         }
       }

@@ -126,7 +126,7 @@ struct gb_ctx {
   std::vector<gb_table *> slots;
   int *d_err = nullptr;
   // kind -> thread override (autotuner)
-  int threads_override[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int threads_override[16] = {};  // [base kind + 8 * accurate]
   // plain-path scratch
   std::vector<double *> plain_buf;
   std::vector<size_t> plain_buf_elems;

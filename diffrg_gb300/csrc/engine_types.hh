@@ -38,8 +38,11 @@ namespace gbint
     K_S1 = 1,       // 2-axis (q, c) + PROP1, FP32c: rows q, inner c
     K_S2 = 2,       // (mode, q, c) + FTLOOP, FP32c: rows (mode, q), inner c
     K_S3 = 3,       // (q, c, phi) + PROP3, FP32c: rows (q, c), inner phi
-    K_S5 = 5        // (q, c1, c2, phi) + VERT4, FP32c: rows (q, c1), mid c2, inner phi
+    K_S5 = 5,       // (q, c1, c2, phi) + VERT4, FP32c: rows (q, c1), mid c2, inner phi
+    K_ACC = 16      // flag on K_S*: double-float evaluation of the per-point factors
   };
+  constexpr int kind_base(int k) { return k & 15; }
+  constexpr bool kind_acc(int k) { return (k & K_ACC) != 0; }
 
   struct ItemDev {
     int kind;

@@ -29,6 +29,52 @@ namespace gbint
       pn1 = p0;
     }
 
+    // Solve (J - shift I) y = rhs in place for the symmetric tridiagonal J (diagonal a, squared
+    // off-diagonals b) by Gaussian elimination with partial (row) pivoting.  Row interchanges
+    // create one extra super-diagonal (u2).  Exactly singular pivots are replaced by a tiny value,
+    // which is what inverse iteration at a converged eigenvalue needs.
+    void tridiag_solve_pivoted(const std::vector<long double> &a, const std::vector<long double> &b,
+                               long double shift, std::vector<long double> &rhs)
+    {
+      const int n = (int)a.size();
+      if (n == 1) {
+        const long double d0 = a[0] - shift;
+        rhs[0] /= (d0 == 0 ? 1e-300L : d0);
+        return;
+      }
+      std::vector<long double> d(n), lo(n, 0), u1(n, 0), u2(n, 0);
+      for (int j = 0; j < n; ++j) d[j] = a[j] - shift;
+      for (int j = 0; j + 1 < n; ++j) lo[j] = u1[j] = std::sqrt(b[j]);
+      const long double tiny = 1e-300L;
+      for (int j = 0; j + 1 < n; ++j) {
+        if (std::fabs(d[j]) >= std::fabs(lo[j])) {
+          if (d[j] == 0) d[j] = tiny;
+          const long double f = lo[j] / d[j];
+          d[j + 1] -= f * u1[j];
+          rhs[j + 1] -= f * rhs[j];
+          u2[j] = 0;
+        } else {
+          // swap rows j and j+1, then eliminate
+          const long double f = d[j] / lo[j];
+          d[j] = lo[j];
+          const long double t = d[j + 1];
+          d[j + 1] = u1[j] - f * t;
+          if (j + 2 < n) {
+            u2[j] = u1[j + 1];
+            u1[j + 1] = -f * u2[j];
+          }
+          u1[j] = t;
+          const long double r = rhs[j];
+          rhs[j] = rhs[j + 1];
+          rhs[j + 1] = r - f * rhs[j + 1];
+        }
+      }
+      if (d[n - 1] == 0) d[n - 1] = tiny;
+      rhs[n - 1] /= d[n - 1];
+      rhs[n - 2] = (rhs[n - 2] - u1[n - 2] * rhs[n - 1]) / d[n - 2];
+      for (int j = n - 3; j >= 0; --j) rhs[j] = (rhs[j] - u1[j] * rhs[j + 1] - u2[j] * rhs[j + 2]) / d[j];
+    }
+
     // number of eigenvalues of the Jacobi matrix below lambda (Sturm count of the LDL^T pivots)
     int sturm_count(const std::vector<long double> &a, const std::vector<long double> &b, long double lambda)
     {
@@ -101,16 +147,19 @@ namespace gbint
       }
       const long double lam = (l + h) / 2;
       x[k] = lam;
-      // Christoffel weights from the orthonormal recurrence
-      long double p_prev = 0, p = 1, s = 1;
-      for (int j = 0; j + 1 < n; ++j) {
-        const long double beta = std::sqrt(b[j]);
-        const long double pn = ((lam - a[j]) * p - (j > 0 ? std::sqrt(b[j - 1]) : 0.0L) * p_prev) / beta;
-        p_prev = p;
-        p = pn;
-        s += p * p;
+      // weight = mu0 * (first component of the normalised eigenvector)^2; the eigenvector comes
+      // from two steps of inverse iteration with a pivoted tridiagonal solve (the forward
+      // three-term recurrence is unstable for the decaying components of this rule)
+      const long double shift = lam + (std::fabs(lam) + 1e-30L) * 64 * std::numeric_limits<long double>::epsilon();
+      std::vector<long double> v(n, 1.0L);
+      for (int it = 0; it < 3; ++it) {
+        tridiag_solve_pivoted(a, b, shift, v);
+        long double nrm = 0;
+        for (int j = 0; j < n; ++j) nrm += v[j] * v[j];
+        nrm = std::sqrt(nrm);
+        for (int j = 0; j < n; ++j) v[j] /= nrm;
       }
-      w[k] = mu0 / s;
+      w[k] = mu0 * v[0] * v[0];
     }
   }
 

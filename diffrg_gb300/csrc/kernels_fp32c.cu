@@ -1,19 +1,22 @@
 // kernels_fp32c.cu -- FP32-compensated persistent kernels for the catalogue workloads.
 //
-// Structure shared by all kinds (one CTA per SM slot, persistent):
-//   * the CTA's dressing tables are staged into shared memory once by non-tensor TMA bulk
-//     copies (cp.async.bulk + mbarrier complete_tx) and restaged only when an item uses others;
-//   * work units (item, 'rows' range) are taken from an atomic counter; the node records of the
-//     unit's inner axes are TMA-prefetched into a second buffer while the current unit computes;
+// Structure shared by all kinds (persistent CTAs):
+//   * the CTA's dressing tables are staged into shared memory by non-tensor TMA bulk copies
+//     (cp.async.bulk + mbarrier complete_tx) and restaged only when an item uses others;
+//   * work units (item, row range) come from an atomic counter; the node records of the unit's
+//     inner axes are TMA-prefetched into a second buffer while the current unit computes;
 //   * one thread per row loops over the inner axes in FP32 with double-float constants and a
-//     Kahan sum, multiplies by the row's hoisted FP64 factor and the unit is reduced in FP64;
+//     Kahan sum, multiplies by the row's hoisted FP64 factor, and the unit is reduced in FP64;
 //   * the last unit of an item sums the item's unit partials in a fixed order (deterministic).
+// Two arithmetic variants per kind:
+//   fast (ACC = false): per-point factors in FP32 (rms error ~5e-8 per factor, no bias);
+//   accurate (ACC = true): the same factors in double-float -- coordinate, table index and
+//     interpolation, regulator, reciprocal and weighted term -- for integrals whose weight sits
+//     on few points (rms error a few 1e-9 per factor).
 // Tensor cores are not used: this is a reduction, not a dense contraction.
 #include "device_common.cuh"
 #include "integrands.cuh"
 #include "kernels.hh"
-
-#include <algorithm>
 
 namespace gbint
 {
@@ -21,7 +24,7 @@ namespace gbint
 
   namespace
   {
-    // A + B*c with A, B, c double-float, rounded once to FP32
+    // A + B*c with A, B, c double-float: one rounding to FP32, or kept as double-float
     __device__ __forceinline__ float lin_df(df A, df B, float c_hi, float c_lo)
     {
       const df p = two_prod(B.hi, c_hi);
@@ -29,9 +32,17 @@ namespace gbint
       const float corr = __fadd_rn(__fadd_rn(s.lo, A.lo), __fmaf_rn(B.hi, c_lo, __fmaf_rn(B.lo, c_hi, p.lo)));
       return __fadd_rn(s.hi, corr);
     }
+    __device__ __forceinline__ df lin_dd(df A, df B, float c_hi, float c_lo)
+    {
+      const df p = two_prod(B.hi, c_hi);
+      const df s = two_sum(A.hi, p.hi);
+      const float corr = __fadd_rn(__fadd_rn(s.lo, A.lo), __fmaf_rn(B.hi, c_lo, __fmaf_rn(B.lo, c_hi, p.lo)));
+      return fast_two_sum(s.hi, corr);
+    }
     __device__ __forceinline__ df df_neg(df a) { return df{-a.hi, -a.lo}; }
     __device__ __forceinline__ df df_scale2(df a, float s) { return df{a.hi * s, a.lo * s}; }  // s a power of 2
     __device__ __forceinline__ df dfc(double v) { return df_from(v); }
+    __device__ __forceinline__ df df_max(df a, float m) { return a.hi < m ? df{m, 0.f} : a; }
 
     // fractional index on a linear axis for a double-float coordinate
     __device__ __forceinline__ float axis_frac_lin_df(const AxisDev &a, df v, int &i)
@@ -60,22 +71,73 @@ namespace gbint
       return fminf(fmaxf(f, 0.f), 1.f);
     }
 
-    __device__ __forceinline__ float tab1_32(const float *d, const AxisDev &a, float x)
+    __device__ __forceinline__ float rcp32(float x) { return __frcp_rn(x); }
+
+    // G = 1/(Z x + R(x)) for a 1D table, fast and accurate forms
+    __device__ __forceinline__ float G1_32(const float *T, const AxisDev &a, float x)
     {
       int i;
       const float f = axis_frac(a, x, i);
-      return lerp32(d[i], d[i + 1], f);
+      return rcp32(__fmaf_rn(lerp32(T[i], T[i + 1], f), x, reg_R(x)));
     }
-    // bilinear: lerp along axis 0 at columns j, j+1, then along axis 1
-    __device__ __forceinline__ float bil32(const float *d, int n1, int i, float fx, int j, float fy)
+    __device__ __forceinline__ df G1_df(const float *T, const AxisDev &a, df x)
+    {
+      int i;
+      const float f = axis_frac_df(a, x.hi, x.lo, i);
+      const df z = lerp_df(T[i], T[i + 1], f);
+      return df_rcp(df_add(df_mul(z, x), reg_R_df(x)));
+    }
+    __device__ __forceinline__ float V1_32(const float *T, const AxisDev &a, float x)
+    {
+      int i;
+      const float f = axis_frac(a, x, i);
+      return lerp32(T[i], T[i + 1], f);
+    }
+    __device__ __forceinline__ df V1_df(const float *T, const AxisDev &a, df x)
+    {
+      int i;
+      const float f = axis_frac_df(a, x.hi, x.lo, i);
+      return lerp_df(T[i], T[i + 1], f);
+    }
+    // bilinear in a row-major [n0][n1] table: lerp along the point-varying axis first and along
+    // the fixed one last, so that the rounding of the first lerps is not shared by many points
+    // (varying = 0: axis 0 first)
+    __device__ __forceinline__ float bil32_v0(const float *d, int n1, int i, float fx, int j, float fy)
     {
       const float *r0 = d + i * n1 + j;
       const float *r1 = r0 + n1;
-      const float lo = lerp32(r0[0], r1[0], fx);
-      const float hi = lerp32(r0[1], r1[1], fx);
-      return lerp32(lo, hi, fy);
+      return lerp32(lerp32(r0[0], r1[0], fx), lerp32(r0[1], r1[1], fx), fy);
     }
-    __device__ __forceinline__ float rcp32(float x) { return __frcp_rn(x); }
+    __device__ __forceinline__ float bil32_v1(const float *d, int n1, int i, float fx, int j, float fy)
+    {
+      const float *r0 = d + i * n1 + j;
+      const float *r1 = r0 + n1;
+      return lerp32(lerp32(r0[0], r0[1], fy), lerp32(r1[0], r1[1], fy), fx);
+    }
+    __device__ __forceinline__ df bil_df_v0(const float *d, int n1, int i, float fx, int j, float fy)
+    {
+      const float *r0 = d + i * n1 + j;
+      const float *r1 = r0 + n1;
+      return lerp_dd(lerp_df(r0[0], r1[0], fx), lerp_df(r0[1], r1[1], fx), fy);
+    }
+    __device__ __forceinline__ df bil_df_v1(const float *d, int n1, int i, float fx, int j, float fy)
+    {
+      const float *r0 = d + i * n1 + j;
+      const float *r1 = r0 + n1;
+      return lerp_dd(lerp_df(r0[0], r0[1], fy), lerp_df(r1[0], r1[1], fy), fx);
+    }
+
+    // Kahan sum of the high parts plus a plain FP32 sum of the low parts of double-float terms
+    struct AccDF {
+      Kahan k;
+      float lo = 0.f;
+      __device__ __forceinline__ void add(df t)
+      {
+        k.add(t.hi);
+        lo = __fadd_rn(lo, t.lo);
+      }
+      __device__ __forceinline__ double value() const { return k.value() + (double)lo; }
+    };
 
     // ---------------------------------------------------------------- per-kind traits
     template <int KIND> struct Traits;
@@ -92,7 +154,7 @@ namespace gbint
       static constexpr int kTables = 2;
     };
 
-    // records a unit needs: (axis index, count) pairs staged back to back
+    // node records a unit needs (inner axes), staged back to back
     __device__ __forceinline__ int rec_axes(int kind, const ItemDev &it, int &a0, int &a1)
     {
       switch (kind) {
@@ -101,9 +163,6 @@ namespace gbint
         a1 = -1;
         return it.ax[1].n;
       case K_S2:
-        a0 = 2;
-        a1 = -1;
-        return it.ax[2].n;
       case K_S3:
         a0 = 2;
         a1 = -1;
@@ -125,15 +184,18 @@ namespace gbint
       const int n = rec_axes(kind, it, a0, a1);
       mbar_expect_tx(bar, (uint32_t)(n * sizeof(NodeRec)));
       tma_bulk_g2s(dst, P.prec + it.ax[a0].off, (uint32_t)(it.ax[a0].n * sizeof(NodeRec)), bar);
-      if (a1 >= 0) tma_bulk_g2s(dst + it.ax[a0].n, P.prec + it.ax[a1].off, (uint32_t)(it.ax[a1].n * sizeof(NodeRec)), bar);
+      if (a1 >= 0)
+        tma_bulk_g2s(dst + it.ax[a0].n, P.prec + it.ax[a1].off, (uint32_t)(it.ax[a1].n * sizeof(NodeRec)), bar);
     }
 
     __device__ __forceinline__ df rec_v(const NodeRec &r) { return df{r.v_hi, r.v_lo}; }
     __device__ __forceinline__ df rec_a(const NodeRec &r) { return df{r.a_hi, r.a_lo}; }
     __device__ __forceinline__ df rec_w(const NodeRec &r) { return df{r.w_hi, r.w_lo}; }
+    __device__ __forceinline__ df rec_aw(const NodeRec &r) { return df{r.aw_hi, r.aw_lo}; }
 
     // ---------------------------------------------------------------- S1: (q, c) x PROP1
     // row = q node i; inner = c nodes; hoisted F_i = w_q kfac G(q^2) Rdot(q^2) (FP64)
+    template <bool ACC>
     __device__ __forceinline__ double row_s1(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
                                              const float *tab, const TableDev *sT)
     {
@@ -142,22 +204,34 @@ namespace gbint
       const df A = df_add(rec_a(qr), dfc(p * p));
       const df B = df_mul(dfc(2.0 * p), rec_v(qr));
       const AxisDev ax = sT[0].a0;
-      Kahan k;
       const int nc = it.ax[1].n;
+      if constexpr (!ACC) {
+        Kahan k;
 #pragma unroll 2
-      for (int l = 0; l < nc; ++l) {
-        const NodeRec r = rc[l];
-        const float x2 = fmaxf(lin_df(A, B, r.v_hi, r.v_lo), 1e-30f);
-        const float z = tab1_32(tab, ax, x2);
-        const float g = rcp32(__fmaf_rn(z, x2, reg_R(x2)));
-        k.add(__fmaf_rn(r.aw_hi, g, __fmul_rn(r.aw_lo, g)));
+        for (int l = 0; l < nc; ++l) {
+          const NodeRec r = rc[l];
+          const float x2 = fmaxf(lin_df(A, B, r.v_hi, r.v_lo), 1e-30f);
+          const float g = G1_32(tab, ax, x2);
+          k.add(__fmaf_rn(r.aw_hi, g, __fmul_rn(r.aw_lo, g)));
+        }
+        return P.seg[it.seg_off + row] * k.value();
+      } else {
+        AccDF k;
+#pragma unroll 1
+        for (int l = 0; l < nc; ++l) {
+          const NodeRec r = rc[l];
+          const df x2 = df_max(lin_dd(A, B, r.v_hi, r.v_lo), 1e-30f);
+          k.add(df_mul(rec_aw(r), G1_df(tab, ax, x2)));
+        }
+        return P.seg[it.seg_off + row] * k.value();
       }
-      return P.seg[it.seg_off + row] * k.value();
     }
 
     // ---------------------------------------------------------------- S2: (mode, q, c) x FTLOOP
     // row = (mode m, q node i); inner = c nodes, each at +w_m and (m >= pm_from) -w_m;
-    // hoisted F_{m,i} = w_m w_q Rdot(q^2) G(w_m, q^2) (FP64)
+    // hoisted F_{m,i} = w_m w_q Rdot(q^2) G(w_m, q^2) (FP64).  The second propagator sits at
+    // frequency +-w_m + W (W the external frequency).
+    template <bool ACC>
     __device__ __forceinline__ double row_s2(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
                                              const float *tab, const TableDev *sT)
     {
@@ -170,12 +244,11 @@ namespace gbint
       const df A = df_add(rec_a(qr), dfc(p * p));
       const df B = df_mul(dfc(2.0 * p), rec_v(qr));
       const TableDev &Z = sT[0];
-      AxisDev axq = Z.a1;  // |q| axis, fed with log2(x2) -> halve the scale
+      AxisDev axq = Z.a1;  // |q| axis, fed with x2 = |q+p|^2 -> half the log2 scale
       axq.scale.hi *= 0.5f;
       axq.scale.lo *= 0.5f;
       const int n1 = Z.n1;
       const double inv2piT = 1.0 / (2.0 * 3.14159265358979323846 * T);
-      // per sign: table row index/fraction (FP64 -> exact enough), w^2 as double-float
       int j0[2];
       float fy0[2];
       df w2[2];
@@ -187,29 +260,48 @@ namespace gbint
         j0[s] = jj;
         w2[s] = dfc(ws * ws);
       }
-      Kahan k;
       const int nc = it.ax[2].n;
+      if constexpr (!ACC) {
+        Kahan k;
 #pragma unroll 1
-      for (int l = 0; l < nc; ++l) {
-        const NodeRec r = rc[l];
-        const float x2 = fmaxf(lin_df(A, B, r.v_hi, r.v_lo), 1e-30f);
-        int jq;
-        const float fq = axis_frac(axq, x2, jq);
-        const float R = reg_R(x2);
-        float gsum = 0.f;
-        for (int s = 0; s < ns; ++s) {
-          // Z[(mode cell j0) .. +1][(|q| cell jq) .. +1]
-          const float z = bil32(tab, n1, j0[s], fy0[s], jq, fq);
-          const float den = __fmaf_rn(z, __fadd_rn(__fadd_rn(w2[s].hi, x2), w2[s].lo), R);
-          gsum = __fadd_rn(gsum, rcp32(den));
+        for (int l = 0; l < nc; ++l) {
+          const NodeRec r = rc[l];
+          const float x2 = fmaxf(lin_df(A, B, r.v_hi, r.v_lo), 1e-30f);
+          int jq;
+          const float fq = axis_frac(axq, x2, jq);
+          const float R = reg_R(x2);
+          float gsum = 0.f;
+          for (int s = 0; s < ns; ++s) {
+            const float z = bil32_v1(tab, n1, j0[s], fy0[s], jq, fq);
+            const float den = __fmaf_rn(z, __fadd_rn(__fadd_rn(w2[s].hi, x2), w2[s].lo), R);
+            gsum = __fadd_rn(gsum, rcp32(den));
+          }
+          k.add(__fmaf_rn(r.w_hi, gsum, __fmul_rn(r.w_lo, gsum)));
         }
-        k.add(__fmaf_rn(r.w_hi, gsum, __fmul_rn(r.w_lo, gsum)));
+        return P.seg[it.seg_off + row] * k.value();
+      } else {
+        AccDF k;
+#pragma unroll 1
+        for (int l = 0; l < nc; ++l) {
+          const NodeRec r = rc[l];
+          const df x2 = df_max(lin_dd(A, B, r.v_hi, r.v_lo), 1e-30f);
+          int jq;
+          const float fq = axis_frac_df(axq, x2.hi, x2.lo, jq);
+          const df R = reg_R_df(x2);
+          df gsum{0.f, 0.f};
+          for (int s = 0; s < ns; ++s) {
+            const df z = bil_df_v1(tab, n1, j0[s], fy0[s], jq, fq);
+            gsum = df_add(gsum, df_rcp(df_add(df_mul(z, df_add(w2[s], x2)), R)));
+          }
+          k.add(df_mul(rec_w(r), gsum));
+        }
+        return P.seg[it.seg_off + row] * k.value();
       }
-      return P.seg[it.seg_off + row] * k.value();
     }
 
     // ---------------------------------------------------------------- S3: (q, c, phi) x PROP3
     // row = (q node i, c node j); inner = phi nodes; hoisted F_i = w_q Rdot(q^2) G_A(q^2) (FP64)
+    template <bool ACC>
     __device__ __forceinline__ double row_s3(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
                                              const float *tab, const TableDev *sT, const int *toff)
     {
@@ -220,34 +312,51 @@ namespace gbint
       const double Pm = it.args[1], ct = it.args[2], st = it.args[3];
       const df q2 = rec_a(qr);
       const df qP = df_mul(rec_v(qr), dfc(Pm));
-      const df X = df_mul(qP, df_mul(rec_v(cr), dfc(ct)));      // q P c cos(th)
+      const df X = df_mul(qP, df_mul(rec_v(cr), dfc(ct)));  // q P c cos(th)
       const df q2pp = df_add(q2, dfc(Pm * Pm));
-      const df A = df_add(q2pp, df_scale2(df_neg(X), 2.f));       // |q-p|^2 at cos(phi) = 0
+      const df A = df_add(q2pp, df_scale2(df_neg(X), 2.f));  // |q-p|^2 at cos(phi) = 0
       const df Ap = df_add(df_add(q2, dfc(0.25 * Pm * Pm)), df_neg(X));
       const df B = df_scale2(df_neg(df_mul(qP, df_mul(rec_a(cr), dfc(st)))), 2.f);  // -2 q P s sin(th)
       const df Bh = df_scale2(B, 0.5f);
       const df third = dfc(1.0 / 3.0);
-      const float sb = df_round(df_mul(q2pp, third));
+      const df sbd = df_mul(q2pp, third);
       const float *TB = tab + toff[1], *TC = tab + toff[2], *TD = tab + toff[3];
       const AxisDev aB = sT[1].a0, aC = sT[2].a0, aD = sT[3].a0;
-      Kahan k;
       const int nf = it.ax[2].n;
+      double inner;
+      if constexpr (!ACC) {
+        const float sb = df_round(sbd);
+        Kahan k;
 #pragma unroll 1
-      for (int l = 0; l < nf; ++l) {
-        const NodeRec r = rc[l];  // a = cos(phi), w = 2 pi w_phi
-        const float r2 = fmaxf(lin_df(A, B, r.a_hi, r.a_lo), 1e-30f);
-        const float t2 = fmaxf(lin_df(Ap, Bh, r.a_hi, r.a_lo), 1e-30f);
-        const float sv = __fmaf_rn(r2, third.hi, __fmaf_rn(r2, third.lo, sb));
-        const float gB = rcp32(__fmaf_rn(tab1_32(TB, aB, r2), r2, reg_R(r2)));
-        const float g = gB * tab1_32(TC, aC, sv) * tab1_32(TD, aD, t2);
-        k.add(__fmaf_rn(r.w_hi, g, __fmul_rn(r.w_lo, g)));
+        for (int l = 0; l < nf; ++l) {
+          const NodeRec r = rc[l];  // a = cos(phi), w = 2 pi w_phi
+          const float r2 = fmaxf(lin_df(A, B, r.a_hi, r.a_lo), 1e-30f);
+          const float t2 = fmaxf(lin_df(Ap, Bh, r.a_hi, r.a_lo), 1e-30f);
+          const float sv = __fmaf_rn(r2, third.hi, __fmaf_rn(r2, third.lo, sb));
+          const float g = G1_32(TB, aB, r2) * V1_32(TC, aC, sv) * V1_32(TD, aD, t2);
+          k.add(__fmaf_rn(r.w_hi, g, __fmul_rn(r.w_lo, g)));
+        }
+        inner = k.value();
+      } else {
+        AccDF k;
+#pragma unroll 1
+        for (int l = 0; l < nf; ++l) {
+          const NodeRec r = rc[l];
+          const df r2 = df_max(lin_dd(A, B, r.a_hi, r.a_lo), 1e-30f);
+          const df t2 = df_max(lin_dd(Ap, Bh, r.a_hi, r.a_lo), 1e-30f);
+          const df sv = df_add(sbd, df_mul(r2, third));
+          const df g = df_mul(df_mul(G1_df(TB, aB, r2), V1_df(TC, aC, sv)), V1_df(TD, aD, t2));
+          k.add(df_mul(rec_w(r), g));
+        }
+        inner = k.value();
       }
-      return P.seg[it.seg_off + i] * P.pw[it.ax[1].off + j] * k.value();
+      return P.seg[it.seg_off + i] * P.pw[it.ax[1].off + j] * inner;
     }
 
     // ---------------------------------------------------------------- S5: (q, c1, c2, phi) x VERT4
     // row = (q node i, c1 node j); mid = c2 nodes; inner = phi nodes;
     // hoisted F_ij = w_q w_c1 Rdot(q^2) G(q^2, c1) (FP64)
+    template <bool ACC>
     __device__ __forceinline__ double row_s5(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
                                              const float *tab, const TableDev *sT, const int *toff)
     {
@@ -260,59 +369,87 @@ namespace gbint
       const df q2pp = df_add(rec_a(qr), dfc(Pm * Pm));
       const df c1 = rec_v(cr);
       const df qPc1 = df_mul(qP, c1);
-      const float r1 = fmaxf(df_round(df_add(q2pp, df_scale2(df_neg(qPc1), 2.f))), 1e-30f);  // |q-p1|^2
+      const df r1d = df_max(df_add(q2pp, df_scale2(df_neg(qPc1), 2.f)), 1e-30f);  // |q-p1|^2
       const df A2 = df_add(q2pp, df_scale2(df_mul(qPc1, dfc(ca)), 2.f));
       const df B2 = df_scale2(df_mul(qP, df_mul(rec_a(cr), dfc(sa))), 2.f);
       const TableDev &TA = sT[0];
       const float *DA = tab + toff[0], *DB = tab + toff[1];
       const int tn1 = TA.n1;
-      // row-level table coordinates: x-cell of r1^2, t-cell of c1
-      int ir1;
-      const float fr1 = axis_frac(TA.a0, r1, ir1);
-      const float Rr1 = reg_R(r1);
       int jc1;
       const float fc1 = axis_frac_lin_df(TA.a1, c1, jc1);
       const int n2 = it.ax[2].n, n3 = it.ax[3].n;
       const NodeRec *rphi = rc + n2;
-      Kahan kmid;
+      if constexpr (!ACC) {
+        const float r1 = df_round(r1d);
+        int ir1;
+        const float fr1 = axis_frac(TA.a0, r1, ir1);
+        const float Rr1 = reg_R(r1);
+        Kahan kmid;
 #pragma unroll 1
-      for (int l = 0; l < n2; ++l) {
-        const NodeRec r2r = rc[l];  // c2: v = c2, a = s2, w = 2 w_c2
-        int jc2;
-        const float fc2 = axis_frac_lin_df(TA.a1, rec_v(r2r), jc2);
-        const float gr1 = rcp32(__fmaf_rn(bil32(DA, tn1, ir1, fr1, jc2, fc2), r1, Rr1));
-        const df Bs = df_mul(B2, rec_a(r2r));
-        Kahan kin;
+        for (int l = 0; l < n2; ++l) {
+          const NodeRec r2r = rc[l];  // c2: v = c2, a = s2, w = 2 w_c2
+          int jc2;
+          const float fc2 = axis_frac_lin_df(TA.a1, rec_v(r2r), jc2);
+          const float gr1 = rcp32(__fmaf_rn(bil32_v0(DA, tn1, ir1, fr1, jc2, fc2), r1, Rr1));
+          const df Bs = df_mul(B2, rec_a(r2r));
+          Kahan kin;
 #pragma unroll 2
-        for (int m = 0; m < n3; ++m) {
-          const NodeRec rp = rphi[m];  // a = cos(phi), w = 2 pi w_phi
-          const float x = fmaxf(lin_df(A2, Bs, rp.a_hi, rp.a_lo), 1e-30f);
-          int ix;
-          const float fx = axis_frac(TA.a0, x, ix);
-          const float gv = rcp32(__fmaf_rn(bil32(DA, tn1, ix, fx, jc1, fc1), x, reg_R(x)));
-          const float vv = bil32(DB, tn1, ix, fx, jc2, fc2);
-          const float g = gv * vv;
-          kin.add(__fmaf_rn(rp.w_hi, g, __fmul_rn(rp.w_lo, g)));
+          for (int m = 0; m < n3; ++m) {
+            const NodeRec rp = rphi[m];  // a = cos(phi), w = 2 pi w_phi
+            const float x = fmaxf(lin_df(A2, Bs, rp.a_hi, rp.a_lo), 1e-30f);
+            int ix;
+            const float fx = axis_frac(TA.a0, x, ix);
+            const float gv = rcp32(__fmaf_rn(bil32_v0(DA, tn1, ix, fx, jc1, fc1), x, reg_R(x)));
+            const float g = gv * bil32_v0(DB, tn1, ix, fx, jc2, fc2);
+            kin.add(__fmaf_rn(rp.w_hi, g, __fmul_rn(rp.w_lo, g)));
+          }
+          const float mt = __fmul_rn((float)kin.value(), gr1);
+          kmid.add(__fmaf_rn(r2r.w_hi, mt, __fmul_rn(r2r.w_lo, mt)));
         }
-        const float mt = __fmul_rn((float)kin.value(), gr1);
-        kmid.add(__fmaf_rn(r2r.w_hi, mt, __fmul_rn(r2r.w_lo, mt)));
+        return P.seg[it.seg_off + row] * kmid.value();
+      } else {
+        int ir1;
+        const float fr1 = axis_frac_df(TA.a0, r1d.hi, r1d.lo, ir1);
+        const df Rr1 = reg_R_df(r1d);
+        AccDF kmid;
+#pragma unroll 1
+        for (int l = 0; l < n2; ++l) {
+          const NodeRec r2r = rc[l];
+          int jc2;
+          const float fc2 = axis_frac_lin_df(TA.a1, rec_v(r2r), jc2);
+          const df gr1 = df_rcp(df_add(df_mul(bil_df_v0(DA, tn1, ir1, fr1, jc2, fc2), r1d), Rr1));
+          const df Bs = df_mul(B2, rec_a(r2r));
+          AccDF kin;
+#pragma unroll 1
+          for (int m = 0; m < n3; ++m) {
+            const NodeRec rp = rphi[m];
+            const df x = df_max(lin_dd(A2, Bs, rp.a_hi, rp.a_lo), 1e-30f);
+            int ix;
+            const float fx = axis_frac_df(TA.a0, x.hi, x.lo, ix);
+            const df gv = df_rcp(df_add(df_mul(bil_df_v0(DA, tn1, ix, fx, jc1, fc1), x), reg_R_df(x)));
+            const df g = df_mul(gv, bil_df_v0(DB, tn1, ix, fx, jc2, fc2));
+            kin.add(df_mul(rec_w(rp), g));
+          }
+          const df si = fast_two_sum(kin.k.s, __fsub_rn(kin.lo, kin.k.c));
+          kmid.add(df_mul(rec_w(r2r), df_mul(si, gr1)));
+        }
+        return P.seg[it.seg_off + row] * kmid.value();
       }
-      return P.seg[it.seg_off + row] * kmid.value();
     }
 
-    template <int KIND>
+    template <int KIND, bool ACC>
     __device__ __forceinline__ double row_value(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
                                                 const float *tab, const TableDev *sT, const int *toff)
     {
-      if constexpr (KIND == K_S1) return row_s1(P, it, row, rc, tab + toff[0], sT);
-      if constexpr (KIND == K_S2) return row_s2(P, it, row, rc, tab + toff[0], sT);
-      if constexpr (KIND == K_S3) return row_s3(P, it, row, rc, tab, sT, toff);
-      if constexpr (KIND == K_S5) return row_s5(P, it, row, rc, tab, sT, toff);
+      if constexpr (KIND == K_S1) return row_s1<ACC>(P, it, row, rc, tab + toff[0], sT);
+      if constexpr (KIND == K_S2) return row_s2<ACC>(P, it, row, rc, tab + toff[0], sT);
+      if constexpr (KIND == K_S3) return row_s3<ACC>(P, it, row, rc, tab, sT, toff);
+      if constexpr (KIND == K_S5) return row_s5<ACC>(P, it, row, rc, tab, sT, toff);
       return 0.0;
     }
   } // namespace
 
-  template <int KIND, int THREADS>
+  template <int KIND, bool ACC, int THREADS>
   __global__ void __launch_bounds__(THREADS) k_fp32c(const RunParams P, int tab_bytes_cap, int rec_cap)
   {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -385,7 +522,7 @@ namespace gbint
       }
       double acc = 0.0;
       if (ok && (int)threadIdx.x < U.row_count)
-        acc = row_value<KIND>(P, it, U.row_begin + threadIdx.x, buf ? rec_s1 : rec_s0, tab_s, sT, s_toff);
+        acc = row_value<KIND, ACC>(P, it, U.row_begin + threadIdx.x, buf ? rec_s1 : rec_s0, tab_s, sT, s_toff);
       const double tot = block_sum(acc, red);
       unit_finish(P, u, U.item, tot, red, &s_flag);
       buf ^= 1;
@@ -397,30 +534,36 @@ namespace gbint
   // ------------------------------------------------------------------------------------------
   namespace
   {
-    template <int KIND, int THREADS> const void *kfun() { return (const void *)&k_fp32c<KIND, THREADS>; }
+    template <int KIND, bool ACC, int THREADS> const void *kfun() { return (const void *)&k_fp32c<KIND, ACC, THREADS>; }
+
+    template <int KIND, bool ACC> const void *sel_threads(int threads)
+    {
+      if (threads == 128) return kfun<KIND, ACC, 128>();
+      if (threads == 256) return kfun<KIND, ACC, 256>();
+      if (threads == 512) return kfun<KIND, ACC, 512>();
+      return nullptr;
+    }
 
     const void *select(int kind, int threads)
     {
-#define GB_SEL(K)                                     \
-  case K:                                             \
-    if (threads == 128) return kfun<K, 128>();        \
-    if (threads == 256) return kfun<K, 256>();        \
-    if (threads == 512) return kfun<K, 512>();        \
-    return nullptr;
-      switch (kind) {
-        GB_SEL(K_S1)
-        GB_SEL(K_S2)
-        GB_SEL(K_S3)
-        GB_SEL(K_S5)
+      const bool acc = kind_acc(kind);
+      switch (kind_base(kind)) {
+      case K_S1:
+        return acc ? sel_threads<K_S1, true>(threads) : sel_threads<K_S1, false>(threads);
+      case K_S2:
+        return acc ? sel_threads<K_S2, true>(threads) : sel_threads<K_S2, false>(threads);
+      case K_S3:
+        return acc ? sel_threads<K_S3, true>(threads) : sel_threads<K_S3, false>(threads);
+      case K_S5:
+        return acc ? sel_threads<K_S5, true>(threads) : sel_threads<K_S5, false>(threads);
       }
-#undef GB_SEL
       return nullptr;
     }
   } // namespace
 
   int kind_default_threads(int kind)
   {
-    switch (kind) {
+    switch (kind_base(kind)) {
     case K_S1:
       return 128;
     case K_S5:

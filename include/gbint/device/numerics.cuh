@@ -83,15 +83,151 @@ namespace gbint
     // ---------------------------------------------------------------- regulator (b = 1, k = 1)
     // R(x) = x/expm1(x), Rdot(x) = 2 x^2 e^x / expm1(x)^2
     // (BosonicRegulator<b=1>::RB / RBdot, DiFfRG/include/DiFfRG/physics/regulators.hh:76-99)
+    //
+    // FP32 form built only from correctly rounded operations (add, mul, fma, div), so that its
+    // rounding errors have no preferred sign, and with truncation / constant errors below 1e-10:
+    //  * x < 1/4: Bernoulli series R = 1 - x/2 + x^2 (1/12 - x^2/720 + x^4/30240 - x^6/1209600);
+    //  * x >= 1/4: e^x - 1 = 2^n (1 + em) - 1 with x log2(e) = n + f split in double-float,
+    //    em = e^(f ln 2) - 1 from its Taylor series (|f ln 2| <= 0.35, 9 terms), then one fma and
+    //    one division.  (The library expm1f was measured to carry a ~3e-9 relative bias.)
     __device__ __forceinline__ float reg_R(float x)
     {
-      if (x < 1e-30f) return 1.f;
-      return __fdiv_rn(x, expm1f(x));
+      if (x < 0.25f) {
+        if (x < 1e-30f) return 1.f;
+        const float y = __fmul_rn(x, x);
+        float p = __fmaf_rn(y, -8.2671957671957672e-07f, 3.3068783068783070e-05f);  // -1/1209600, 1/30240
+        p = __fmaf_rn(y, p, -1.3888888888888889e-03f);                                 // -1/720
+        // 1/12 as a double-float pair: h = y (1/12 + y p)
+        const float c12_hi = 8.33333358e-02f, c12_lo = -2.48352705e-09f;
+        const float h = __fmaf_rn(y, __fmaf_rn(y, p, c12_lo), __fmul_rn(y, c12_hi));
+        // small part first, then a single rounding of 1 + s (rounding 1 - x/2 on its own is
+        // always upward for x below the ulp of 1 and biases R)
+        return __fadd_rn(1.0f, __fmaf_rn(-0.5f, x, h));
+      }
+      if (x > 88.0f) return 0.f;  // x e^-x < 1e-36
+      // t = x log2(e) in double-float
+      const float L2E_hi = 1.44269502e+00f, L2E_lo = 1.92596299e-08f;
+      const float t_hi = __fmul_rn(x, L2E_hi);
+      const float t_lo = __fmaf_rn(x, L2E_lo, __fmaf_rn(x, L2E_hi, -t_hi));
+      const float n = rintf(t_hi);
+      const float f = __fadd_rn(__fsub_rn(t_hi, n), t_lo);  // t_hi - n is exact
+      // r = f ln2 in double-float
+      const float LN2_hi = 6.93147182e-01f, LN2_lo = -1.90465421e-09f;
+      const float r_hi = __fmul_rn(f, LN2_hi);
+      const float r_lo = __fmaf_rn(f, LN2_lo, __fmaf_rn(f, LN2_hi, -r_hi));
+      // e^r - 1 = r + r^2 (1/2 + r/6 + r^2/24 + ... + r^7/362880)
+      float q = __fmaf_rn(r_hi, 2.75573192239858907e-06f, 2.48015873015873016e-05f);
+      q = __fmaf_rn(r_hi, q, 1.98412698412698413e-04f);
+      q = __fmaf_rn(r_hi, q, 1.38888888888888889e-03f);
+      q = __fmaf_rn(r_hi, q, 8.33333333333333333e-03f);
+      q = __fmaf_rn(r_hi, q, 4.16666666666666667e-02f);
+      // 1/6 as a double-float pair (its FP32 rounding alone biased R by ~6e-10)
+      const float c6_hi = 1.66666672e-01f, c6_lo = -4.96705388e-09f;
+      q = __fmaf_rn(r_hi, q, c6_hi);
+      q = __fmaf_rn(r_hi, q, 0.5f);
+      const float r2 = __fmul_rn(r_hi, r_hi);
+      const float em =
+          __fadd_rn(r_hi, __fmaf_rn(r2, q, __fmaf_rn(__fmul_rn(r2, r_hi), c6_lo, r_lo)));
+      // e^x - 1 = 2^n em + (2^n - 1), one rounding
+      const float pn = ldexpf(1.0f, (int)n);
+      const float D = __fmaf_rn(pn, em, __fsub_rn(pn, 1.0f));
+      return __fdiv_rn(x, D);
     }
     GBINT_HD double reg_R(double x)
     {
       if (x == 0.0) return 1.0;
       return x / expm1(x);
+    }
+
+    // ---------------------------------------------------------------- double-float helpers
+    __device__ __forceinline__ df df_norm(float hi, float lo) { return fast_two_sum(hi, lo); }
+    __device__ __forceinline__ df df_add_f(df a, float b)
+    {
+      const df s = two_sum(a.hi, b);
+      return fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+    }
+    // 1/a: one Newton step on the FP32 reciprocal, residual e = 1 - g a formed exactly by fma
+    __device__ __forceinline__ df df_rcp(df a)
+    {
+      const float g = __frcp_rn(a.hi);
+      const float e = __fsub_rn(__fmaf_rn(-g, a.hi, 1.0f), __fmul_rn(g, a.lo));
+      return fast_two_sum(g, __fmul_rn(g, e));
+    }
+    // y0 + f (y1 - y0) for FP32 table values, result double-float
+    __device__ __forceinline__ df lerp_df(float y0, float y1, float f)
+    {
+      const df d = two_sum(y1, -y0);
+      const df p = two_prod(f, d.hi);
+      const df s = two_sum(y0, p.hi);
+      return fast_two_sum(s.hi, __fadd_rn(s.lo, __fmaf_rn(f, d.lo, p.lo)));
+    }
+    // a + f (b - a) for double-float a, b
+    __device__ __forceinline__ df lerp_dd(df a, df b, float f)
+    {
+      const df d = df_add(b, df{-a.hi, -a.lo});
+      return df_add(a, df_mul(df{f, 0.f}, d));
+    }
+
+    // R(x) = x/expm1(x) for a double-float x, double-float result with a relative error of a few
+    // 1e-9 (the FP32 Taylor polynomial of e^r - 1 beyond its quadratic term is the limit).
+    __device__ __forceinline__ df reg_R_df(df x)
+    {
+      const float xh = x.hi, xl = x.lo;
+      if (xh < 0.25f) {
+        if (xh < 1e-30f) return df{1.f, 0.f};
+        const float y = __fmul_rn(xh, xh);
+        float p = __fmaf_rn(y, -8.2671957671957672e-07f, 3.3068783068783070e-05f);
+        p = __fmaf_rn(y, p, -1.3888888888888889e-03f);
+        const float c12_hi = 8.33333358e-02f, c12_lo = -2.48352705e-09f;
+        const float h = __fmaf_rn(y, __fmaf_rn(y, p, c12_lo), __fmul_rn(y, c12_hi));
+        const df s = two_sum(__fmul_rn(-0.5f, xh), h);  // -x/2 exact
+        const df r = fast_two_sum(1.0f, s.hi);
+        return df_norm(r.hi, __fadd_rn(r.lo, __fmaf_rn(-0.5f, xl, s.lo)));
+      }
+      if (xh > 88.0f) return df{0.f, 0.f};
+      const float L2E_hi = 1.44269502e+00f, L2E_lo = 1.92596299e-08f;
+      const float t_hi = __fmul_rn(xh, L2E_hi);
+      const float t_lo =
+          __fadd_rn(__fmaf_rn(xh, L2E_hi, -t_hi), __fmaf_rn(xh, L2E_lo, __fmul_rn(xl, L2E_hi)));
+      const float n = rintf(t_hi);
+      const float f_hi = __fsub_rn(t_hi, n);  // exact; f = f_hi + t_lo
+      const float LN2_hi = 6.93147182e-01f, LN2_lo = -1.90465421e-09f;
+      const float r_hi0 = __fmul_rn(f_hi, LN2_hi);
+      const float r_lo0 =
+          __fadd_rn(__fmaf_rn(f_hi, LN2_hi, -r_hi0), __fmaf_rn(f_hi, LN2_lo, __fmul_rn(t_lo, LN2_hi)));
+      const df r = fast_two_sum(r_hi0, r_lo0);
+      float q = __fmaf_rn(r.hi, 2.75573192239858907e-06f, 2.48015873015873016e-05f);
+      q = __fmaf_rn(r.hi, q, 1.98412698412698413e-04f);
+      q = __fmaf_rn(r.hi, q, 1.38888888888888889e-03f);
+      q = __fmaf_rn(r.hi, q, 8.33333333333333333e-03f);
+      q = __fmaf_rn(r.hi, q, 4.16666666666666667e-02f);
+      const float c6_hi = 1.66666672e-01f, c6_lo = -4.96705388e-09f;
+      q = __fmaf_rn(r.hi, q, c6_hi);
+      q = __fmaf_rn(r.hi, q, 0.5f);
+      // em = r + r^2 q: r^2 and r^2 q as double-float
+      const df r2 = two_prod(r.hi, r.hi);
+      const float r2l = __fmaf_rn(2.0f * r.hi, r.lo, r2.lo);
+      const df tq = two_prod(r2.hi, q);
+      const float tl = __fmaf_rn(r2l, q, __fmaf_rn(__fmul_rn(r2.hi, r.hi), c6_lo, tq.lo));
+      const df e0 = two_sum(r.hi, tq.hi);
+      const df em = fast_two_sum(e0.hi, __fadd_rn(e0.lo, __fadd_rn(r.lo, tl)));
+      // D = 2^n (1 + em) - 1 in double-float
+      df D;
+      const int ni = (int)n;
+      const float pn = ldexpf(1.0f, ni);
+      if (ni == 0) {
+        D = em;
+      } else if (ni <= 24) {
+        const df s = two_sum(__fsub_rn(pn, 1.0f), __fmul_rn(pn, em.hi));
+        D = fast_two_sum(s.hi, __fmaf_rn(pn, em.lo, s.lo));
+      } else {
+        const df s = two_sum(pn, __fmul_rn(pn, em.hi));
+        D = fast_two_sum(s.hi, __fadd_rn(s.lo, __fmaf_rn(pn, em.lo, -1.0f)));
+      }
+      // x / D
+      const float q0 = __fdiv_rn(xh, D.hi);
+      const float rem = __fadd_rn(__fsub_rn(__fmaf_rn(-q0, D.hi, xh), __fmul_rn(q0, D.lo)), xl);
+      return fast_two_sum(q0, __fdiv_rn(rem, D.hi));
     }
     GBINT_HD double reg_Rdot(double x)
     {
@@ -111,20 +247,156 @@ namespace gbint
       double scale64, shift64;
     };
 
-    // FP32 index and fraction; u clamped to [0, n-1], cell i in [0, n-2]
-    __device__ __forceinline__ float axis_frac(const AxisDev &a, float v, int &i)
+    // log2(v) = e + lm for a positive normal v: integer exponent e and |lm| <= 1/2 from log2f of
+    // the mantissa scaled into [1/sqrt2, sqrt2).  Absolute error ~3e-8 instead of ~1e-6 for
+    // log2f(v) itself when |log2 v| ~ 10 (measured on GB300; __log2f was biased, log2f is not).
+    __device__ __forceinline__ void log2_split(float v, float &e, float &lm)
     {
-      const float g = a.log ? log2f(v) : v;
-      // u = scale*g + shift in double-float, rounded once
-      const df sg = two_prod(a.scale.hi, g);
-      const float lo = __fadd_rn(__fmaf_rn(a.scale.lo, g, sg.lo), a.shift.lo);
-      const df s = two_sum(sg.hi, a.shift.hi);
-      float u = __fadd_rn(s.hi, __fadd_rn(s.lo, lo));
-      u = fminf(fmaxf(u, 0.f), (float)(a.n - 1));  // fmaxf maps NaN to 0
-      int ii = (int)u;
-      ii = min(ii, a.n - 2);
+      const int b = __float_as_int(v);
+      int ex = ((b >> 23) & 0xff) - 127;
+      float m = __int_as_float((b & 0x007fffff) | 0x3f800000);
+      if (m > 1.41421356f) {
+        m = __fmul_rn(m, 0.5f);
+        ex += 1;
+      }
+      e = (float)ex;
+      lm = log2f(m);
+    }
+
+    // Cell i in [0, n-2] and fraction in [0, 1] of u = scale * g + shift (u clamped to [0, n-1]),
+    // g = log2(v) or v.  u is formed in double-float and its fraction taken before any rounding
+    // of u itself: rounding u (up to ~n) to FP32 first costs ~1e-5 of a cell, the largest
+    // per-point error of a naive FP32 table lookup.
+    // log2(m) for m in [1/sqrt2, sqrt2) as a double-float, absolute error ~5e-10:
+    // ln m = 2 atanh(s) = 2 s + 2 s^3 (1/3 + s^2/5 + ... + s^10/13), s = (m-1)/(m+1) in
+    // double-float, |s| <= 0.172 (truncation < 1e-11); then times log2(e) in double-float.
+    __device__ __forceinline__ df log2_mant_df(float m)
+    {
+      const float num = __fsub_rn(m, 1.0f);  // exact (Sterbenz)
+      const df den = two_sum(m, 1.0f);
+      const float s0 = __fdiv_rn(num, den.hi);
+      const float rr = __fsub_rn(__fmaf_rn(-s0, den.hi, num), __fmul_rn(s0, den.lo));
+      const float s1 = __fdiv_rn(rr, den.hi);
+      const float t = __fmul_rn(s0, s0);
+      float P = __fmaf_rn(t, 7.69230769e-02f, 9.09090909e-02f);  // 1/13, 1/11
+      P = __fmaf_rn(t, P, 1.11111111e-01f);                       // 1/9
+      P = __fmaf_rn(t, P, 1.42857143e-01f);                       // 1/7
+      P = __fmaf_rn(t, P, 2.00000000e-01f);                       // 1/5
+      P = __fmaf_rn(t, P, 3.33333343e-01f);                       // 1/3
+      const float c3 = __fmul_rn(__fmul_rn(2.0f * s0, t), P);
+      const df lnm = fast_two_sum(2.0f * s0, __fmaf_rn(2.0f, s1, c3));
+      const df l2e{1.44269502e+00f, 1.92596299e-08f};
+      return df_mul(lnm, l2e);
+    }
+
+    __device__ __forceinline__ float axis_frac_c(const AxisDev &a, float v, float corr, int &i);
+    __device__ __forceinline__ float axis_frac(const AxisDev &a, float v, int &i) { return axis_frac_c(a, v, 0.f, i); }
+    __device__ __forceinline__ float frac_from_u(const AxisDev &a, float uh, float ul, int &i);
+    // same for a double-float coordinate v = vh + vl, with log2 of the mantissa in double-float
+    // (log2_mant_df) and the low part of v entering the index linearly
+    __device__ __forceinline__ float axis_frac_df(const AxisDev &a, float vh, float vl, int &i)
+    {
+      if (!a.log) {
+        const df u = df_add(df_mul(a.scale, df_add(df{vh, 0.f}, df{vl, 0.f})), a.shift);
+        return frac_from_u(a, u.hi, u.lo, i);
+      }
+      if (!(vh >= 1e-30f)) {
+        vh = 1e-30f;
+        vl = 0.f;
+      }
+      if (!(vh <= 3e38f)) {
+        vh = 3e38f;
+        vl = 0.f;
+      }
+      const int b = __float_as_int(vh);
+      int ex = ((b >> 23) & 0xff) - 127;
+      float m = __int_as_float((b & 0x007fffff) | 0x3f800000);
+      if (m > 1.41421356f) {
+        m = __fmul_rn(m, 0.5f);
+        ex += 1;
+      }
+      const df lm = log2_mant_df(m);
+      // g = ex + lm + vl / (vh ln 2)
+      const df g0 = two_sum((float)ex, lm.hi);
+      const float gl = __fadd_rn(__fadd_rn(g0.lo, lm.lo), __fmul_rn(1.44269504f, __fmul_rn(vl, __frcp_rn(vh))));
+      const df g = fast_two_sum(g0.hi, gl);
+      const df u = df_add(df_mul(a.scale, g), a.shift);
+      return frac_from_u(a, u.hi, u.lo, i);
+    }
+    __device__ __forceinline__ float frac_from_u(const AxisDev &a, float uh, float ul, int &i)
+    {
+      const float ur = __fadd_rn(uh, ul);
+      if (!(ur > 0.f)) {
+        i = 0;
+        return 0.f;
+      }
+      if (ur >= (float)(a.n - 1)) {
+        i = a.n - 2;
+        return 1.f;
+      }
+      int ii = (int)ur;
+      float f = __fadd_rn(__fsub_rn(uh, (float)ii), ul);
+      if (f < 0.f) {
+        if (ii > 0) {
+          ii -= 1;
+          f = __fadd_rn(__fsub_rn(uh, (float)ii), ul);
+        } else
+          f = 0.f;
+      }
+      if (ii > a.n - 2) {
+        ii = a.n - 2;
+        f = 1.f;
+      }
       i = ii;
-      return __fsub_rn(u, (float)ii);
+      return fminf(f, 1.f);
+    }
+    // `corr` is added to the low part of u (first-order contribution of a coordinate's low part)
+    __device__ __forceinline__ float axis_frac_c(const AxisDev &a, float v, float corr, int &i)
+    {
+      float uh, ul;
+      if (a.log) {
+        if (!(v >= 1e-30f)) v = 1e-30f;  // also maps NaN
+        if (!(v <= 3e38f)) v = 3e38f;
+        float e, lm;
+        log2_split(v, e, lm);
+        const df p1 = two_prod(a.scale.hi, e);
+        const df p2 = two_prod(a.scale.hi, lm);
+        const df s1 = two_sum(p1.hi, a.shift.hi);
+        const df s2 = two_sum(s1.hi, p2.hi);
+        const float lo = __fadd_rn(__fadd_rn(__fadd_rn(p1.lo, p2.lo), __fadd_rn(s1.lo, s2.lo)),
+                                   __fadd_rn(__fmaf_rn(a.scale.lo, __fadd_rn(e, lm), 0.f), a.shift.lo));
+        uh = s2.hi;
+        ul = __fadd_rn(lo, corr);
+      } else {
+        const df p = two_prod(a.scale.hi, v);
+        const df s = two_sum(p.hi, a.shift.hi);
+        uh = s.hi;
+        ul = __fadd_rn(__fadd_rn(__fadd_rn(p.lo, s.lo), __fmaf_rn(a.scale.lo, v, a.shift.lo)), corr);
+      }
+      const float ur = __fadd_rn(uh, ul);
+      if (!(ur > 0.f)) {
+        i = 0;
+        return 0.f;
+      }
+      if (ur >= (float)(a.n - 1)) {
+        i = a.n - 2;
+        return 1.f;
+      }
+      int ii = (int)ur;
+      float f = __fadd_rn(__fsub_rn(uh, (float)ii), ul);  // uh - ii is exact
+      if (f < 0.f) {
+        if (ii > 0) {
+          ii -= 1;
+          f = __fadd_rn(__fsub_rn(uh, (float)ii), ul);
+        } else
+          f = 0.f;
+      }
+      if (ii > a.n - 2) {
+        ii = a.n - 2;
+        f = 1.f;
+      }
+      i = ii;
+      return fminf(f, 1.f);
     }
     GBINT_HD double axis_frac64(const AxisDev &a, double v, int &i)
     {
