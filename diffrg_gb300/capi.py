@@ -31,7 +31,7 @@ EXPORTS = [
     "gb_quad_gl", "gb_quad_matsubara", "gb_quad_config",
     "gb_table_create", "gb_table_update", "gb_table_update_device", "gb_table_epoch", "gb_table_destroy",
     "gb_batch_create", "gb_batch_run", "gb_batch_run_graph", "gb_batch_results", "gb_batch_get",
-    "gb_batch_run_plain", "gb_batch_info", "gb_batch_destroy", "gb_get",
+    "gb_batch_run_plain", "gb_batch_info", "gb_batch_destroy", "gb_get", "gb_get_noalloc",
     "gb_serve_start", "gb_serve_stop", "gb_submit", "gb_poll", "gb_wait", "gb_cancel",
     "gb_get_stats", "gb_reset_stats", "gb_measure_peaks",
 ]
@@ -106,6 +106,7 @@ def load(path: str = LIB_PATH):
     L.gb_batch_info.argtypes = [vp, vp, C.POINTER(C.c_uint64), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.gb_batch_destroy.argtypes = [vp, vp]
     L.gb_get.argtypes = [vp, C.POINTER(Integral), C.POINTER(vp), C.c_int, C.c_int, dp]
+    L.gb_get_noalloc.argtypes = [vp, C.POINTER(Integral), C.POINTER(vp), C.c_int, dp]
     L.gb_serve_start.argtypes = [vp, C.c_int, C.c_int]
     L.gb_serve_stop.argtypes = [vp]
     L.gb_submit.argtypes = [vp, C.POINTER(Integral), C.c_int, C.POINTER(vp), C.c_int, C.c_int,

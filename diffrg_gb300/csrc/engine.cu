@@ -705,6 +705,39 @@ namespace gbint
     }
     return GB_OK;
   }
+
+  // Device descriptor of one integral for the generic FP64 kernel: axes from the context's node
+  // pool (pre-allocated; new quadrature orders are copied in, nothing is allocated on the device)
+  // and table directory slots.  Caller holds ctx->mu.
+  int prepare_item_fp64(gb_ctx *ctx, const gb_integral &g, gb_table *const *tables, int n_tables, ItemDev &it,
+                        uint64_t &grid_points)
+  {
+    std::memset(&it, 0, sizeof(it));
+    if (g.integrand != GB_IG_POLY && g.integrand != GB_IG_PROP1 && g.integrand != GB_IG_PROP3 &&
+        g.integrand != GB_IG_VERT4 && g.integrand != GB_IG_FTLOOP)
+      return set_error(ctx, GB_EINVAL, "unknown integrand");
+    it.kind = K_GENERIC;
+    it.integrand = g.integrand;
+    it.family = g.family;
+    it.k = g.k;
+    std::memcpy(it.args, g.args, sizeof(it.args));
+    int rc = family_axes(ctx, g, it.ax, it.n_axes);
+    if (rc) return rc;
+    const int nt = tables_needed(g.integrand);
+    if (nt > n_tables) return set_error(ctx, GB_EINVAL, "integrand needs more tables than given");
+    for (int t = 0; t < 4; ++t) it.tab[t] = -1;
+    for (int t = 0; t < nt; ++t) {
+      if (!tables || !tables[t] || tables[t]->slot < 0) return set_error(ctx, GB_EINVAL, "null table");
+      it.tab[t] = tables[t]->slot;
+    }
+    if (g.integrand == GB_IG_FTLOOP && (tables[0]->spec.n1 < 2 || !(g.args[2] > 0)))
+      return set_error(ctx, GB_EINVAL, "FTLOOP needs a 2D table and T > 0");
+    if (g.integrand == GB_IG_VERT4 && tables[0]->spec.n1 < 2)
+      return set_error(ctx, GB_EINVAL, "VERT4 needs 2D tables");
+    grid_points = 1;
+    for (int a = 0; a < it.n_axes; ++a) grid_points *= (uint64_t)it.ax[a].n;
+    return GB_OK;
+  }
 } // namespace gbint
 
 // ============================================================================ C ABI

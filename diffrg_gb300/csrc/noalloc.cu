@@ -1,0 +1,176 @@
+// noalloc.cu -- gb_get_noalloc: one FP64 integral evaluated without allocating device memory.
+//
+// Who needs it: hosts that must not call cudaMalloc/cudaFree (or any allocating library
+// routine) while they integrate -- e.g. a time stepper that records a whole right-hand-side
+// evaluation under CUDA stream capture in global mode, where cudaMalloc is an illegal call, or
+// a code that runs under a fixed device-memory budget handed out once at start-up by another
+// allocator.  gb_get builds a small batch per call and allocates its scratch; this entry point
+// keeps its scratch in a fixed file-scope device array instead.
+//
+// Scratch: g_noalloc_scratch below, GB_NOALLOC_SCRATCH_BYTES (36 KiB) per device, resident from
+// module load until process exit.  It holds the integral's descriptor, two counters, the result
+// and one FP64 partial per work unit of 1024 grid points, so one call accepts at most
+// GB_NOALLOC_MAX_POINTS = 4096 * 1024 = 4,194,304 grid points (nodes per axis multiplied; the
+// +-q0 pairs of finite-T axes count once).  Larger integrals are rejected with GB_EINVAL.
+//
+// Every call on a device shares the one array; the counters are cleared on the stream before
+// each launch.  Calls serialise on the context mutex and complete (stream synchronised) before
+// they return; two contexts on the same device whose calls overlap on the GPU race on the array.
+//
+// The host cannot use the array's name as a device address (in host code it names a host-side
+// stand-in).  The first call on each device resolves the address with cudaGetSymbolAddress with
+// that device current and caches it; make that first call before any stream capture begins.
+// New quadrature orders fill host-side caches and are copied into the context's pre-allocated
+// node pool; no device or pinned memory is allocated by this entry point.
+#include <cstddef>
+#include <mutex>
+
+#include "device_common.cuh"
+#include "engine.hh"
+#include "integrands.cuh"
+#include "kernels.hh"
+
+namespace gbint
+{
+  int prepare_item_fp64(gb_ctx *ctx, const gb_integral &g, gb_table *const *tables, int n_tables, ItemDev &it,
+                        uint64_t &grid_points);
+
+  namespace
+  {
+    constexpr int kNoAllocMaxUnits = GB_NOALLOC_MAX_POINTS / kGenericUnitPoints;
+    static_assert(GB_NOALLOC_MAX_POINTS % kGenericUnitPoints == 0, "unit size must divide the point limit");
+
+    struct NoAllocScratch {
+      ItemDev item;
+      int unit_counter;
+      int item_count;
+      int pad[2];
+      double result;
+      double partials[kNoAllocMaxUnits];
+    };
+    static_assert(sizeof(NoAllocScratch) <= GB_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds the stated size");
+
+    // the scratch: fixed size, one copy per device, lives until process exit
+    static __device__ __align__(256) unsigned char g_noalloc_scratch[GB_NOALLOC_SCRATCH_BYTES];
+
+    std::mutex g_addr_mu;
+    void *g_addr[64] = {};  // device address of g_noalloc_scratch per device ordinal
+
+    // same per-point evaluation as the generic kernel (kernels_generic.cu)
+    __device__ __forceinline__ double eval_point_na(const ItemDev &it, long long pt, const double *pv, const double *pw,
+                                                    const TableDev *T)
+    {
+      dev::Pt P{0, 0, 0, 0, 0, 0, 0, 0, it.k};
+      double w = 1.0;
+      bool pm = false;
+      long long rem = pt;
+      for (int a = it.n_axes - 1; a >= 0; --a) {
+        const AxisRef ax = it.ax[a];
+        const int idx = (int)(rem % ax.n);
+        rem /= ax.n;
+        const int node = ax.off + idx;
+        dev::set_role(P, ax.role, pv[node]);
+        w *= pw[node];
+        if (idx >= ax.pm_from) pm = true;
+      }
+      double f = dev::ig_eval64(it.integrand, it.family, P, it.args, T);
+      if (pm) {
+        P.q0 = -P.q0;
+        f += dev::ig_eval64(it.integrand, it.family, P, it.args, T);
+      }
+      return w * f;
+    }
+
+    // The generic FP64 kernel with its work units implied (unit u = grid points
+    // [u*1024, (u+1)*1024)) and all scratch -- descriptor, counters, partials, result -- in the
+    // static array.  Reduction order equals the generic kernel's, so results agree bitwise.
+    __global__ void __launch_bounds__(kGenericThreads) k_generic_noalloc(NoAllocScratch *S, long long points,
+                                                                       const double *pv, const double *pw,
+                                                                       const TableDev *tabs)
+    {
+      __shared__ double red[32];
+      __shared__ int s_unit, s_flag;
+      __shared__ TableDev sT[4];
+      const ItemDev &it = S->item;
+      RunParams P{};
+      P.items = &S->item;
+      P.partials = S->partials;
+      P.item_count = &S->item_count;
+      P.out = &S->result;
+      if (threadIdx.x < 4) {
+        const int slot = it.tab[threadIdx.x];
+        if (slot >= 0) sT[threadIdx.x] = tabs[slot];
+      }
+      for (;;) {
+        if (threadIdx.x == 0) s_unit = atomicAdd(&S->unit_counter, 1);
+        __syncthreads();
+        const int u = s_unit;
+        if (u >= it.n_units) break;
+        const long long begin = (long long)u * kGenericUnitPoints;
+        const long long count = min((long long)kGenericUnitPoints, points - begin);
+        double acc = 0.0;
+#pragma unroll 1
+        for (int k = 0; k < kGenericPPT; ++k) {
+          const int local = threadIdx.x + k * blockDim.x;
+          if (local < count) acc += eval_point_na(it, begin + local, pv, pw, sT);
+        }
+        const double tot = dev::block_sum(acc, red);
+        dev::unit_finish(P, u, 0, tot, red, &s_flag);
+      }
+    }
+
+    int scratch_address(gb_ctx *ctx, NoAllocScratch **out)
+    {
+      if (ctx->device < 0 || ctx->device >= 64) return set_error(ctx, GB_ENODEV, "device ordinal beyond 63");
+      std::lock_guard<std::mutex> lk(g_addr_mu);
+      if (!g_addr[ctx->device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // device is current
+        if (e != cudaSuccess || !p) return cuda_fail(ctx, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_addr[ctx->device] = p;
+      }
+      *out = static_cast<NoAllocScratch *>(g_addr[ctx->device]);
+      return GB_OK;
+    }
+  } // namespace
+} // namespace gbint
+
+using namespace gbint;
+
+extern "C" int gb_get_noalloc(gb_ctx *ctx, const gb_integral *item, gb_table *const *tables, int n_tables,
+                              double *out)
+{
+  if (!ctx || !item || !out) return GB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  NoAllocScratch *S = nullptr;
+  int rc = scratch_address(ctx, &S);
+  if (rc) return rc;
+  ItemDev it;
+  uint64_t points = 0;
+  rc = prepare_item_fp64(ctx, *item, tables, n_tables, it, points);
+  if (rc) return rc;
+  if (points > (uint64_t)GB_NOALLOC_MAX_POINTS)
+    return set_error(ctx, GB_EINVAL,
+                     "gb_get_noalloc: the integral has " + std::to_string(points) +
+                         " grid points; the allocation-free entry point accepts at most " +
+                         std::to_string(GB_NOALLOC_MAX_POINTS) + " (use gb_get)");
+  const int n_units = (int)((points + kGenericUnitPoints - 1) / kGenericUnitPoints);
+  it.unit_begin = 0;
+  it.n_units = n_units;
+  it.rows = (int)points;
+  cudaStream_t s = ctx->stream;
+  // descriptor in, counters cleared (the array keeps the previous call's contents)
+  e = cudaMemcpyAsync(&S->item, &it, sizeof(ItemDev), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&S->unit_counter, 0, 2 * sizeof(int), s);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gb_get_noalloc set-up copy");
+  const int ctas = std::min(n_units, ctx->num_sms * 8);
+  k_generic_noalloc<<<ctas, kGenericThreads, 0, s>>>(S, (long long)points, ctx->pool.d_v, ctx->pool.d_w, ctx->d_dir);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "k_generic_noalloc launch");
+  e = cudaMemcpyAsync(out, &S->result, sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gb_get_noalloc result copy");
+  return GB_OK;
+}

@@ -193,6 +193,20 @@ int gb_batch_destroy(gb_ctx *ctx, gb_batch *b);
 int gb_get(gb_ctx *ctx, const gb_integral *item, gb_table *const *tables, int n_tables, int precision,
            double *out);
 
+/* Allocation-free get() in FP64 -- no counterpart in the reference.  For hosts that must not
+ * allocate device memory while they integrate: code running under CUDA stream capture in
+ * global mode (where cudaMalloc is an illegal call) or under a fixed memory budget handed out by
+ * another allocator at start-up.  It calls no cudaMalloc/cudaFree nor any allocating library
+ * routine; its scratch is one fixed file-scope device array of GB_NOALLOC_SCRATCH_BYTES per
+ * device, held until process exit.  Limit: GB_NOALLOC_MAX_POINTS grid points per integral
+ * (larger ones return GB_EINVAL).  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress) -- make it before any stream capture.  All calls on a device share the
+ * array: calls through one context serialise, calls from two contexts that overlap on the GPU
+ * race.  Results equal gb_get(..., GB_PREC_FP64, ...). */
+#define GB_NOALLOC_MAX_POINTS 4194304
+#define GB_NOALLOC_SCRATCH_BYTES 36864
+int gb_get_noalloc(gb_ctx *ctx, const gb_integral *item, gb_table *const *tables, int n_tables, double *out);
+
 /* ------------------------------------------------------------------ serving (request loop)
  * request(): admit n integrals to the continuously batching loop; work that arrives while
  * other batches are on the GPU is launched on another stream as soon as a slot and budget
