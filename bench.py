@@ -42,6 +42,9 @@ UNIT = "integrals/s"
 # frequency, as the reference counts points): F basic FP32 flops (FMA = 2), S special functions
 FLOPS_PER_POINT = 18
 SPECIALS_PER_POINT = 4
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant kernel, from the
+# ncu capture summarised in profiles/ (k_fp32c_S2acc_C2_finiteT.md)
+TRAFFIC_BYTES_PER_LAUNCH = {"C2": 388352}
 
 
 def parse():
@@ -297,13 +300,7 @@ def main():
     xu_achieved = SPECIALS_PER_POINT * pts_per_s / 1e9
     frac32 = fp32_achieved / fp32_peak
     fracxu = xu_achieved / mufu_peak
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)
-    if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
-        except Exception:
-            traffic = None
+    traffic = TRAFFIC_BYTES_PER_LAUNCH.get(args.workload)
     roof = {"bound": "xu" if fracxu >= frac32 else "fp32",
             "achieved": xu_achieved if fracxu >= frac32 else fp32_achieved,
             "peak": mufu_peak if fracxu >= frac32 else fp32_peak,

@@ -811,6 +811,7 @@ int gb_ctx_destroy(gb_ctx *ctx)
   if (ctx->serve) serve_stop(ctx);
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
+  destroy_slots(ctx);
   for (auto &kv : ctx->gl) {
     cudaFree(kv.second.d64x);
     cudaFree(kv.second.d64w);

@@ -59,6 +59,7 @@ namespace gbint
 
   struct Ticket;
   struct ServeState;
+  struct SlotPool;
 } // namespace gbint
 
 struct gb_table {
@@ -136,6 +137,8 @@ struct gb_ctx {
   double *plain_res_h = nullptr;   // pinned host
   // serving
   gbint::ServeState *serve = nullptr;
+  // request slots of the C++ class templates
+  gbint::SlotPool *slotpool = nullptr;
 };
 
 namespace gbint
@@ -155,4 +158,5 @@ namespace gbint
   int serve_cancel(gb_ctx *ctx, gb_ticket t);
   int serve_stats(gb_ctx *ctx, gb_stats *out);
   int serve_reset_stats(gb_ctx *ctx);
+  void destroy_slots(gb_ctx *ctx);
 } // namespace gbint

@@ -207,6 +207,26 @@ int gb_get(gb_ctx *ctx, const gb_integral *item, gb_table *const *tables, int n_
 #define GB_NOALLOC_SCRATCH_BYTES 36864
 int gb_get_noalloc(gb_ctx *ctx, const gb_integral *item, gb_table *const *tables, int n_tables, double *out);
 
+/* ------------------------------------------------------------------ user-kernel launches
+ * Runtime side of the C++ class templates (include/gbint/integrators.hh), which compile the
+ * user's KERNEL into a fused kernel in the user's translation unit.  A slot is the per-request
+ * state the reference takes from its RMM pool and rmm::cuda_stream_pool
+ * (integrator_4D_gpu.hh:141-197): a pooled stream, FP64 partials for up to `units` work units,
+ * two counters (cleared on the slot's stream by acquire), a device result and a pinned host copy.
+ * request() launches on slot.stream right away; gb_slot_wait is the future's get(). */
+typedef struct {
+  double *partials; /* device, capacity_units entries                 */
+  int *counters;    /* device: [0] work-unit counter, [1] arrivals     */
+  double *result;   /* device: the reduced integral                    */
+  void *stream;     /* cudaStream_t the request runs on                */
+  int capacity_units;
+  int id;
+} gb_slot;
+int gb_slot_acquire(gb_ctx *ctx, int units, gb_slot *out);
+int gb_slot_wait(gb_ctx *ctx, const gb_slot *slot, double *out);
+int gb_slot_release(gb_ctx *ctx, const gb_slot *slot);
+int gb_device_info(gb_ctx *ctx, int *device, int *num_sms);
+
 /* ------------------------------------------------------------------ serving (request loop)
  * request(): admit n integrals to the continuously batching loop; work that arrives while
  * other batches are on the GPU is launched on another stream as soon as a slot and budget

@@ -1,0 +1,184 @@
+// Test driver of the DiFfRG-compatible class templates (include/gbint/integrators.hh).
+//
+// Like the reference's integrator tests (e.g. DiFfRG/tests/physics/integration/integrator_4D_gpu.cu),
+// each family integrates a product of polynomials (a rational function in q0 for the finite-T
+// q0 families).  Cases come on stdin, one per line:
+//   family d n0 n1 n2 n3 x_extent x0_extent x0_summands T k prec a0 .. a23
+// (prec 0 = NT double, 1 = NT float; family numbers as GB_FAM_* in gbint.h); the driver prints
+// one value per case with 17 significant digits.  tests/test_gpu_cpp_api.py compares them with
+// the FP64 oracle and with the closed forms.
+#include <cstdio>
+#include <iostream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "gbint/integrators.hh"
+
+using namespace DiFfRG;
+
+struct Coeffs {
+  double a[24];
+};
+
+template <typename NT> __host__ __device__ inline NT pv(const double *c, int n, NT x)
+{
+  NT r = 0;
+  for (int i = n - 1; i >= 0; --i) r = r * x + (NT)c[i];
+  return r;
+}
+template <typename NT> __host__ __device__ inline NT pq0(const Coeffs &C, NT q0)
+{
+  const NT v = pv<NT>(C.a + 19, 4, q0);
+  return C.a[23] != 0 ? (NT)1 / v : v;
+}
+
+template <typename NT> struct K1 {  // (q)
+  static __host__ __device__ NT kernel(NT q, NT, const Coeffs &C) { return pv<NT>(C.a + 1, 6, q); }
+  static __host__ __device__ NT constant(NT, const Coeffs &C) { return (NT)C.a[0]; }
+};
+template <typename NT> struct K2 {  // (q, cos) -- angle; Cartesian 2D (qx, qy)
+  static __host__ __device__ NT kernel(NT q, NT c, NT, const Coeffs &C) { return pv<NT>(C.a + 1, 6, q) * pv<NT>(C.a + 7, 4, c); }
+  static __host__ __device__ NT constant(NT, const Coeffs &C) { return (NT)C.a[0]; }
+};
+template <typename NT> struct K3 {  // (q, c1, x3): 3D (phi), 4D2Ang (cos2), Cartesian 3D (qz)
+  static __host__ __device__ NT kernel(NT q, NT c, NT z, NT, const Coeffs &C)
+  {
+    return pv<NT>(C.a + 1, 6, q) * pv<NT>(C.a + 7, 4, c) * pv<NT>(C.a + 11, 4, z);
+  }
+  static __host__ __device__ NT constant(NT, const Coeffs &C) { return (NT)C.a[0]; }
+};
+template <typename NT> struct K4 {  // 4D (q, c1, c2, phi)
+  static __host__ __device__ NT kernel(NT q, NT c1, NT c2, NT phi, NT, const Coeffs &C)
+  {
+    return pv<NT>(C.a + 1, 6, q) * pv<NT>(C.a + 7, 4, c1) * pv<NT>(C.a + 11, 4, c2) * pv<NT>(C.a + 15, 4, phi);
+  }
+  static __host__ __device__ NT constant(NT, const Coeffs &C) { return (NT)C.a[0]; }
+};
+template <typename NT> struct KT1 {  // (q, q0)
+  static __host__ __device__ NT kernel(NT q, NT q0, NT, const Coeffs &C) { return pv<NT>(C.a + 1, 6, q) * pq0<NT>(C, q0); }
+  static __host__ __device__ NT constant(NT, const Coeffs &C) { return (NT)C.a[0]; }
+};
+template <typename NT> struct KT2 {  // (q, cos, q0)
+  static __host__ __device__ NT kernel(NT q, NT c, NT q0, NT, const Coeffs &C)
+  {
+    return pv<NT>(C.a + 1, 6, q) * pv<NT>(C.a + 7, 4, c) * pq0<NT>(C, q0);
+  }
+  static __host__ __device__ NT constant(NT, const Coeffs &C) { return (NT)C.a[0]; }
+};
+template <typename NT> struct KT3 {  // (q, cos, phi, q0)
+  static __host__ __device__ NT kernel(NT q, NT c, NT phi, NT q0, NT, const Coeffs &C)
+  {
+    return pv<NT>(C.a + 1, 6, q) * pv<NT>(C.a + 7, 4, c) * pv<NT>(C.a + 11, 4, phi) * pq0<NT>(C, q0);
+  }
+  static __host__ __device__ NT constant(NT, const Coeffs &C) { return (NT)C.a[0]; }
+};
+template <typename NT> struct KC {  // constant integrator: kernel(k)
+  static __host__ __device__ NT kernel(NT k, const Coeffs &C) { return pv<NT>(C.a + 1, 6, k); }
+  static __host__ __device__ NT constant(NT, const Coeffs &C) { return (NT)C.a[0]; }
+};
+
+struct Case {
+  int fam, d, n[4], ns, prec;
+  double xe, x0e, T, k;
+  Coeffs C;
+};
+
+template <typename NT, int d> double run_d(QuadratureProvider &qp, const Case &c)
+{
+  const NT xe = (NT)c.xe, k = (NT)c.k;
+  const uint n0 = c.n[0], n1 = c.n[1], n2 = c.n[2], n3 = c.n[3];
+  switch (c.fam) {
+  case GB_FAM_1D: return IntegratorGPU<d, NT, K1<NT>>(qp, {{n0}}, xe).get(k, c.C);
+  case GB_FAM_ANGLE: return IntegratorAngleGPU<d, NT, K2<NT>>(qp, {{n0, n1}}, xe).get(k, c.C);
+  case GB_FAM_FTQ0: return IntegratorFiniteTq0GPU<d, NT, KT1<NT>>(qp, {{n0}}, xe, (NT)c.T).get(k, c.C);
+  case GB_FAM_ANGLE_FTQ0: return IntegratorAngleFiniteTq0GPU<d, NT, KT2<NT>>(qp, {{n0, n1}}, xe, (NT)c.T).get(k, c.C);
+  case GB_FAM_FTX0:
+    return IntegratorFiniteTx0GPU<d, NT, KT1<NT>>(qp, {{n0, n1}}, xe, (NT)c.x0e, c.ns, (NT)c.T).get(k, c.C);
+  case GB_FAM_ANGLE_FTX0:
+    return IntegratorAngleFiniteTx0GPU<d, NT, KT2<NT>>(qp, {{n0, n1, n2}}, xe, (NT)c.x0e, c.ns, (NT)c.T).get(k, c.C);
+  case GB_FAM_CONST: return IntegratorConstant<d, NT, KC<NT>>(qp, {{n0}}, xe).get(k, c.C);
+  }
+  throw std::runtime_error("family without dimension template");
+}
+
+template <typename NT> double run(QuadratureProvider &qp, const Case &c)
+{
+  const NT xe = (NT)c.xe, k = (NT)c.k;
+  const uint n0 = c.n[0], n1 = c.n[1], n2 = c.n[2], n3 = c.n[3];
+  switch (c.fam) {
+  case GB_FAM_3D: return Integrator3DGPU<NT, K3<NT>>(qp, {{n0, n1, n2}}, xe).get(k, c.C);
+  case GB_FAM_4D2ANG: return Integrator4D2AngGPU<NT, K3<NT>>(qp, {{n0, n1, n2}}, xe).get(k, c.C);
+  case GB_FAM_4D: return Integrator4DGPU<NT, K4<NT>>(qp, {{n0, n1, n2, n3}}, xe).get(k, c.C);
+  case GB_FAM_CART1: {
+    Integrator1DCartesianGPU<NT, K1<NT>> I(qp, {{n0}});
+    I.set_qx_min(-1.0), I.set_qx_max(1.5);
+    return I.get(k, c.C);
+  }
+  case GB_FAM_CART2: {
+    Integrator2DCartesianGPU<NT, K2<NT>> I(qp, {{n0, n1}});
+    I.set_qx_min(-1.0), I.set_qx_max(1.5), I.set_qy_min(-0.5), I.set_qy_max(0.5);
+    return I.get(k, c.C);
+  }
+  case GB_FAM_CART3: {
+    Integrator3DCartesianGPU<NT, K3<NT>> I(qp, {{n0, n1, n2}});
+    I.set_qx_min(-1.0), I.set_qx_max(1.5), I.set_qy_min(-0.5), I.set_qy_max(0.5), I.set_qz_min(-2.0),
+        I.set_qz_max(1.0);
+    return I.get(k, c.C);
+  }
+  case GB_FAM_2DPQ0: return Integrator2Dpq0GPU<NT, KT2<NT>>(qp, {{n0, n1, n2}}, xe, (NT)c.x0e).get(k, c.C);
+  case GB_FAM_2DPX0: return Integrator2Dpx0GPU<NT, KT2<NT>>(qp, {{n0, n1, n2}}, xe, (NT)c.x0e).get(k, c.C);
+  case GB_FAM_3DPQ0: return Integrator3Dpq0GPU<NT, KT3<NT>>(qp, {{n0, n1, n2, n3}}, xe, (NT)c.x0e).get(k, c.C);
+  case GB_FAM_3DPX0: return Integrator3Dpx0GPU<NT, KT3<NT>>(qp, {{n0, n1, n2, n3}}, xe, (NT)c.x0e).get(k, c.C);
+  case GB_FAM_4D_FTQ0: return Integrator4DFiniteTq0GPU<NT, KT3<NT>>(qp, {{n0, n1, n2}}, xe, (NT)c.T).get(k, c.C);
+  case GB_FAM_4D_FTX0:
+    return Integrator4DFiniteTx0GPU<NT, KT3<NT>>(qp, {{n0, n1, n2, n3}}, xe, (NT)c.x0e, c.ns, (NT)c.T).get(k, c.C);
+  }
+  if (c.d == 3) return run_d<NT, 3>(qp, c);
+  if (c.d == 4) return run_d<NT, 4>(qp, c);
+  throw std::runtime_error("unsupported d");
+}
+
+int main(int argc, char **argv)
+{
+  QuadratureProvider qp;
+  std::string line;
+  std::vector<Case> cases;
+  while (std::getline(std::cin, line)) {
+    if (line.empty()) continue;
+    std::istringstream is(line);
+    Case c{};
+    is >> c.fam >> c.d >> c.n[0] >> c.n[1] >> c.n[2] >> c.n[3] >> c.xe >> c.x0e >> c.ns >> c.T >> c.k >> c.prec;
+    for (int i = 0; i < 24; ++i) is >> c.C.a[i];
+    cases.push_back(c);
+  }
+  // first all values through get(), then the same through request() launched back to back
+  std::vector<double> got(cases.size());
+  for (size_t i = 0; i < cases.size(); ++i) {
+    try {
+      got[i] = cases[i].prec ? run<float>(qp, cases[i]) : run<double>(qp, cases[i]);
+    } catch (const std::exception &e) {
+      std::printf("ERROR %s\n", e.what());
+      return 2;
+    }
+    std::printf("%.17g\n", got[i]);
+  }
+  if (argc > 1 && std::string(argv[1]) == "--requests") {
+    // futures in flight together (pooled streams), then resolved
+    IntegratorAngleGPU<4, double, K2<double>> I(qp, {{64, 12}}, 1.5);
+    std::vector<std::future<double>> fs;
+    Coeffs C{};
+    C.a[1] = 1.0;
+    C.a[7] = 1.0;
+    for (int j = 0; j < 32; ++j) {
+      C.a[2] = 0.01 * j;
+      fs.push_back(I.request(0.8, C));
+    }
+    for (int j = 0; j < 32; ++j) {
+      C.a[2] = 0.01 * j;
+      const double a = fs[j].get(), b = I.get(0.8, C);
+      std::printf("REQ %.17g %.17g\n", a, b);
+    }
+  }
+  return 0;
+}
