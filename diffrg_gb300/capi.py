@@ -34,6 +34,8 @@ EXPORTS = [
     "gb_batch_run_plain", "gb_batch_info", "gb_batch_destroy", "gb_get", "gb_get_noalloc",
     "gb_serve_start", "gb_serve_stop", "gb_submit", "gb_poll", "gb_wait", "gb_cancel",
     "gb_get_stats", "gb_reset_stats", "gb_measure_peaks",
+    "gb_buffer_create", "gb_buffer_upload", "gb_buffer_destroy",
+    "gb_slot_acquire", "gb_slot_wait", "gb_slot_release", "gb_device_info",
 ]
 
 

@@ -812,6 +812,8 @@ int gb_ctx_destroy(gb_ctx *ctx)
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
   destroy_slots(ctx);
+  for (auto &kv : ctx->buffers) cudaFree(kv.first);
+  ctx->buffers.clear();
   for (auto &kv : ctx->gl) {
     cudaFree(kv.second.d64x);
     cudaFree(kv.second.d64w);

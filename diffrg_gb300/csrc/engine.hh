@@ -139,6 +139,8 @@ struct gb_ctx {
   gbint::ServeState *serve = nullptr;
   // request slots of the C++ class templates
   gbint::SlotPool *slotpool = nullptr;
+  // gb_buffer_* allocations and their sizes
+  std::map<void *, size_t> buffers;
 };
 
 namespace gbint

@@ -132,6 +132,49 @@ int gb_slot_release(gb_ctx *ctx, const gb_slot *slot)
   return GB_OK;
 }
 
+int gb_buffer_create(gb_ctx *ctx, size_t bytes, void **d_ptr)
+{
+  if (!ctx || !d_ptr || bytes == 0) return set_error(ctx, GB_EINVAL, "bad buffer request");
+  if (ctx->in_use + bytes > ctx->budget) return set_error(ctx, GB_EBUDGET, "buffer exceeds the HBM budget");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = cudaMalloc(d_ptr, bytes);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gb_buffer_create");
+  ctx->in_use += bytes;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  ctx->buffers[*d_ptr] = bytes;
+  return GB_OK;
+}
+
+int gb_buffer_upload(gb_ctx *ctx, void *d_ptr, const void *host, size_t bytes)
+{
+  if (!ctx || !d_ptr || !host) return GB_EINVAL;
+  {
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    auto it = ctx->buffers.find(d_ptr);
+    if (it == ctx->buffers.end() || it->second < bytes) return set_error(ctx, GB_EINVAL, "unknown buffer or too many bytes");
+  }
+  // in place, after the device drained: kernels in flight on pooled streams may read the buffer
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(d_ptr, host, bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gb_buffer_upload");
+  return GB_OK;
+}
+
+int gb_buffer_destroy(gb_ctx *ctx, void *d_ptr)
+{
+  if (!ctx || !d_ptr) return GB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  auto it = ctx->buffers.find(d_ptr);
+  if (it == ctx->buffers.end()) return GB_EINVAL;
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();  // in-flight kernels may still read it
+  cudaFree(d_ptr);
+  ctx->in_use -= it->second;
+  ctx->buffers.erase(it);
+  return GB_OK;
+}
+
 int gb_device_info(gb_ctx *ctx, int *device, int *num_sms)
 {
   if (!ctx) return GB_EINVAL;

@@ -222,6 +222,12 @@ typedef struct {
   int capacity_units;
   int id;
 } gb_slot;
+/* Device buffers owned by the context (counted against its HBM budget): the data of the
+ * interpolator objects of the C++ layer (TexLinearInterpolator*::update copies host data and
+ * synchronises, tex_linear_interpolation_1D.cu:169-186; gb_buffer_upload copies synchronously). */
+int gb_buffer_create(gb_ctx *ctx, size_t bytes, void **d_ptr);
+int gb_buffer_upload(gb_ctx *ctx, void *d_ptr, const void *host, size_t bytes);
+int gb_buffer_destroy(gb_ctx *ctx, void *d_ptr);
 int gb_slot_acquire(gb_ctx *ctx, int units, gb_slot *out);
 int gb_slot_wait(gb_ctx *ctx, const gb_slot *slot, double *out);
 int gb_slot_release(gb_ctx *ctx, const gb_slot *slot);

@@ -14,8 +14,23 @@
 #include <vector>
 
 #include "gbint/integrators.hh"
+#include "gbint/interpolators.hh"
 
 using namespace DiFfRG;
+
+// KERNEL reading two dressing functions through interpolator objects passed as arguments,
+// the way generated DiFfRG kernels do (e.g. ZA.kernel): G(x) = 1/(Z(x) x + R(x)), R = x/expm1(x)
+using ZTex = TexLinearInterpolator1D<double, LogarithmicCoordinates1D<float>>;
+using ZLin = LinearInterpolator1D<double, LinearCoordinates1D<double>>;
+struct KInterp {
+  static __host__ __device__ double kernel(double q, double c, double k, const ZTex &Z, const ZLin &W, double p)
+  {
+    const double q2 = q * q, x2 = q2 + p * p + 2 * p * q * c;
+    const double R1 = q2 > 0 ? q2 / expm1(q2) : 1.0, R2 = x2 > 0 ? x2 / expm1(x2) : 1.0;
+    return W(q2) / ((Z((float)q2) * q2 + R1) * (Z((float)x2) * x2 + R2));
+  }
+  static __host__ __device__ double constant(double, const ZTex &, const ZLin &, double) { return 0.0; }
+};
 
 struct Coeffs {
   double a[24];
@@ -162,6 +177,51 @@ int main(int argc, char **argv)
       return 2;
     }
     std::printf("%.17g\n", got[i]);
+  }
+  if (argc > 1 && std::string(argv[1]) == "--interp") {
+    // device interpolation inside a user KERNEL vs the same quadrature summed on the host with
+    // the interpolators' host branch
+    std::vector<double> z(64), wv(33);
+    for (int i = 0; i < 64; ++i) z[i] = 1.0 + 0.3 * std::sin(0.37 * i);
+    for (int i = 0; i < 33; ++i) wv[i] = 0.5 + 0.01 * i * i;
+    ZTex Z(z, LogarithmicCoordinates1D<float>(64, 1e-4f, 50.f, 3.f));
+    ZLin W(wv, LinearCoordinates1D<double>(33, 0.0, 4.0));
+    const uint nx = 48, nc = 16;
+    const double xe = 3.0, k = 1.1;
+    IntegratorAngleGPU<4, double, KInterp> I(qp, {{nx, nc}}, xe);
+    for (double p : {0.01, 0.5, 2.0}) {
+      const double got = I.get(k, Z, W, p);
+      const auto &X = qp.get_points<double>(nx), &Xw = qp.get_weights<double>(nx);
+      const auto &A = qp.get_points<double>(nc), &Aw = qp.get_weights<double>(nc);
+      const double Sd = 2 * M_PI * M_PI;
+      double ref = 0;
+      for (uint i = 0; i < nx; ++i) {
+        const double q = k * std::sqrt(X[i] * xe);
+        const double ie = Sd * (q * q / 2 * k * k) * 0.5 / std::pow(2 * M_PI, 4);
+        for (uint j = 0; j < nc; ++j) {
+          const double c = 2 * (A[j] - 0.5);
+          ref += ie * 2 * Aw[j] * Xw[i] * xe * KInterp::kernel(q, c, k, Z, W, p);
+        }
+      }
+      std::printf("INTERP %.17g %.17g\n", got, ref);
+    }
+    // update(): new host values become visible to the next launch
+    for (int i = 0; i < 64; ++i) Z[i] = 2.0f;
+    Z.update();
+    const double after = I.get(k, Z, W, 0.5);
+    double ref2 = 0;
+    {
+      const auto &X = qp.get_points<double>(nx), &Xw = qp.get_weights<double>(nx);
+      const auto &A = qp.get_points<double>(nc), &Aw = qp.get_weights<double>(nc);
+      for (uint i = 0; i < nx; ++i) {
+        const double q = k * std::sqrt(X[i] * xe);
+        const double ie = 2 * M_PI * M_PI * (q * q / 2 * k * k) * 0.5 / std::pow(2 * M_PI, 4);
+        for (uint j = 0; j < nc; ++j)
+          ref2 += ie * 2 * Aw[j] * Xw[i] * xe * KInterp::kernel(q, 2 * (A[j] - 0.5), k, Z, W, 0.5);
+      }
+    }
+    std::printf("INTERP %.17g %.17g\n", after, ref2);
+    return 0;
   }
   if (argc > 1 && std::string(argv[1]) == "--requests") {
     // futures in flight together (pooled streams), then resolved

@@ -75,6 +75,18 @@ def test_all_families_double_and_float(binary, oracle):
         assert abs(got64 - ana) <= tol * max(1.0, abs(ana)), (f, got64, ana)
 
 
+def test_interpolators_inside_user_kernels(binary):
+    """TexLinearInterpolator1D / LinearInterpolator1D objects passed into a KERNEL: device
+    interpolation equals the interpolators' host branch summed over the same quadrature, and
+    update() reaches the next launch."""
+    out = run(binary, [], extra=["--interp"])
+    rows = [l.split()[1:] for l in out if l.startswith("INTERP")]
+    assert len(rows) == 4
+    for a, b in rows:
+        assert abs(float(a) - float(b)) <= 1e-6 * abs(float(b)), (a, b)
+    assert abs(float(rows[3][0]) - float(rows[1][0])) > 1e-3 * abs(float(rows[1][0]))
+
+
 def test_request_futures_match_get(binary):
     out = run(binary, [], extra=["--requests"])
     reqs = [l.split() for l in out if l.startswith("REQ")]
