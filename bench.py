@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--workload", default="C2", choices=["C1", "C2", "C3", "C5"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip the C4 serving measurement")
     return ap.parse_args()
 
 
@@ -167,6 +168,53 @@ def run_reference(args):
                                        "reference CPU integrators, OpenMP over integrals" % (sub.size, n, args.workload)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def serving_c4(device):
+    """C4: one Cash-Karp step (6 right-hand sides x 4096 integrals) of the served flow, with
+    Poisson arrivals at 2000 integrals/s and saturated (each evaluation submitted at once);
+    latency = submit -> result ready, from the library's request loop."""
+    from diffrg_gb300 import serving as SV
+    from diffrg_gb300.engine import Context
+
+    w = SV.c4()
+    ctx = Context(device)
+    ctx.serve_start(8, 2048)
+    f = SV.Flow(ctx, w, rate=None)
+    f.integrals_at(0.0, w["y0"])  # warm-up: arenas, quadrature axes
+    out = {"workload": "C4 served RK45 (Cash-Karp) flow: 32 dressing functions x 128 p, requests of 8-2048 "
+                       "integrals (2D PROP1 / 3D PROP3, GL orders 32-128 per axis), tables updated every stage",
+           "integrals_per_rhs": w["integrals_per_rhs"], "points_per_rhs": w["points_per_rhs"],
+           "max_inflight_batches": 8, "max_batch_items": 2048}
+
+    def one_step(rate):
+        f.rate = rate
+        ctx.reset_stats()
+        r0, i0 = f.requests, f.integrals
+        t0 = time.perf_counter()
+        SV.cash_karp_step(f.rhs, 0.0, w["y0"].copy(), 0.2)
+        wall = time.perf_counter() - t0
+        st = ctx.stats()
+        return {"requests": f.requests - r0, "integrals": f.integrals - i0, "wall_s": wall,
+                "integrals_per_s": (f.integrals - i0) / wall, "p50_ms": st["p50_latency_s"] * 1e3,
+                "p99_ms": st["p99_latency_s"] * 1e3, "max_ms": st["max_latency_s"] * 1e3,
+                "batches": st["batches_launched"], "gpu_busy_frac": st["busy_seconds"] / wall,
+                "rejected": st["rejected"]}
+
+    out["saturated"] = one_step(None)
+    out["poisson"] = one_step(w["rate"])
+    out["poisson"]["offered_integrals_per_s"] = w["rate"]
+    # the reference's pattern on the same integrals: one launch + CUB + sync per integral
+    b = ctx.batch(SV.rhs_items(w, 1.0), f.tlist, "fp64")
+    b.run_plain(16)
+    t0 = time.perf_counter()
+    b.run_plain(16)
+    out["plain_fp64_integrals_per_s"] = b.n / (time.perf_counter() - t0)
+    out["saturated_over_plain_fp64"] = out["saturated"]["integrals_per_s"] / out["plain_fp64_integrals_per_s"]
+    b.close()
+    f.close()
+    ctx.close()
+    return out
 
 
 def main():
@@ -326,6 +374,8 @@ def main():
         if plain is not None:
             err["plain_fp64_max_rel_err_vs_oracle"] = float((np.abs(resp - ref) / np.abs(ref)).max())
 
+    serve = None if args.no_serve else serving_c4(local)
+
     lat_ms = sorted(x * 1e3 for x in lat)
     sl_ms = sorted(x * 1e3 for x in sl)
 
@@ -350,7 +400,11 @@ def main():
             "latency_ms": {"batch_e2e_p50": pct(lat_ms, 0.5), "batch_e2e_p99": pct(lat_ms, 0.99),
                            "single_integral_get_p50": pct(sl_ms, 0.5), "single_integral_get_p99": pct(sl_ms, 0.99)},
             "accuracy": err,
+            "serving": serve,
             "cpu_baseline": cpu}
+    if serve:
+        line["latency_ms"]["serving_c4_p50"] = serve["poisson"]["p50_ms"]
+        line["latency_ms"]["serving_c4_p99"] = serve["poisson"]["p99_ms"]
     if rank == 0:
         print(json.dumps(line))
     b32.close()

@@ -45,7 +45,7 @@ class TableSpec(C.Structure):
 
 
 class Integral(C.Structure):
-    _fields_ = [("family", C.c_int), ("integrand", C.c_int), ("d", C.c_int), ("n", C.c_int * 4),
+    _fields_ = [("family", C.c_int), ("integrand", C.c_int), ("d", C.c_int), ("n", C.c_int * 4), ("table_base", C.c_int),
                 ("x_extent", C.c_double), ("x0_extent", C.c_double), ("x0_summands", C.c_int),
                 ("T", C.c_double), ("E", C.c_double), ("k", C.c_double),
                 ("qmin", C.c_double * 3), ("qmax", C.c_double * 3), ("args", C.c_double * GB_MAX_ARGS)]

@@ -25,11 +25,6 @@ namespace gbint
   }
 } // namespace gbint
 
-#define GB_CUDA(call)                                  \
-  do {                                                 \
-    cudaError_t e__ = (call);                          \
-    if (e__ != cudaSuccess) return cuda_fail(ctx, e__, #call); \
-  } while (0)
 
 namespace
 {
@@ -104,22 +99,72 @@ namespace
     AK_ONE = 10    // single node 0 with weight C
   };
 
+  // first fit in the free list, else the bump region
+  bool pool_take(NodePool &P, int n, int &off)
+  {
+    for (auto it = P.free_ranges.begin(); it != P.free_ranges.end(); ++it)
+      if (it->second >= n) {
+        off = it->first;
+        const int rest = it->second - n;
+        P.free_ranges.erase(it);
+        if (rest) P.free_ranges[off + n] = rest;
+        return true;
+      }
+    if (P.used + n > P.capacity) return false;
+    off = P.used;
+    P.used += n;
+    return true;
+  }
+
+  // drop every axis no batch holds; its range joins the free list (coalesced)
+  void pool_evict_unheld(gb_ctx *ctx)
+  {
+    NodePool &P = ctx->pool;
+    for (auto it = ctx->axis_cache.begin(); it != ctx->axis_cache.end();) {
+      if (it->second.refs == 0) {
+        P.free_ranges[it->second.ref.off] = it->second.ref.n;
+        P.evictions++;
+        it = ctx->axis_cache.erase(it);
+      } else
+        ++it;
+    }
+    for (auto it = P.free_ranges.begin(); it != P.free_ranges.end();) {
+      auto nx = std::next(it);
+      if (nx != P.free_ranges.end() && it->first + it->second == nx->first) {
+        it->second += nx->second;
+        P.free_ranges.erase(nx);
+        continue;
+      }
+      ++it;
+    }
+    if (!P.free_ranges.empty()) {  // a free tail returns to the bump region
+      auto last = std::prev(P.free_ranges.end());
+      if (last->first + last->second == P.used) {
+        P.used = last->first;
+        P.free_ranges.erase(last);
+      }
+    }
+  }
+
   int pool_append(gb_ctx *ctx, const HostAxis &h, AxisRef &ref)
   {
     const int n = (int)h.v.size();
-    if (ctx->pool.used + n > ctx->pool.capacity) return set_error(ctx, GB_ENOMEM, "node pool exhausted");
+    int off = 0;
+    if (!pool_take(ctx->pool, n, off)) {
+      pool_evict_unheld(ctx);
+      if (!pool_take(ctx->pool, n, off))
+        return set_error(ctx, GB_ENOMEM, "node pool exhausted (all axes held by live batches)");
+    }
     std::vector<NodeRec> rec(n);
     for (int i = 0; i < n; ++i) {
       const dev::df v = dev::df_from(h.v[i]), w = dev::df_from(h.w[i]), a = dev::df_from(h.a[i]),
                     aw = dev::df_from(h.w[i] * h.a[i]);
       rec[i] = NodeRec{v.hi, v.lo, w.hi, w.lo, a.hi, a.lo, aw.hi, aw.lo};
     }
-    const int off = ctx->pool.used;
     GB_CUDA(cudaMemcpy(ctx->pool.d_v + off, h.v.data(), n * sizeof(double), cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(ctx->pool.d_w + off, h.w.data(), n * sizeof(double), cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(ctx->pool.d_a + off, h.a.data(), n * sizeof(double), cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(ctx->pool.d_rec + off, rec.data(), n * sizeof(NodeRec), cudaMemcpyHostToDevice));
-    ctx->pool.used += n;
     ref.off = off;
     ref.n = n;
     ref.pm_from = std::min(h.pm_from, n);
@@ -258,22 +303,27 @@ namespace
     return GB_OK;
   }
 
-  int get_axis(gb_ctx *ctx, const AxisKey &key, int role, AxisRef &ref)
+  // the axis of `key` (built and copied into the pool on first use); `hold` (if given) takes a
+  // reference that keeps it from eviction until release_axes
+  int get_axis(gb_ctx *ctx, const AxisKey &key, int role, AxisRef &ref, std::vector<AxisKey> *hold)
   {
     auto it = ctx->axis_cache.find(key);
-    if (it != ctx->axis_cache.end()) {
-      ref = it->second;
-      ref.role = role;
-      return GB_OK;
+    if (it == ctx->axis_cache.end()) {
+      HostAxis h;
+      int rc = build_axis(ctx, key, h);
+      if (rc) return rc;
+      if (h.v.empty()) return set_error(ctx, GB_EINVAL, "empty quadrature axis");
+      AxisRef r{};
+      rc = pool_append(ctx, h, r);
+      if (rc) return rc;
+      it = ctx->axis_cache.emplace(key, AxisEntry{r, 0}).first;
     }
-    HostAxis h;
-    int rc = build_axis(ctx, key, h);
-    if (rc) return rc;
-    if (h.v.empty()) return set_error(ctx, GB_EINVAL, "empty quadrature axis");
-    rc = pool_append(ctx, h, ref);
-    if (rc) return rc;
+    ref = it->second.ref;
     ref.role = role;
-    ctx->axis_cache[key] = ref;
+    if (hold) {
+      it->second.refs++;
+      hold->push_back(key);
+    }
     return GB_OK;
   }
 
@@ -289,7 +339,7 @@ namespace
 
   // Family -> axes.  Every reference int_element / weight factor is folded into the axes
   // (constants into the radial axis).  Sources per family in gbint.h.
-  int family_axes(gb_ctx *ctx, const gb_integral &g, AxisRef ax[4], int &na)
+  int family_axes(gb_ctx *ctx, const gb_integral &g, AxisRef ax[4], int &na, std::vector<AxisKey> *hold)
   {
     const double k = g.k, xe = g.x_extent, tp = 2 * kPi;
     const int d = g.d;
@@ -299,7 +349,7 @@ namespace
       if (key.kind != AK_MATS && key.kind != AK_FTX0 && key.kind != AK_ONE && key.kind != AK_MODES &&
           (key.n <= 0 || key.n > 4096))
         return set_error(ctx, GB_EINVAL, "quadrature order out of range (1..4096)");
-      int rc = get_axis(ctx, key, role, ax[na]);
+      int rc = get_axis(ctx, key, role, ax[na], hold);
       if (rc) return rc;
       ++na;
       return GB_OK;
@@ -443,30 +493,47 @@ namespace
 // ============================================================================ batches
 namespace gbint
 {
+  void release_axes(gb_ctx *ctx, std::vector<AxisKey> &held)
+  {
+    for (const AxisKey &k : held) {
+      auto it = ctx->axis_cache.find(k);
+      if (it != ctx->axis_cache.end() && it->second.refs > 0) it->second.refs--;
+    }
+    held.clear();
+  }
+
   void free_batch(gb_ctx *ctx, gb_batch *b)
   {
     if (!b) return;
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    cudaFree(b->d_items);
-    cudaFree(b->d_units);
-    cudaFree(b->d_segs);
-    cudaFree(b->d_seg);
-    cudaFree(b->d_partials);
-    cudaFree(b->d_item_count);
-    cudaFree(b->d_counters);
-    cudaFree(b->d_out);
-    if (ctx) ctx->in_use -= b->bytes;
+    if (!b->arena) {
+      cudaFree(b->d_items);
+      cudaFree(b->d_units);
+      cudaFree(b->d_segs);
+      cudaFree(b->d_seg);
+      cudaFree(b->d_partials);
+      cudaFree(b->d_item_count);
+      cudaFree(b->d_counters);
+      cudaFree(b->d_out);
+      if (ctx) ctx->in_use -= b->bytes;
+    }
+    if (ctx) release_axes(ctx, b->held);
     delete b;
   }
 
-  int build_batch(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
-                  gb_batch **out)
+  size_t batch_device_bytes(const gb_batch *b)
   {
-    if (!ctx || !out || n <= 0 || !items) return set_error(ctx, GB_EINVAL, "bad batch arguments");
+    const size_t n = b->n, nu = b->units.size();
+    return n * sizeof(ItemDev) + nu * sizeof(UnitDev) + b->segs.size() * sizeof(SegDev) +
+           b->seg_total * sizeof(double) + nu * sizeof(double) + n * sizeof(int) + b->runs.size() * sizeof(int) +
+           n * sizeof(double);
+  }
+
+  int plan_batch(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *const *item_tables,
+                 const int *item_ntables, int precision, gb_batch *b)
+  {
+    if (!ctx || n <= 0 || !items) return set_error(ctx, GB_EINVAL, "bad batch arguments");
     if (precision < GB_PREC_FP32C || precision > GB_PREC_FP32A) return set_error(ctx, GB_EINVAL, "bad precision");
-    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-    GB_CUDA(cudaSetDevice(ctx->device));
-    auto b = std::make_unique<gb_batch>();
     b->n = n;
     b->precision = precision;
     b->src.assign(items, items + n);
@@ -484,9 +551,13 @@ namespace gbint
       if (g.integrand != GB_IG_POLY && g.integrand != GB_IG_PROP1 && g.integrand != GB_IG_PROP3 &&
           g.integrand != GB_IG_VERT4 && g.integrand != GB_IG_FTLOOP)
         return set_error(ctx, GB_EINVAL, "unknown integrand");
-      int rc = family_axes(ctx, g, it.ax, it.n_axes);
+      int rc = family_axes(ctx, g, it.ax, it.n_axes, &b->held);
       if (rc) return rc;
       // tables
+      if (g.table_base < 0 || g.table_base > item_ntables[i])
+        return set_error(ctx, GB_EINVAL, "table_base outside the table list");
+      gb_table *const *tables = item_tables[i] ? item_tables[i] + g.table_base : nullptr;
+      const int n_tables = item_ntables[i] - g.table_base;
       const int nt = tables_needed(g.integrand);
       if (nt > n_tables) return set_error(ctx, GB_EINVAL, "integrand needs more tables than given");
       for (int t = 0; t < 4; ++t) it.tab[t] = -1;
@@ -644,34 +715,55 @@ namespace gbint
       }
       b->runs.push_back(run);
     }
+    return GB_OK;
+  }
+
+  int build_batch(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
+                  gb_batch **out)
+  {
+    if (!ctx || !out || n <= 0 || !items) return set_error(ctx, GB_EINVAL, "bad batch arguments");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    GB_CUDA(cudaSetDevice(ctx->device));
+    std::vector<gb_table *const *> tl(n, tables);
+    std::vector<int> tn(n, n_tables);
+    gb_batch *b = new gb_batch();
+    int rc = plan_batch(ctx, items, n, tl.data(), tn.data(), precision, b);
+    if (rc) {
+      free_batch(ctx, b);
+      return rc;
+    }
     // device buffers
     const size_t nu = b->units.size();
-    size_t bytes = n * sizeof(ItemDev) + nu * sizeof(UnitDev) + b->segs.size() * sizeof(SegDev) +
-                   b->seg_total * sizeof(double) + nu * sizeof(double) + n * sizeof(int) +
-                   b->runs.size() * sizeof(int) + n * sizeof(double);
-    if (ctx->in_use + bytes > ctx->budget) return set_error(ctx, GB_EBUDGET, "batch exceeds the HBM budget");
-    auto alloc = [&](void **p, size_t sz) -> int {
-      GB_CUDA(cudaMalloc(p, std::max<size_t>(sz, 16)));
-      return GB_OK;
+    const size_t bytes = batch_device_bytes(b);
+    if (ctx->in_use + bytes > ctx->budget) {
+      free_batch(ctx, b);
+      return set_error(ctx, GB_EBUDGET, "batch exceeds the HBM budget");
+    }
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](void **p, size_t sz) {
+      if (e == cudaSuccess) e = cudaMalloc(p, std::max<size_t>(sz, 16));
     };
-    int rc;
-    if ((rc = alloc((void **)&b->d_items, n * sizeof(ItemDev)))) return rc;
-    if ((rc = alloc((void **)&b->d_units, nu * sizeof(UnitDev)))) { free_batch(nullptr, b.release()); return rc; }
-    if ((rc = alloc((void **)&b->d_segs, b->segs.size() * sizeof(SegDev)))) { free_batch(nullptr, b.release()); return rc; }
-    if ((rc = alloc((void **)&b->d_seg, b->seg_total * sizeof(double)))) { free_batch(nullptr, b.release()); return rc; }
-    if ((rc = alloc((void **)&b->d_partials, nu * sizeof(double)))) { free_batch(nullptr, b.release()); return rc; }
-    if ((rc = alloc((void **)&b->d_item_count, n * sizeof(int)))) { free_batch(nullptr, b.release()); return rc; }
-    if ((rc = alloc((void **)&b->d_counters, b->runs.size() * sizeof(int)))) { free_batch(nullptr, b.release()); return rc; }
-    if ((rc = alloc((void **)&b->d_out, n * sizeof(double)))) { free_batch(nullptr, b.release()); return rc; }
+    alloc((void **)&b->d_items, n * sizeof(ItemDev));
+    alloc((void **)&b->d_units, nu * sizeof(UnitDev));
+    alloc((void **)&b->d_segs, b->segs.size() * sizeof(SegDev));
+    alloc((void **)&b->d_seg, b->seg_total * sizeof(double));
+    alloc((void **)&b->d_partials, nu * sizeof(double));
+    alloc((void **)&b->d_item_count, n * sizeof(int));
+    alloc((void **)&b->d_counters, b->runs.size() * sizeof(int));
+    alloc((void **)&b->d_out, n * sizeof(double));
     b->bytes = bytes;
     ctx->in_use += bytes;
-    GB_CUDA(cudaMemcpy(b->d_items, b->items.data(), n * sizeof(ItemDev), cudaMemcpyHostToDevice));
-    GB_CUDA(cudaMemcpy(b->d_units, b->units.data(), nu * sizeof(UnitDev), cudaMemcpyHostToDevice));
-    if (!b->segs.empty())
-      GB_CUDA(cudaMemcpy(b->d_segs, b->segs.data(), b->segs.size() * sizeof(SegDev), cudaMemcpyHostToDevice));
-    GB_CUDA(cudaMemset(b->d_item_count, 0, n * sizeof(int)));
-    GB_CUDA(cudaMemset(b->d_out, 0, n * sizeof(double)));
-    *out = b.release();
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_items, b->items.data(), n * sizeof(ItemDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_units, b->units.data(), nu * sizeof(UnitDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !b->segs.empty())
+      e = cudaMemcpy(b->d_segs, b->segs.data(), b->segs.size() * sizeof(SegDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(b->d_item_count, 0, n * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(b->d_out, 0, n * sizeof(double));
+    if (e != cudaSuccess) {
+      free_batch(ctx, b);
+      return cuda_fail(ctx, e, "batch device buffers");
+    }
+    *out = b;
     return GB_OK;
   }
 
@@ -710,18 +802,21 @@ namespace gbint
   // pool (pre-allocated; new quadrature orders are copied in, nothing is allocated on the device)
   // and table directory slots.  Caller holds ctx->mu.
   int prepare_item_fp64(gb_ctx *ctx, const gb_integral &g, gb_table *const *tables, int n_tables, ItemDev &it,
-                        uint64_t &grid_points)
+                        uint64_t &grid_points, std::vector<AxisKey> &hold)
   {
     std::memset(&it, 0, sizeof(it));
     if (g.integrand != GB_IG_POLY && g.integrand != GB_IG_PROP1 && g.integrand != GB_IG_PROP3 &&
         g.integrand != GB_IG_VERT4 && g.integrand != GB_IG_FTLOOP)
       return set_error(ctx, GB_EINVAL, "unknown integrand");
+    if (g.table_base < 0 || g.table_base > n_tables) return set_error(ctx, GB_EINVAL, "table_base outside the table list");
+    if (tables) tables += g.table_base;
+    n_tables -= g.table_base;
     it.kind = K_GENERIC;
     it.integrand = g.integrand;
     it.family = g.family;
     it.k = g.k;
     std::memcpy(it.args, g.args, sizeof(it.args));
-    int rc = family_axes(ctx, g, it.ax, it.n_axes);
+    int rc = family_axes(ctx, g, it.ax, it.n_axes, &hold);
     if (rc) return rc;
     const int nt = tables_needed(g.integrand);
     if (nt > n_tables) return set_error(ctx, GB_EINVAL, "integrand needs more tables than given");
@@ -781,6 +876,7 @@ int gb_ctx_create(int device, size_t budget, gb_ctx **out)
   CK(cudaSetDevice(device));
   CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&c->tables_event, cudaEventDisableTiming));
   c->pool_streams.resize(kPoolStreams);
   for (auto &s : c->pool_streams) CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   c->pool.capacity = kPoolCapacity;
@@ -846,6 +942,7 @@ int gb_ctx_destroy(gb_ctx *ctx)
   cudaFree(ctx->d_err);
   for (auto s : ctx->pool_streams) cudaStreamDestroy(s);
   cudaStreamDestroy(ctx->stream);
+  cudaEventDestroy(ctx->tables_event);
   delete ctx;
   return GB_OK;
 }
@@ -993,12 +1090,18 @@ static int table_update_impl(gb_ctx *ctx, gb_table *t, const float *src, cudaMem
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   GB_CUDA(cudaSetDevice(ctx->device));
   const int back = t->front ^ 1;
+  // serving batches still reading the back buffer (an older epoch) finish first
+  if (ctx->serve) {
+    const int rc = serve_fence_tables(ctx, s);
+    if (rc) return rc;
+  }
   GB_CUDA(cudaMemcpyAsync(t->buf[back], src, (size_t)t->elems * 4, kind, s));
   // publish the new buffer in the directory, ordered after the data on the same stream
   TableDev &D = ctx->h_dir[t->slot];
   D.data = t->buf[back];
   GB_CUDA(cudaMemcpyAsync(ctx->d_dir + t->slot, &D, sizeof(TableDev), cudaMemcpyHostToDevice, s));
   // the pageable host source (h_dir entry) is staged by the runtime before the call returns
+  GB_CUDA(cudaEventRecord(ctx->tables_event, s));
   t->front = back;
   t->epoch++;
   return GB_OK;

@@ -50,11 +50,20 @@ namespace gbint
     float *d32x = nullptr, *d32w = nullptr;
   };
 
-  // device pool of axis nodes (FP64 arrays + 32-byte FP32 records); offsets never move
+  // device pool of axis nodes (FP64 arrays + 32-byte FP32 records).  An axis keeps its offset
+  // while any batch holds it; unheld axes are evicted (their ranges go to the free list) only
+  // when an allocation would otherwise fail.
   struct NodePool {
     int capacity = 0, used = 0;
     double *d_v = nullptr, *d_w = nullptr, *d_a = nullptr;
     NodeRec *d_rec = nullptr;
+    std::map<int, int> free_ranges;  // offset -> length
+    uint64_t evictions = 0;
+  };
+
+  struct AxisEntry {
+    AxisRef ref;
+    int refs = 0;  // batches (and in-progress calls) holding the axis
   };
 
   struct Ticket;
@@ -103,6 +112,9 @@ struct gb_batch {
   // graph replay
   cudaGraphExec_t graph = nullptr;
   cudaStream_t graph_stream = nullptr;
+  // axes held in the node pool while the batch exists
+  std::vector<gbint::AxisKey> held;
+  bool arena = false;  // device buffers belong to a serving slot (not freed with the batch)
 };
 
 struct gb_ctx {
@@ -120,11 +132,12 @@ struct gb_ctx {
   std::vector<std::unique_ptr<gbint::MatsEntry>> mats;
   // nodes
   gbint::NodePool pool;
-  std::map<gbint::AxisKey, gbint::AxisRef> axis_cache;
+  std::map<gbint::AxisKey, gbint::AxisEntry> axis_cache;
   // tables
   gbint::TableDev *d_dir = nullptr;
   std::vector<gbint::TableDev> h_dir;
   std::vector<gb_table *> slots;
+  cudaEvent_t tables_event = nullptr;  // recorded after every table update (serving orders on it)
   int *d_err = nullptr;
   // kind -> thread override (autotuner)
   int threads_override[16] = {};  // [base kind + 8 * accurate]
@@ -149,6 +162,14 @@ namespace gbint
   int cuda_fail(gb_ctx *ctx, cudaError_t e, const char *what);
   int build_batch(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
                   gb_batch **out);
+  // host half of build_batch: descriptors, units, segments, kind runs; item i reads the
+  // tables item_tables[i][0..item_ntables[i]).  Caller holds ctx->mu; b->held keeps the axes.
+  int plan_batch(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *const *item_tables,
+                 const int *item_ntables, int precision, gb_batch *b);
+  size_t batch_device_bytes(const gb_batch *b);
+  void release_axes(gb_ctx *ctx, std::vector<AxisKey> &held);
+  // the table-update stream waits for in-flight serving batches (double-buffer reuse)
+  int serve_fence_tables(gb_ctx *ctx, cudaStream_t s);
   int run_batch(gb_ctx *ctx, gb_batch *b, double *d_out, cudaStream_t s);
   void free_batch(gb_ctx *ctx, gb_batch *b);
   // serving
@@ -162,3 +183,10 @@ namespace gbint
   int serve_reset_stats(gb_ctx *ctx);
   void destroy_slots(gb_ctx *ctx);
 } // namespace gbint
+
+// return the CUDA failure (with the failing call's text) from a function that has `ctx`
+#define GB_CUDA(call)                                           \
+  do {                                                          \
+    cudaError_t e__ = (call);                                   \
+    if (e__ != cudaSuccess) return gbint::cuda_fail(ctx, e__, #call); \
+  } while (0)

@@ -33,7 +33,7 @@
 namespace gbint
 {
   int prepare_item_fp64(gb_ctx *ctx, const gb_integral &g, gb_table *const *tables, int n_tables, ItemDev &it,
-                        uint64_t &grid_points);
+                        uint64_t &grid_points, std::vector<AxisKey> &hold);
 
   namespace
   {
@@ -149,7 +149,14 @@ extern "C" int gb_get_noalloc(gb_ctx *ctx, const gb_integral *item, gb_table *co
   if (rc) return rc;
   ItemDev it;
   uint64_t points = 0;
-  rc = prepare_item_fp64(ctx, *item, tables, n_tables, it, points);
+  // the axes stay held (not evictable) until the result is back; the node pool keeps its
+  // pre-allocated capacity, so this holds no device memory of its own
+  struct Hold {
+    gb_ctx *c;
+    std::vector<AxisKey> keys;
+    ~Hold() { release_axes(c, keys); }
+  } hold{ctx, {}};
+  rc = prepare_item_fp64(ctx, *item, tables, n_tables, it, points, hold.keys);
   if (rc) return rc;
   if (points > (uint64_t)GB_NOALLOC_MAX_POINTS)
     return set_error(ctx, GB_EINVAL,

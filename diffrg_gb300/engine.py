@@ -19,8 +19,8 @@ from .capi import FAM, IG, PREC, GbError, Integral, TableSpec
 
 
 def integral(family, integrand="POLY", n=(0, 0, 0, 0), k=1.0, d=4, x_extent=1.0, x0_extent=0.0, x0_summands=0,
-             T=0.0, E=0.0, qmin=(-np.pi,) * 3, qmax=(np.pi,) * 3, args=()) -> Integral:
-    """Descriptor of one integral (gb_integral)."""
+             T=0.0, E=0.0, qmin=(-np.pi,) * 3, qmax=(np.pi,) * 3, args=(), table_base=0) -> Integral:
+    """Descriptor of one integral (gb_integral); it reads tables[table_base:] of its batch."""
     g = Integral()
     g.family = FAM[family] if isinstance(family, str) else int(family)
     g.integrand = IG[integrand] if isinstance(integrand, str) else int(integrand)
@@ -28,6 +28,7 @@ def integral(family, integrand="POLY", n=(0, 0, 0, 0), k=1.0, d=4, x_extent=1.0,
     nn = list(n) + [0] * (4 - len(n))
     for i in range(4):
         g.n[i] = int(nn[i])
+    g.table_base = int(table_base)
     g.x_extent = x_extent
     g.x0_extent = x0_extent
     g.x0_summands = int(x0_summands)
@@ -132,6 +133,37 @@ class Batch:
             self.h = None
 
 
+class Ticket:
+    """A submitted request: poll() / wait() return its results (float64, one per integral)."""
+
+    def __init__(self, ctx: "Context", tid: int, n: int):
+        self.ctx = ctx
+        self.id = tid
+        self.n = n
+
+    def poll(self):
+        """The results if the request is finished, else None."""
+        out = np.zeros(self.n)
+        rc = capi.lib().gb_poll(self.ctx.h, self.id, capi._dp(out))
+        if rc == capi.GB_EAGAIN:
+            return None
+        self.ctx.check(rc)
+        return out
+
+    def wait(self, timeout: float = 0.0) -> np.ndarray:
+        out = np.zeros(self.n)
+        self.ctx.check(capi.lib().gb_wait(self.ctx.h, self.id, capi._dp(out), timeout))
+        return out
+
+    def cancel(self) -> bool:
+        """True if the request was still queued and is now canceled."""
+        rc = capi.lib().gb_cancel(self.ctx.h, self.id)
+        if rc == capi.GB_EAGAIN:
+            return False
+        self.ctx.check(rc)
+        return True
+
+
 class Context:
     """One device context (gb_ctx): provider caches, node pool, table directory, streams."""
 
@@ -189,6 +221,32 @@ class Context:
         self.check(capi.lib().gb_get(self.h, C.byref(g), _table_array(tables), len(tables), PREC[precision],
                                      C.byref(out)))
         return out.value
+
+    # serving (continuous batching)
+    def serve_start(self, max_inflight: int = 8, max_items: int = 2048):
+        """Start the request loop: up to `max_inflight` device batches in flight, each merging
+        queued requests up to `max_items` integrals."""
+        self.check(capi.lib().gb_serve_start(self.h, max_inflight, max_items))
+
+    def serve_stop(self):
+        self.check(capi.lib().gb_serve_stop(self.h))
+
+    def submit(self, integrals: Sequence[Integral], tables: Sequence[Table] = (), precision: str = "fp32c") -> "Ticket":
+        """Queue one request (the integrals of one request() fan-out); returns its ticket."""
+        n = len(integrals)
+        arr = (Integral * n)(*integrals)
+        t = C.c_uint64()
+        self.check(capi.lib().gb_submit(self.h, arr, n, _table_array(tables), len(tables), PREC[precision],
+                                        C.byref(t)))
+        return Ticket(self, int(t.value), n)
+
+    def stats(self) -> dict:
+        st = capi.Stats()
+        self.check(capi.lib().gb_get_stats(self.h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in capi.Stats._fields_}
+
+    def reset_stats(self):
+        self.check(capi.lib().gb_reset_stats(self.h))
 
     def measure_peaks(self):
         """(FP32 TFLOP/s, MUFU G op/s, FP64 TFLOP/s) of this GPU from the library's probes."""

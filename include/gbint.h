@@ -114,6 +114,7 @@ typedef struct {
   int integrand;   /* GB_IG_*                                                              */
   int d;           /* template dimension of IntegratorGPU<d>, IntegratorAngleGPU<d>, ...     */
   int n[4];        /* grid_sizes (finite-T x0: spatial orders then the tail order)           */
+  int table_base;  /* the integral reads tables[table_base ...] of its batch/request (0: first) */
   double x_extent; /* x = q^2/k^2 in [0, x_extent]; qmax for GB_FAM_QLOOP*                   */
   double x0_extent;/* q0_extent (pq0), x0_extent (px0, finite-T x0)                          */
   int x0_summands; /* explicit Matsubara terms (finite-T x0); M for GB_FAM_QLOOP_T            */
@@ -234,9 +235,23 @@ int gb_slot_release(gb_ctx *ctx, const gb_slot *slot);
 int gb_device_info(gb_ctx *ctx, int *device, int *num_sms);
 
 /* ------------------------------------------------------------------ serving (request loop)
- * request(): admit n integrals to the continuously batching loop; work that arrives while
- * other batches are on the GPU is launched on another stream as soon as a slot and budget
- * allow.  Tables are read at launch time (their latest epoch). */
+ * Replaces the request()/get() fan-out of a flow's right-hand side (physics/utils.hh:31-147;
+ * integrator request() launches, e.g. integration/integrator_angle_gpu.hh:166-219) with one
+ * continuously batching loop per context.
+ * gb_serve_start: up to max_inflight_batches device batches in flight (1..64); a batch merges
+ *   consecutive queued requests of one precision up to max_batch_items integrals.
+ * gb_submit: queue one request of n integrals (tables: that request's tables, as in
+ *   gb_batch_create); returns a ticket at once.  Work that arrives while other batches are
+ *   on the GPU is launched on another stream as soon as a slot frees and its buffers fit the
+ *   HBM budget (GB_EBUDGET: a request that can never fit).  A batch starts after the latest
+ *   gb_table_update issued before it and reads one epoch of every table; a table update
+ *   waits for batches in flight.
+ * gb_poll: GB_OK and n results in out, GB_EAGAIN while pending; the ticket is consumed on any
+ *   other return.  gb_wait blocks (timeout_s <= 0: no limit; GB_ETIMEDOUT keeps the ticket).
+ * gb_cancel: GB_OK if still queued (its gb_poll then returns GB_ECANCELED), GB_EAGAIN if it
+ *   already runs.
+ * gb_get_stats: counts, busy time, p50/p99/max latency (submit -> result ready, nearest rank)
+ *   since gb_serve_start / gb_reset_stats, and the budget in use. */
 int gb_serve_start(gb_ctx *ctx, int max_inflight_batches, int max_batch_items);
 int gb_serve_stop(gb_ctx *ctx);
 int gb_submit(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,

@@ -1,0 +1,232 @@
+"""GPU: the continuously batching request loop (gb_serve_* / gb_submit / gb_wait).
+
+* served results equal the same integrals run as one gb_batch, bit for bit, and the FP64
+  oracle within 1e-9 (FP32-compensated) / 1e-12 (FP64);
+* a request gives bit-identical results alone and in a mix of concurrent requests;
+* a request in flight reads one table epoch, never a mixture (table updates are ordered);
+* cancel / poll / unknown tickets / HBM-budget admission;
+* the node pool evicts unheld axes, so an RG flow with a new k per stage never runs out;
+* one Cash-Karp step of the C4 flow, FP32-compensated against FP64.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from diffrg_gb300 import capi, serving
+from diffrg_gb300.capi import GbError
+from diffrg_gb300.engine import Context, integral
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def w():
+    return serving.c4()
+
+
+@pytest.fixture(scope="module")
+def sctx(gblib):
+    c = Context(0)
+    c.serve_start(8, 2048)
+    yield c
+    c.serve_stop()
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def tabs(sctx, w):
+    ts = [sctx.table(w["spec"], w["y0"][i]) for i in range(serving.N_FUNC)]
+    return ts, [ts[i] for i in serving.table_order()]
+
+
+def serve_all(ctx, items, tlist, sizes, precision="fp32c"):
+    tk = []
+    off = 0
+    for s in sizes:
+        tk.append((off, ctx.submit(items[off:off + s], tlist, precision)))
+        off += s
+    out = np.empty(len(items))
+    for o, t in tk:
+        out[o:o + t.n] = t.wait(timeout=300)
+    return out
+
+
+def test_served_equals_batch_and_oracle(sctx, tabs, w, oracle):
+    _, tlist = tabs
+    k = 0.7
+    items = serving.rhs_items(w, k)
+    sizes = serving.request_sizes(np.random.default_rng(3), len(items), 8, 2048)
+    served = serve_all(sctx, items, tlist, sizes)
+    b = sctx.batch(items, tlist, "fp32c")
+    ref = b.get()
+    b.close()
+    assert np.array_equal(served, ref)
+    pairs = [(i, j) for i in range(0, 32, 5) for j in (0, 77, 127)]
+    want = serving.oracle_subset(oracle, w, w["y0"], k, pairs)
+    got = np.array([served[i * 128 + j] for i, j in pairs])
+    err = np.abs(got - want) / np.abs(want)
+    assert np.max(err) <= 1e-9, err
+
+
+def test_fp64_requests_match_oracle(sctx, tabs, w, oracle):
+    _, tlist = tabs
+    k = 0.9
+    items = serving.rhs_items(w, k)
+    pairs = [(0, 5), (1, 60), (6, 127), (11, 0)]
+    sub = [items[i * 128 + j] for i, j in pairs]
+    got = sctx.submit(sub, tlist, "fp64").wait(timeout=300)
+    want = serving.oracle_subset(oracle, w, w["y0"], k, pairs)
+    assert np.max(np.abs(got - want) / np.abs(want)) <= 1e-12
+
+
+def test_alone_equals_in_mix_bitwise(sctx, tabs, w):
+    _, tlist = tabs
+    items = serving.rhs_items(w, 0.55)
+    probe = items[1000:1100]  # crosses function boundaries: 2D and 3D integrals, many tables
+    alone = sctx.submit(probe, tlist).wait(timeout=300)
+    sctx.reset_stats()
+    rng = np.random.default_rng(11)
+    for rep in range(3):
+        tk = []
+        order = rng.permutation(6)
+        for m in order:
+            lo = int(m) * 600
+            tk.append(sctx.submit(items[lo:lo + 600], tlist))
+            if m == 2:
+                tk.append(("probe", sctx.submit(probe, tlist)))
+        mixed = None
+        for t in tk:
+            if isinstance(t, tuple):
+                mixed = t[1].wait(timeout=300)
+            else:
+                t.wait(timeout=300)
+        assert np.array_equal(mixed, alone), rep
+    st = sctx.stats()
+    assert st["completed"] == 21 and st["batches_launched"] >= 2
+    assert 0 < st["p50_latency_s"] <= st["p99_latency_s"] <= st["max_latency_s"]
+
+
+def test_request_reads_one_table_epoch(sctx, tabs, w):
+    ts, tlist = tabs
+    items = serving.rhs_items(w, 0.8)[1024:3072]
+    yA = w["y0"]
+    yB = np.clip(w["y0"] * 1.07, 0.5, 1.5)
+    for i in range(serving.N_FUNC):
+        ts[i].update(yA[i])
+    bA = sctx.batch(items, tlist).get()
+    for i in range(serving.N_FUNC):
+        ts[i].update(yB[i])
+    bB = sctx.batch(items, tlist).get()
+    assert not np.array_equal(bA, bB)
+    for rep in range(3):
+        for i in range(serving.N_FUNC):
+            ts[i].update(yA[i])
+        t1 = sctx.submit(items, tlist)
+        for i in range(serving.N_FUNC):  # issued while t1 is queued or running
+            ts[i].update(yB[i])
+        t2 = sctx.submit(items, tlist)
+        r1 = t1.wait(timeout=300)
+        r2 = t2.wait(timeout=300)
+        assert np.array_equal(r1, bA) or np.array_equal(r1, bB), rep
+        assert np.array_equal(r2, bB), rep
+    for i in range(serving.N_FUNC):
+        ts[i].update(w["y0"][i])
+
+
+def test_poll_cancel_and_tickets(gblib, w):
+    c = Context(0)
+    try:
+        c.serve_start(1, 2048)
+        ts = [c.table(w["spec"], w["y0"][i]) for i in range(serving.N_FUNC)]
+        tlist = [ts[i] for i in serving.table_order()]
+        items = serving.rhs_items(w, 0.6)
+        big = c.submit(items[128:2176], tlist, "fp32c")  # ~0.5e9 points on the one slot
+        small = c.submit(items[:8], tlist, "fp64")  # another precision: its own batch
+        canceled = small.cancel()
+        r = big.poll()
+        assert r is None or r.shape == (2048,)
+        big_res = big.wait(timeout=300) if r is None else r
+        assert np.all(np.isfinite(big_res))
+        if canceled:
+            with pytest.raises(GbError) as e:
+                small.wait(timeout=60)
+            assert e.value.code == capi.GB_ECANCELED
+        else:
+            assert np.all(np.isfinite(small.wait(timeout=60)))
+        with pytest.raises(GbError) as e:  # a consumed ticket is unknown
+            big.wait(timeout=1)
+        assert e.value.code == capi.GB_EINVAL
+        # a finished request stays pollable until consumed
+        t = c.submit(items[:8], tlist)
+        res = t.wait(timeout=60)
+        assert res.shape == (8,)
+    finally:
+        c.close()
+
+
+def test_hbm_budget_admission(gblib, w):
+    c = Context(0, budget_bytes=1 << 20)
+    try:
+        c.serve_start(2, 8192)
+        ts = [c.table(w["spec"], w["y0"][i]) for i in range(serving.N_FUNC)]
+        tlist = [ts[i] for i in serving.table_order()]
+        items = serving.rhs_items(w, 0.6)
+        with pytest.raises(GbError) as e:  # descriptors alone exceed the budget
+            c.submit(items, tlist)
+        assert e.value.code == capi.GB_EBUDGET
+        # fits at submit, but its work units (3D integrals) do not fit the budget at launch
+        t = c.submit(items[:2048], tlist)
+        with pytest.raises(GbError) as e:
+            t.wait(timeout=120)
+        assert e.value.code == capi.GB_EBUDGET
+        ok = c.submit(items[:16], tlist).wait(timeout=60)
+        assert np.all(np.isfinite(ok))
+        st = c.stats()
+        assert st["rejected"] >= 2 and st["bytes_in_use"] <= st["bytes_budget"]
+    finally:
+        c.close()
+
+
+def test_node_pool_evicts_unheld_axes(ctx, oracle):
+    """600 RG scales x a 4096-node radial axis exceed the 2^21-node pool: unheld axes are
+    evicted and reused; a batch built before the churn keeps its axes and its result."""
+    from diffrg_gb300.workloads import poly_args
+
+    args = poly_args(q=(1.0, 0.5, 0, 0, 0, 0))
+    g0 = integral("1D", "POLY", d=3, n=(4096,), k=0.5, x_extent=2.0, args=args)
+    keep = ctx.batch([g0], precision="fp64")
+    v0 = keep.get()[0]
+    for m in range(600):
+        k = 0.5 + 1e-3 * (m + 1)
+        b = ctx.batch([integral("1D", "POLY", d=3, n=(4096,), k=k, x_extent=2.0, args=args)], precision="fp64")
+        v = b.get()[0]
+        b.close()
+        if m % 150 == 0:
+            d = oracle.family_desc("1D", d=3, n=(4096,), x_extent=2.0)
+            want = oracle.family(d, "POLY", k, args[None, :])[0]
+            assert abs(v - want) <= 1e-12 * abs(want)
+    assert keep.get()[0] == v0
+    keep.close()
+
+
+def test_c4_flow_step_fp32c_vs_fp64(gblib, w):
+    c = Context(0)
+    try:
+        c.serve_start(8, 2048)
+        out = {}
+        for prec in ("fp32c", "fp64"):
+            f = serving.Flow(c, w, precision=prec, rate=None)
+            y, err = serving.cash_karp_step(f.rhs, 0.0, w["y0"].copy(), 0.2)
+            out[prec] = y
+            assert f.rhs_evals == 6 and f.integrals == 6 * 4096
+            f.close()
+        y32, y64 = out["fp32c"], out["fp64"]
+        assert np.all(np.isfinite(y32)) and 0.4 < y32.min() and y32.max() < 1.6
+        # stage values enter the tables rounded to FP32, so a 1e-10 difference between the two
+        # runs can flip one table entry by an FP32 ulp (6e-8) at a later stage
+        assert np.max(np.abs(y32 - y64) / np.abs(y64)) <= 1e-8
+        st = c.stats()
+        assert st["completed"] >= 2 * 6 * 2 and st["rejected"] == 0
+    finally:
+        c.close()
