@@ -252,7 +252,10 @@ namespace gbint
       int j0[2];
       float fy0[2];
       df w2[2];
-      const int ns = pm ? 2 : 1;
+      // With Om = 0 the +-w evaluations read |w| and w^2 only: they are bitwise equal, so one
+      // evaluation is doubled (exact) instead of computing the second.
+      const bool twin = pm && Om == 0.0;
+      const int ns = pm && !twin ? 2 : 1;
       for (int s = 0; s < 2; ++s) {
         const double ws = (s == 0 ? w : -w) + Om;
         int jj;
@@ -276,6 +279,7 @@ namespace gbint
             const float den = __fmaf_rn(z, __fadd_rn(__fadd_rn(w2[s].hi, x2), w2[s].lo), R);
             gsum = __fadd_rn(gsum, rcp32(den));
           }
+          if (twin) gsum = __fadd_rn(gsum, gsum);
           k.add(__fmaf_rn(r.w_hi, gsum, __fmul_rn(r.w_lo, gsum)));
         }
         return P.seg[it.seg_off + row] * k.value();
@@ -293,6 +297,7 @@ namespace gbint
             const df z = bil_df_v1(tab, n1, j0[s], fy0[s], jq, fq);
             gsum = df_add(gsum, df_rcp(df_add(df_mul(z, df_add(w2[s], x2)), R)));
           }
+          if (twin) gsum = df_add(gsum, gsum);
           k.add(df_mul(rec_w(r), gsum));
         }
         return P.seg[it.seg_off + row] * k.value();

@@ -172,6 +172,49 @@ def test_reference_pattern_matches_oracle(ctx, oracle, W, name):
     assert np.max(rel(got, ref)) <= TOL64
 
 
+def c2_items_with_omega(W, w, Om):
+    from diffrg_gb300.engine import integral
+
+    return [integral("QLOOP_T", "FTLOOP", n=(w["nq"], w["nc"]), k=1.0, x_extent=w["qmax"], x0_summands=w["M"],
+                     T=T, args=(0.0, p, T, Om)) for p, T in zip(w["p"], w["T"])]
+
+
+@pytest.mark.parametrize("prec", ["fp32c", "fp32f", "fp64"])
+def test_c2_twin_signs_are_bitwise_the_two_sign_sum(ctx, W, prec):
+    """Omega = 0: the +-w evaluations of the finite-T loop are one doubled evaluation; a
+    negligible Omega (1e-300, which leaves every w +- Omega unchanged) takes the two-sign path
+    and must give the same bits."""
+    w = subset(W, "C2")
+    _, tabs = W.engine_items(w)
+    T = [ctx.table(s, d) for s, d in tabs]
+    out = []
+    for Om in (0.0, 1e-300):
+        b = ctx.batch(c2_items_with_omega(W, w, Om), T, prec)
+        out.append(b.get())
+        b.close()
+    for t in T:
+        t.close()
+    assert np.array_equal(out[0], out[1])
+
+
+def test_c2_nonzero_external_frequency_matches_oracle(ctx, oracle, W):
+    w = subset(W, "C2")
+    _, tabs = W.engine_items(w)
+    T = [ctx.table(s, d) for s, d in tabs]
+    Om = 2 * math.pi * 0.2 * 3  # a bosonic external frequency of the T = 0.2 rows
+    b = ctx.batch(c2_items_with_omega(W, w, Om), T, "fp32c")
+    got = b.get()
+    b.close()
+    b = ctx.batch(c2_items_with_omega(W, w, Om), T, "fp64")
+    got64 = b.get()
+    b.close()
+    for t in T:
+        t.close()
+    ref = oracle.w2(w["tables"][0], w["M"], w["nq"], w["nc"], w["qmax"], w["p"], w["T"], Omega=Om)
+    assert np.max(rel(got64, ref)) <= TOL64
+    assert np.max(rel(got, ref)) <= TOL32["C2"]
+
+
 # ------------------------------------------------------------------ batching semantics
 def test_alone_and_in_mix_are_bitwise_identical(ctx, W):
     """Each integral's result is independent of what else is in the launch (deterministic
