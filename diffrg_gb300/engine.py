@@ -77,6 +77,20 @@ class Table:
             self.h = None
 
 
+def integral_array(integrals) -> "C.Array":
+    """A ctypes array of gb_integral: `integrals` itself if it already is one (no copy)."""
+    if isinstance(integrals, C.Array):
+        return integrals
+    return (Integral * len(integrals))(*integrals)
+
+
+def integral_view(arr: "C.Array", lo: int, hi: int) -> "C.Array":
+    """Elements lo..hi-1 of a ctypes gb_integral array, sharing its memory."""
+    if not 0 <= lo <= hi <= len(arr):
+        raise IndexError("integral_view out of range")
+    return (Integral * (hi - lo)).from_address(C.addressof(arr) + lo * C.sizeof(Integral))
+
+
 def _table_array(tables: Sequence[Table]):
     arr = (C.c_void_p * max(1, len(tables)))()
     for i, t in enumerate(tables):
@@ -89,7 +103,7 @@ class Batch:
                  precision: str = "fp32c"):
         self.ctx = ctx
         self.n = len(integrals)
-        arr = (Integral * self.n)(*integrals)
+        arr = integral_array(integrals)
         h = C.c_void_p()
         ctx.check(capi.lib().gb_batch_create(ctx.h, arr, self.n, _table_array(tables), len(tables),
                                              PREC[precision], C.byref(h)))
@@ -234,7 +248,7 @@ class Context:
     def submit(self, integrals: Sequence[Integral], tables: Sequence[Table] = (), precision: str = "fp32c") -> "Ticket":
         """Queue one request (the integrals of one request() fan-out); returns its ticket."""
         n = len(integrals)
-        arr = (Integral * n)(*integrals)
+        arr = integral_array(integrals)
         t = C.c_uint64()
         self.check(capi.lib().gb_submit(self.h, arr, n, _table_array(tables), len(tables), PREC[precision],
                                         C.byref(t)))

@@ -22,7 +22,7 @@ import time
 
 import numpy as np
 
-from .engine import Context, Table, integral
+from .engine import Context, Table, integral, integral_array, integral_view
 from .workloads import SEEDS, seeded_table, spec_log
 
 N_FUNC = 32
@@ -60,6 +60,22 @@ def table_order():
     """Indices of the table list passed with every request: 0..31 then 0, 1, 2, so that the
     four tables of 3D function i are the contiguous list entries i..i+3."""
     return list(range(N_FUNC)) + [0, 1, 2]
+
+
+class RhsItems:
+    """The right-hand side's descriptors as one ctypes array, built once; at(k) rewrites the
+    RG scale of every descriptor in place (a numpy view of the array)."""
+
+    def __init__(self, w: dict):
+        self.arr = integral_array(rhs_items(w, 1.0))
+        self.view = np.ctypeslib.as_array(self.arr)
+
+    def at(self, k: float):
+        self.view["k"][:] = k
+        return self.arr
+
+    def slice(self, lo: int, hi: int):
+        return integral_view(self.arr, lo, hi)
 
 
 def rhs_items(w: dict, k: float):
@@ -107,6 +123,7 @@ class Flow:
         self.rng = np.random.default_rng(seed)
         self.tables = [Table(ctx, self.w["spec"], self.w["y0"][i]) for i in range(N_FUNC)]
         self.tlist = [self.tables[i] for i in table_order()]
+        self.items = RhsItems(self.w)
         self.rhs_evals = 0
         self.requests = 0
         self.integrals = 0
@@ -119,8 +136,9 @@ class Flow:
         """Publish y as the tables and serve all N_FUNC x N_P integrals at RG time t."""
         for i in range(N_FUNC):
             self.tables[i].update(y[i])
-        items = rhs_items(self.w, math.exp(-t))
-        sizes = request_sizes(self.rng, len(items), self.w["size_lo"], self.w["size_hi"])
+        n = self.w["integrals_per_rhs"]
+        self.items.at(math.exp(-t))
+        sizes = request_sizes(self.rng, n, self.w["size_lo"], self.w["size_hi"])
         tickets = []
         off = 0
         t_next = time.perf_counter()
@@ -131,14 +149,14 @@ class Flow:
                 dt = t_next - time.perf_counter()
                 if dt > 0:
                     time.sleep(dt)
-            tickets.append((off, self.ctx.submit(items[off:off + s], self.tlist, self.precision)))
+            tickets.append((off, self.ctx.submit(self.items.slice(off, off + s), self.tlist, self.precision)))
             off += s
-        out = np.empty(len(items))
+        out = np.empty(n)
         for o, tk in tickets:
             out[o:o + tk.n] = tk.wait()
         self.rhs_evals += 1
         self.requests += len(sizes)
-        self.integrals += len(items)
+        self.integrals += n
         return out.reshape(N_FUNC, N_P)
 
     def rhs(self, t: float, y: np.ndarray) -> np.ndarray:

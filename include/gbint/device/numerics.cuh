@@ -146,10 +146,11 @@ namespace gbint
       const df s = two_sum(a.hi, b);
       return fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
     }
-    // 1/a: one Newton step on the FP32 reciprocal, residual e = 1 - g a formed exactly by fma
+    // 1/a: one Newton step on an approximate FP32 reciprocal (the residual e = 1 - g a is
+    // formed by fma; the step restores ~44 bits whatever the last bits of g)
     __device__ __forceinline__ df df_rcp(df a)
     {
-      const float g = __frcp_rn(a.hi);
+      const float g = __fdividef(1.0f, a.hi);
       const float e = __fsub_rn(__fmaf_rn(-g, a.hi, 1.0f), __fmul_rn(g, a.lo));
       return fast_two_sum(g, __fmul_rn(g, e));
     }
@@ -224,10 +225,12 @@ namespace gbint
         const df s = two_sum(pn, __fmul_rn(pn, em.hi));
         D = fast_two_sum(s.hi, __fadd_rn(s.lo, __fmaf_rn(pn, em.lo, -1.0f)));
       }
-      // x / D
-      const float q0 = __fdiv_rn(xh, D.hi);
+      // x / D: quotient from an approximate reciprocal, corrected by the fma residual
+      // (D.hi > 2^126 only for x > 87, where R < 1e-35 and the reciprocal flushes to 0)
+      const float rD = __fdividef(1.0f, D.hi);
+      const float q0 = __fmul_rn(xh, rD);
       const float rem = __fadd_rn(__fsub_rn(__fmaf_rn(-q0, D.hi, xh), __fmul_rn(q0, D.lo)), xl);
-      return fast_two_sum(q0, __fdiv_rn(rem, D.hi));
+      return fast_two_sum(q0, __fmul_rn(rem, rD));
     }
     GBINT_HD double reg_Rdot(double x)
     {
@@ -274,9 +277,12 @@ namespace gbint
     {
       const float num = __fsub_rn(m, 1.0f);  // exact (Sterbenz)
       const df den = two_sum(m, 1.0f);
-      const float s0 = __fdiv_rn(num, den.hi);
+      // s = num / den as s0 + s1: s0 from an approximate reciprocal (a few ulp), the residual
+      // num - s0 den is exact with an FMA, and s1 = residual / den needs only ~20 bits
+      const float r = __fdividef(1.0f, den.hi);
+      const float s0 = __fmul_rn(num, r);
       const float rr = __fsub_rn(__fmaf_rn(-s0, den.hi, num), __fmul_rn(s0, den.lo));
-      const float s1 = __fdiv_rn(rr, den.hi);
+      const float s1 = __fmul_rn(rr, r);
       const float t = __fmul_rn(s0, s0);
       float P = __fmaf_rn(t, 7.69230769e-02f, 9.09090909e-02f);  // 1/13, 1/11
       P = __fmaf_rn(t, P, 1.11111111e-01f);                       // 1/9
@@ -318,7 +324,8 @@ namespace gbint
       const df lm = log2_mant_df(m);
       // g = ex + lm + vl / (vh ln 2)
       const df g0 = two_sum((float)ex, lm.hi);
-      const float gl = __fadd_rn(__fadd_rn(g0.lo, lm.lo), __fmul_rn(1.44269504f, __fmul_rn(vl, __frcp_rn(vh))));
+      // vl / vh <= 2^-24: an approximate quotient is ample for this first-order term
+      const float gl = __fadd_rn(__fadd_rn(g0.lo, lm.lo), __fmul_rn(1.44269504f, __fdividef(vl, vh)));
       const df g = fast_two_sum(g0.hi, gl);
       const df u = df_add(df_mul(a.scale, g), a.shift);
       return frac_from_u(a, u.hi, u.lo, i);
