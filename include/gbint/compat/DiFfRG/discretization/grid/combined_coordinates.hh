@@ -1,0 +1,4 @@
+// Forwarding header at the path of DiFfRG/include/DiFfRG/discretization/grid/combined_coordinates.hh:
+// the coordinate classes are provided by gbint/interpolators.hh.
+#pragma once
+#include "gbint/interpolators.hh"

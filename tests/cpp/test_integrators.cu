@@ -154,8 +154,110 @@ template <typename NT> double run(QuadratureProvider &qp, const Case &c)
   throw std::runtime_error("unsupported d");
 }
 
+// device evaluation of an interpolator at host-given points (checks the device branch)
+template <typename I> __global__ void eval_pts3(I f, const double *x, int n, double *out)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) out[t] = (double)f(x[3 * t], x[3 * t + 1], x[3 * t + 2]);
+}
+template <typename I> __global__ void eval_pts2(I f, const double *x, int n, double *out)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) out[t] = (double)f(x[2 * t], x[2 * t + 1]);
+}
+template <int D, typename I> std::vector<double> on_device(const I &f, const std::vector<double> &x)
+{
+  const int n = (int)x.size() / D;
+  double *dx = nullptr, *dout = nullptr;
+  if (cudaMalloc(&dx, x.size() * sizeof(double)) != cudaSuccess || cudaMalloc(&dout, n * sizeof(double)) != cudaSuccess)
+    throw std::runtime_error("cudaMalloc");
+  cudaMemcpy(dx, x.data(), x.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if constexpr (D == 3)
+    eval_pts3<<<(n + 127) / 128, 128>>>(f, dx, n, dout);
+  else
+    eval_pts2<<<(n + 127) / 128, 128>>>(f, dx, n, dout);
+  std::vector<double> out(n);
+  if (cudaMemcpy(out.data(), dout, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    throw std::runtime_error("device evaluation failed");
+  cudaFree(dx);
+  cudaFree(dout);
+  return out;
+}
+
+// 3D and stacked interpolators: device branch vs host branch vs the closed form they must
+// reproduce (multilinear data are interpolated exactly)
+int interp3_cases()
+{
+  using L = LinearCoordinates1D<double>;
+  using P3 = CoordinatePackND<L, L, L>;
+  const uint n0 = 9, n1 = 7, n2 = 5;
+  P3 pk(L(n0, -1.0, 3.0), L(n1, 0.0, 2.0), L(n2, -2.0, 2.0));
+  auto tri = [](double x, double y, double z) {
+    return 1 + 0.5 * x - 0.3 * y + 0.2 * z + 0.1 * x * y - 0.05 * y * z + 0.02 * x * z + 0.01 * x * y * z;
+  };
+  std::vector<double> data((size_t)n0 * n1 * n2);
+  for (uint i = 0; i < n0; ++i)
+    for (uint j = 0; j < n1; ++j)
+      for (uint l = 0; l < n2; ++l) {
+        const auto v = pk.forward(i, j, l);
+        data[((size_t)i * n1 + j) * n2 + l] = tri(v[0], v[1], v[2]);
+      }
+  LinearInterpolator3D<double, P3> lin(data, pk);
+  TexLinearInterpolator3D<double, P3> tex(data, pk);
+  std::vector<double> pts;
+  for (int t = 0; t < 40; ++t) {
+    const double u = std::sin(1.3 * t + 0.2), v = std::cos(0.7 * t), w = std::sin(2.1 * t + 1.0);
+    pts.push_back(1.0 + 1.9 * u);
+    pts.push_back(1.0 + 0.95 * v);
+    pts.push_back(1.9 * w);
+  }
+  const auto dl = on_device<3>(lin, pts), dt = on_device<3>(tex, pts);
+  for (size_t t = 0; t < dl.size(); ++t) {
+    const double x = pts[3 * t], y = pts[3 * t + 1], z = pts[3 * t + 2];
+    std::printf("LIN3 %.17g %.17g %.17g\n", dl[t], lin(x, y, z), tri(x, y, z));
+    std::printf("TEX3 %.17g %.17g %.17g\n", dt[t], tex(x, y, z), tri(x, y, z));
+  }
+  // clamping outside the box: the value at the nearest face
+  const std::vector<double> out_pts{-5.0, 1.0, 0.5, 10.0, -3.0, 0.0};
+  const auto dcl = on_device<3>(lin, out_pts);
+  std::printf("CLAMP3 %.17g %.17g\n", dcl[0], tri(-1.0, 1.0, 0.5));
+  std::printf("CLAMP3 %.17g %.17g\n", dcl[1], tri(3.0, 0.0, 0.0));
+  // finite-T stack: modes n = 0..7 at T, 40 log-spaced p in [1e-3, 10]; data linear in the p
+  // grid index per mode, so the lookup equals a_s + b_s * backward(p) exactly
+  const double T = 0.15;
+  using FT = BosonicCoordinates1DFiniteT<int, double>;
+  FT fc(0, 8, T, 40, 1e-3, 10.0, 4.0);
+  std::vector<double> sd(8 * 40);
+  for (int s2 = 0; s2 < 8; ++s2)
+    for (int i = 0; i < 40; ++i) sd[s2 * 40 + i] = 0.5 + 0.1 * s2 + 0.02 * (s2 + 1) * i;
+  TexLinearInterpolator1DStack<double, FT> st(sd, fc);
+  LogarithmicCoordinates1D<double> lc(40, 1e-3, 10.0, 4.0);
+  std::vector<double> mp;
+  for (int t = 0; t < 24; ++t) {
+    const int mode = t % 10;  // modes 8, 9 lie above the stack: folded onto mode 7
+    mp.push_back(2 * M_PI * T * mode);
+    mp.push_back(std::exp(-6.0 + 0.35 * t));
+  }
+  const auto ds = on_device<2>(st, mp);
+  for (size_t t = 0; t < ds.size(); ++t) {
+    const double m = mp[2 * t], p = mp[2 * t + 1];
+    int s2 = (int)std::lround(m / (2 * M_PI * T));
+    double pp = p;
+    if (s2 > 7) {
+      const double dm = m - 2 * M_PI * T * 7;
+      pp = std::sqrt(p * p + dm * dm);
+      s2 = 7;
+    }
+    double idx = lc.backward(pp);
+    idx = idx < 0 ? 0 : (idx > 39 ? 39 : idx);
+    std::printf("STACK %.17g %.17g %.17g\n", ds[t], st(m, p), 0.5 + 0.1 * s2 + 0.02 * (s2 + 1) * idx);
+  }
+  return 0;
+}
+
 int main(int argc, char **argv)
 {
+  if (argc > 1 && std::string(argv[1]) == "--interp3") return interp3_cases();
   QuadratureProvider qp;
   std::string line;
   std::vector<Case> cases;

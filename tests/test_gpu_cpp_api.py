@@ -93,3 +93,23 @@ def test_request_futures_match_get(binary):
     assert len(reqs) == 32
     for _, a, b in reqs:
         assert float(a) == float(b)
+
+
+def test_3d_and_stacked_interpolators(binary):
+    """TexLinearInterpolator3D / LinearInterpolator3D on a CoordinatePackND of three axes and
+    TexLinearInterpolator1DStack on BosonicCoordinates1DFiniteT: the device branch equals the
+    host branch, and both reproduce data that are multilinear in the grid index exactly
+    (FP32 storage of the Tex* data: 1e-6), including clamping and the folding of frequencies
+    above the stored modes."""
+    out = run(binary, [], extra=["--interp3"])
+    rows = {k: [list(map(float, l.split()[1:])) for l in out if l.startswith(k + " ")]
+            for k in ("LIN3", "TEX3", "CLAMP3", "STACK")}
+    assert len(rows["LIN3"]) == 40 and len(rows["TEX3"]) == 40 and len(rows["STACK"]) == 24
+    for dev, host, ana in rows["LIN3"]:
+        assert abs(dev - host) <= 1e-14 * max(1, abs(ana)) and abs(dev - ana) <= 1e-12 * max(1, abs(ana))
+    for dev, host, ana in rows["TEX3"]:
+        assert abs(dev - host) <= 1e-6 * max(1, abs(ana)) and abs(dev - ana) <= 2e-6 * max(1, abs(ana))
+    for dev, ana in rows["CLAMP3"]:
+        assert abs(dev - ana) <= 1e-12 * max(1, abs(ana))
+    for dev, host, ana in rows["STACK"]:
+        assert abs(dev - host) <= 1e-6 * abs(ana) and abs(dev - ana) <= 2e-6 * abs(ana)
