@@ -243,6 +243,8 @@ def main():
     ctx = Context(local)
     L = capi.lib()
     T = [ctx.table(s, d) for s, d in tabs]
+    # CTA widths of the FP32-compensated kernels for this GPU and workload (library autotuner)
+    tuned = ctx.autotune(items, T, "fp32c")
     b32 = ctx.batch(items, T, "fp32c")
     b64 = ctx.batch(items, T, "fp64")
     points = b32.points
@@ -253,12 +255,15 @@ def main():
     sh = stream.cuda_stream
     assert sh != 0
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
-    # kernels per step: the hoisted-factor kernel + one fused persistent kernel per item kind
-    launches_per_step = 2
+    # one step captured as a CUDA graph: its kernel nodes are the launches per step (the
+    # hoisted-factor kernel + one fused persistent kernel per item kind)
+    step_graph = ctx.capture(lambda: b32.run(stream=sh), stream=sh)
+    launches_per_step = step_graph.kernel_launches
 
-    def timed(batch, steps, warm):
+    def timed(batch, steps, warm, graph=None):
+        run = (lambda: graph.replay(stream=sh)) if graph else (lambda: batch.run(stream=sh))
         for _ in range(warm):
-            batch.run(stream=sh)
+            run()
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -267,7 +272,7 @@ def main():
         for i in range(steps):
             flush.zero_()
             ev[i][0].record(stream)
-            batch.run(stream=sh)
+            run()
             ev[i][1].record(stream)
         torch.cuda.synchronize()
         per = [a.elapsed_time(b) for a, b in ev]
@@ -312,6 +317,11 @@ def main():
         lat.append(time.perf_counter() - s0)
     e2e_total = sum(lat)
     e2e_value = n_int * args.steps * world / e2e_total
+
+    # ---------------------------------------------------------------- the same step replayed as a graph
+    per_graph = timed(b32, args.steps, args.warmup, graph=step_graph)
+    graph_value = n_int / (statistics.mean(per_graph) / 1e3)
+    step_graph.close()
 
     # ---------------------------------------------------------------- fused FP64 and plain FP64 paths
     per64 = timed(b64, max(3, args.steps // 4), 2)
@@ -397,9 +407,12 @@ def main():
             "plain_fp64_gpu": plain,
             "fp32c_over_plain_fp64": (value / world) / plain["value"] if plain else None,
             "fused_fp64_gpu": {"value": fused64, "unit": UNIT},
+            "graph_replay": {"value": graph_value * world, "unit": UNIT, "ms_per_step": statistics.mean(per_graph),
+                             "kernel_launches_per_step": launches_per_step},
             "latency_ms": {"batch_e2e_p50": pct(lat_ms, 0.5), "batch_e2e_p99": pct(lat_ms, 0.99),
                            "single_integral_get_p50": pct(sl_ms, 0.5), "single_integral_get_p99": pct(sl_ms, 0.99)},
             "accuracy": err,
+            "autotune": {"cta_threads_by_kind_slot": tuned},
             "serving": serve,
             "cpu_baseline": cpu}
     if serve:

@@ -36,6 +36,8 @@ EXPORTS = [
     "gb_get_stats", "gb_reset_stats", "gb_measure_peaks",
     "gb_buffer_create", "gb_buffer_upload", "gb_buffer_destroy",
     "gb_slot_acquire", "gb_slot_wait", "gb_slot_release", "gb_device_info",
+    "gb_graph_capture_begin", "gb_graph_capture_end", "gb_graph_launch", "gb_graph_info", "gb_graph_destroy",
+    "gb_autotune", "gb_tune_set",
 ]
 
 
@@ -119,6 +121,14 @@ def load(path: str = LIB_PATH):
     L.gb_get_stats.argtypes = [vp, C.POINTER(Stats)]
     L.gb_reset_stats.argtypes = [vp]
     L.gb_measure_peaks.argtypes = [vp, dp, dp, dp]
+    L.gb_graph_capture_begin.argtypes = [vp, vp]
+    L.gb_graph_capture_end.argtypes = [vp, vp, C.POINTER(vp)]
+    L.gb_graph_launch.argtypes = [vp, vp, vp]
+    L.gb_graph_info.argtypes = [vp, vp, C.POINTER(C.c_int)]
+    L.gb_graph_destroy.argtypes = [vp, vp]
+    L.gb_autotune.argtypes = [vp, C.POINTER(Integral), C.c_int, C.POINTER(vp), C.c_int, C.c_int, C.c_char_p, C.c_int,
+                              C.POINTER(C.c_int)]
+    L.gb_tune_set.argtypes = [vp, C.c_int, C.c_int]
     _lib = L
     return L
 

@@ -23,13 +23,15 @@ def compile_program(src: str, out: str, extra=()) -> str:
     os.makedirs(os.path.dirname(out), exist_ok=True)
     h = hashlib.sha256()
     for p in (src, os.path.join(B.INCLUDE, "gbint.h"), os.path.join(B.INCLUDE, "gbint", "integrators.hh"),
+              os.path.join(B.INCLUDE, "gbint", "interpolators.hh"),
               os.path.join(B.INCLUDE, "gbint", "device", "families.cuh")):
         h.update(open(p, "rb").read())
     h.update(open(lib, "rb").read()[:4096])
     stamp = out + ".stamp"
     if os.path.exists(out) and os.path.exists(stamp) and open(stamp).read() == h.hexdigest():
         return out
-    cmd = [B.nvcc(), "-std=c++17", "-O2", "-lineinfo", "-I", B.INCLUDE] + B.ARCH + list(extra) + \
+    cmd = [B.nvcc(), "-std=c++17", "-O2", "-lineinfo", "--expt-relaxed-constexpr", "-I", B.INCLUDE] + B.ARCH + \
+          list(extra) + \
           [src, "-o", out, "-L", libdir, "-lgbint", "-Xlinker", "-rpath," + libdir]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

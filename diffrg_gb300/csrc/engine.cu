@@ -1089,6 +1089,11 @@ static int table_update_impl(gb_ctx *ctx, gb_table *t, const float *src, cudaMem
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   GB_CUDA(cudaSetDevice(ctx->device));
+  {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone)
+      return set_error(ctx, GB_EINVAL, "table updates cannot be captured in a graph (update before gb_graph_launch)");
+  }
   const int back = t->front ^ 1;
   // serving batches still reading the back buffer (an older epoch) finish first
   if (ctx->serve) {
@@ -1176,10 +1181,81 @@ int gb_batch_run_graph(gb_ctx *ctx, gb_batch *b, void *stream)
   return GB_OK;
 }
 
+// ------------------------------------------------------------------ CUDA-graph sweeps
+struct gb_graph {
+  cudaGraphExec_t exec = nullptr;
+  int launches = 0;  // kernel launches per replay
+};
+
+static bool capturing(cudaStream_t s)
+{
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone;
+}
+
+int gb_graph_capture_begin(gb_ctx *ctx, void *stream)
+{
+  if (!ctx) return GB_EINVAL;
+  GB_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  if (capturing(s)) return set_error(ctx, GB_EINVAL, "stream is already capturing");
+  GB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  return GB_OK;
+}
+
+int gb_graph_capture_end(gb_ctx *ctx, void *stream, gb_graph **out)
+{
+  if (!ctx || !out) return set_error(ctx, GB_EINVAL, "bad gb_graph_capture_end arguments");
+  GB_CUDA(cudaSetDevice(ctx->device));
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(stream ? (cudaStream_t)stream : ctx->stream, &g);
+  if (e != cudaSuccess || !g) return cuda_fail(ctx, e != cudaSuccess ? e : cudaErrorStreamCaptureInvalidated,
+                                               "cudaStreamEndCapture (a captured call failed or was not capturable)");
+  auto G = std::make_unique<gb_graph>();
+  size_t nn = 0;
+  if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn) {
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+      for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) G->launches++;
+      }
+  }
+  e = cudaGraphInstantiate(&G->exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
+  *out = G.release();
+  return GB_OK;
+}
+
+int gb_graph_launch(gb_ctx *ctx, gb_graph *g, void *stream)
+{
+  if (!ctx || !g) return GB_EINVAL;
+  GB_CUDA(cudaSetDevice(ctx->device));
+  GB_CUDA(cudaGraphLaunch(g->exec, stream ? (cudaStream_t)stream : ctx->stream));
+  return GB_OK;
+}
+
+int gb_graph_info(gb_ctx *ctx, gb_graph *g, int *kernel_launches)
+{
+  if (!ctx || !g || !kernel_launches) return GB_EINVAL;
+  *kernel_launches = g->launches;
+  return GB_OK;
+}
+
+int gb_graph_destroy(gb_ctx *ctx, gb_graph *g)
+{
+  if (!ctx || !g) return GB_EINVAL;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  delete g;
+  return GB_OK;
+}
+
 int gb_batch_results(gb_ctx *ctx, gb_batch *b, double *host_out, void *stream)
 {
   if (!ctx || !b || !host_out) return GB_EINVAL;
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  if (capturing(s)) return set_error(ctx, GB_EINVAL, "gb_batch_results cannot be captured in a graph");
   GB_CUDA(cudaSetDevice(ctx->device));
   GB_CUDA(cudaMemcpyAsync(host_out, b->d_out, b->n * sizeof(double), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));

@@ -147,6 +147,25 @@ class Batch:
             self.h = None
 
 
+class Graph:
+    """A captured sweep (gb_graph): replay() launches every captured batch run at once."""
+
+    def __init__(self, ctx: "Context", h):
+        self.ctx = ctx
+        self.h = h
+        n = C.c_int()
+        ctx.check(capi.lib().gb_graph_info(ctx.h, h, C.byref(n)))
+        self.kernel_launches = n.value
+
+    def replay(self, stream=None):
+        self.ctx.check(capi.lib().gb_graph_launch(self.ctx.h, self.h, C.c_void_p(stream) if stream else None))
+
+    def close(self):
+        if self.h:
+            capi.lib().gb_graph_destroy(self.ctx.h, self.h)
+            self.h = None
+
+
 class Ticket:
     """A submitted request: poll() / wait() return its results (float64, one per integral)."""
 
@@ -235,6 +254,35 @@ class Context:
         self.check(capi.lib().gb_get(self.h, C.byref(g), _table_array(tables), len(tables), PREC[precision],
                                      C.byref(out)))
         return out.value
+
+    # autotuner
+    def autotune(self, integrals, tables=(), precision="fp32c", cache_path=None, refresh=False) -> dict:
+        """Time the CTA widths of the FP32-compensated kernels on these integrals and keep the
+        fastest per kernel kind (batches created afterwards use them).  Returns {slot: threads}
+        for the slots that are not at their default."""
+        arr = integral_array(integrals)
+        chosen = (C.c_int * 16)()
+        self.check(capi.lib().gb_autotune(self.h, arr, len(arr), _table_array(tables), len(tables), PREC[precision],
+                                          cache_path.encode() if cache_path else None, 1 if refresh else 0, chosen))
+        return {k: chosen[k] for k in range(16) if chosen[k]}
+
+    def tune_set(self, slot: int, threads: int):
+        self.check(capi.lib().gb_tune_set(self.h, slot, threads))
+
+    # CUDA-graph sweeps
+    def capture(self, body, stream=None) -> Graph:
+        """Capture body() -- gb_batch_run calls on `stream` (None: the context's stream) --
+        into a replayable graph."""
+        L = capi.lib()
+        sp = C.c_void_p(stream) if stream else None
+        self.check(L.gb_graph_capture_begin(self.h, sp))
+        g = C.c_void_p()
+        try:
+            body()
+        finally:
+            rc = L.gb_graph_capture_end(self.h, sp, C.byref(g))
+        self.check(rc)
+        return Graph(self, g)
 
     # serving (continuous batching)
     def serve_start(self, max_inflight: int = 8, max_items: int = 2048):

@@ -234,6 +234,36 @@ int gb_slot_wait(gb_ctx *ctx, const gb_slot *slot, double *out);
 int gb_slot_release(gb_ctx *ctx, const gb_slot *slot);
 int gb_device_info(gb_ctx *ctx, int *device, int *num_sms);
 
+/* ------------------------------------------------------------------ autotuner
+ * CTA width of the FP32-compensated kernels (no reference counterpart; the reference takes a
+ * max_block_size from its JSON settings).  For every kernel kind present in the integrals,
+ * gb_autotune times the widths the kernels are built for (128, 256, 512 threads = rows per
+ * work unit) on a batch of them and keeps the fastest in the context; batches created
+ * afterwards use it.  With cache_path (NULL: none) choices are read from / appended to a text
+ * file keyed by GPU model and SM count, and a cached kind is not timed again unless flags has
+ * GB_TUNE_REFRESH.  chosen (may be NULL) receives the 16 per-kind widths (0 = default), indexed
+ * by kind slot = GB_KIND_* (+ 8 for the double-float form used by GB_PREC_FP32C/FP32A).
+ * gb_tune_set pins one slot by hand (0 = default width). */
+enum { GB_KIND_S1 = 1, GB_KIND_S2 = 2, GB_KIND_S3 = 3, GB_KIND_S5 = 5, GB_KIND_ACC = 8 };
+#define GB_TUNE_REFRESH 1
+int gb_autotune(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
+                const char *cache_path, int flags, int *chosen);
+int gb_tune_set(gb_ctx *ctx, int kind_slot, int threads);
+
+/* ------------------------------------------------------------------ CUDA-graph sweeps
+ * A fixed sweep -- several gb_batch_run calls in order on one caller stream, e.g. every
+ * right-hand side of a timestep -- captured once and replayed with one graph launch
+ * (no reference counterpart: the reference launches every integral separately).  Between
+ * gb_graph_capture_begin and gb_graph_capture_end, gb_batch_run on that stream (NULL: the
+ * context's stream) is recorded, not executed.  Table updates and result reads are refused on a capturing stream: tables are
+ * updated before gb_graph_launch and read when the replay runs; results are read after it. */
+typedef struct gb_graph gb_graph;
+int gb_graph_capture_begin(gb_ctx *ctx, void *stream);
+int gb_graph_capture_end(gb_ctx *ctx, void *stream, gb_graph **out);
+int gb_graph_launch(gb_ctx *ctx, gb_graph *g, void *stream);
+int gb_graph_info(gb_ctx *ctx, gb_graph *g, int *kernel_launches);
+int gb_graph_destroy(gb_ctx *ctx, gb_graph *g);
+
 /* ------------------------------------------------------------------ serving (request loop)
  * Replaces the request()/get() fan-out of a flow's right-hand side (physics/utils.hh:31-147;
  * integrator request() launches, e.g. integration/integrator_angle_gpu.hh:166-219) with one

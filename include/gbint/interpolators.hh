@@ -34,6 +34,13 @@
 
 #include "gbint.h"
 
+// Coordinates return std::array / std::tuple from __host__ __device__ members, as the
+// reference's do; nvcc needs --expt-relaxed-constexpr for that (DiFfRG's own build passes it,
+// DiFfRG/cmake/setup_build_system.cmake:193).
+#if defined(__CUDACC__) && !defined(__CUDACC_RELAXED_CONSTEXPR__)
+#error "gbint/interpolators.hh: compile with nvcc --expt-relaxed-constexpr (as DiFfRG does)"
+#endif
+
 namespace DiFfRG
 {
   using uint = unsigned int;

@@ -249,6 +249,84 @@ def test_graph_replay_matches_direct_run(ctx, W):
         t.close()
 
 
+def test_captured_sweep_replays_every_batch(ctx, W):
+    """One graph holding the runs of three batches (C1, C3, C5 subsets) replays them all;
+    each replay gives the direct runs' bits; table updates are refused while capturing and
+    the replay reads tables as they are when it runs."""
+    from diffrg_gb300.capi import GbError
+
+    Ts, bs, direct = [], [], []
+    for name in ("C1", "C3", "C5"):
+        w = subset(W, name)
+        items, tabs = W.engine_items(w)
+        T = [ctx.table(s, d) for s, d in tabs]
+        b = ctx.batch(items, T, "fp32c")
+        direct.append(b.get())
+        Ts.append((T, tabs))
+        bs.append(b)
+    bad = []
+
+    def body():
+        for b in bs:
+            b.run()
+        try:
+            Ts[0][0][0].update(Ts[0][1][0][1])
+        except GbError as e:
+            bad.append(e.code)
+
+    g = ctx.capture(body)
+    assert bad == [1]
+    assert g.kernel_launches >= 6
+    for _ in range(3):
+        g.replay()
+        for b, d in zip(bs, direct):
+            assert np.array_equal(b.results(), d)
+    # the replay reads the current table contents
+    T1, tabs1 = Ts[0]
+    T1[0].update(tabs1[0][1] * np.float32(1.5))
+    g.replay()
+    changed = bs[0].results()
+    assert not np.array_equal(changed, direct[0])
+    bs[0].run()
+    assert np.array_equal(bs[0].results(), changed)
+    T1[0].update(tabs1[0][1])
+    g.close()
+    for b in bs:
+        b.close()
+    for T, _ in Ts:
+        for t in T:
+            t.close()
+
+
+def test_autotuner_choices_cache_and_accuracy(ctx, oracle, W, tmp_path):
+    """gb_autotune picks a built CTA width per kernel kind, writes the per-GPU cache, reuses it
+    on the next call, and the tuned batches keep the accuracy bar."""
+    cache = str(tmp_path / "tune.txt")
+    try:
+        for name, slot in (("C3", 3 + 8), ("C1", 1 + 8)):
+            w = subset(W, name)
+            items, tabs = W.engine_items(w)
+            T = [ctx.table(s, d) for s, d in tabs]
+            got = ctx.autotune(items, T, "fp32c", cache_path=cache)
+            assert got.get(slot) in (128, 256, 512)
+            lines = open(cache).read().splitlines()
+            assert any(l.split("|")[2] == str(slot) for l in lines)
+            again = ctx.autotune(items, T, "fp32c", cache_path=cache)
+            assert again[slot] == got[slot]
+            b = ctx.batch(items, T, "fp32c")
+            val = b.get()
+            b.close()
+            ref = W.oracle_values(w, oracle)
+            assert np.max(rel(val, ref)) <= TOL32[name]
+            for t in T:
+                t.close()
+        with pytest.raises(Exception):
+            ctx.tune_set(3, 96)
+    finally:
+        for k in range(16):
+            ctx.tune_set(k, 0)
+
+
 def test_table_update_is_seen_by_next_run(ctx, oracle, W):
     w = subset(W, "C1")
     items, tabs = W.engine_items(w)
