@@ -43,8 +43,9 @@ UNIT = "integrals/s"
 FLOPS_PER_POINT = 18
 SPECIALS_PER_POINT = 4
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant kernel, from the
-# ncu capture summarised in profiles/ (k_fp32c_S2acc_C2_finiteT.md)
-TRAFFIC_BYTES_PER_LAUNCH = {"C2": 388352}
+# ncu captures summarised in profiles/ (k_fp32c_S2acc_C2_finiteT.md, k_fp32c_S3acc_C3_uneven3D.md,
+# k_fp32c_S5acc_C5_vertex4D.md)
+TRAFFIC_BYTES_PER_LAUNCH = {"C2": 381952, "C3": 8823552, "C5": 323072}
 
 
 def parse():

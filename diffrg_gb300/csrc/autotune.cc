@@ -4,9 +4,9 @@
 // width fixes both the unit size (scheduling granularity of the persistent grid) and the
 // occupancy.  gb_autotune times every width the kernels are built for (128, 256, 512) on the
 // caller's integrals, kind by kind, and keeps the fastest in the context; batches created
-// afterwards use it.  Choices are cached per GPU model in a text file (one line per kind:
-// "<gpu name>|<SM count>|<kind>|<threads>|<ms>"), so that a later process on the same model skips
-// the timing.
+// afterwards use it.  Choices are cached per GPU model in a text file (one line per kind slot:
+// "<gpu name>|<SM count>|<slot>|<threads>|<ms>", slot = base kind + 8 for the double-float form),
+// so that a later process on the same model skips the timing.
 #include "engine.hh"
 #include "kernels.hh"
 
@@ -30,7 +30,7 @@ namespace gbint
       return name + "|" + std::to_string(ctx->num_sms);
     }
 
-    // cache lines "<gpu>|<sms>|<kind>|<threads>|<ms>" -> kind -> threads
+    // cache lines "<gpu>|<sms>|<slot>|<threads>|<ms>" -> slot -> threads
     std::map<int, int> read_cache(const char *path, const std::string &gpu)
     {
       std::map<int, int> m;
@@ -43,8 +43,9 @@ namespace gbint
         std::string t;
         while (std::getline(ss, t, '|')) tok.push_back(t);
         if (tok.size() < 4 || tok[0] + "|" + tok[1] != gpu) continue;
-        const int kind = std::atoi(tok[2].c_str()), th = std::atoi(tok[3].c_str());
-        if (std::find(std::begin(kCandidates), std::end(kCandidates), th) != std::end(kCandidates)) m[kind] = th;
+        const int slot = std::atoi(tok[2].c_str()), th = std::atoi(tok[3].c_str());
+        if (slot >= 0 && slot < 16 && std::find(std::begin(kCandidates), std::end(kCandidates), th) != std::end(kCandidates))
+          m[slot] = th;
       }
       return m;
     }
@@ -122,7 +123,7 @@ extern "C" int gb_autotune(gb_ctx *ctx, const gb_integral *items, int n, gb_tabl
   std::map<int, std::pair<int, double>> best;
   for (int kind : kinds) {
     const int slot = slot_of(kind);
-    auto c = cached.find(kind);
+    auto c = cached.find(slot);
     if (c != cached.end()) {
       ctx->threads_override[slot] = c->second;
       continue;
@@ -152,7 +153,7 @@ extern "C" int gb_autotune(gb_ctx *ctx, const gb_integral *items, int n, gb_tabl
       }
     }
     ctx->threads_override[slot] = best_t;
-    best[kind] = {best_t, best_ms};
+    best[slot] = {best_t, best_ms};
   }
   if (!best.empty()) write_cache(cache_path, gpu, best);
   if (chosen)
