@@ -38,10 +38,16 @@ sys.path.insert(0, ROOT)
 
 METRIC = "integrals/s and p99 request latency, batched FP32-comp vs plain FP64, 1 GPU"
 UNIT = "integrals/s"
-# algorithmic work per integrand point of the FTLOOP mixed factor (per sign of the Matsubara
-# frequency, as the reference counts points): F basic FP32 flops (FMA = 2), S special functions
-FLOPS_PER_POINT = 18
-SPECIALS_PER_POINT = 4
+# algorithmic work per integrand point after hoisting the per-row invariants: F basic FP32 flops
+# (FMA = 2, add/mul = 1), S special functions (log, exp/expm1, div, rcp, sqrt); C2 counts each
+# sign of the Matsubara frequency as a point, as the reference does.
+#   C1 PROP1: x2 (2), log index (2), fraction (1), lerp (3), Z x2 + R (2), weights (2); log, expm1, div, rcp
+#   C2 FTLOOP: C1's terms + bilinear (6 instead of 3) + w^2 + x2 (1) + mode fraction hoisted; 4 specials
+#   C3 PROP3: r2, t2, s (6), three log-axis lookups (3 x 6), Z r2 + R (2), products + sum (4);
+#             3 logs + expm1, div, rcp
+#   C5 VERT4: r2 (2), one log index shared by both tables (3), two bilinears (2 x 7), Z r2 + R (2),
+#             products + sum (4); log, expm1, div, rcp
+PER_POINT = {"C1": (12, 4), "C2": (18, 4), "C3": (30, 6), "C5": (25, 4)}
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant kernel, from the
 # ncu captures summarised in profiles/ (k_fp32c_S2acc_C2_finiteT.md, k_fp32c_S3acc_C3_uneven3D.md,
 # k_fp32c_S5acc_C5_vertex4D.md)
@@ -61,11 +67,7 @@ def parse():
     return ap.parse_args()
 
 
-def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+from diffrg_gb300.replicas import aggregate_rate, dist_env, max_over_ranks  # noqa: E402
 
 
 class ClockSampler:
@@ -284,12 +286,8 @@ def main():
     sampler.start()
     per32 = timed(b32, args.steps, args.warmup)
     clocks = sampler.stop()
-    tot = sum(per32) / 1e3
-    if world > 1:
-        t = torch.tensor([tot], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tot = float(t.item())
-    value = n_int * args.steps * world / tot
+    tot = max_over_ranks(sum(per32) / 1e3, device="cuda")
+    value = aggregate_rate(n_int, args.steps, world, tot)
     res32 = b32.results(stream=sh)
 
     # ---------------------------------------------------------------- e2e through the public API
@@ -317,7 +315,7 @@ def main():
         e2e_step()
         lat.append(time.perf_counter() - s0)
     e2e_total = sum(lat)
-    e2e_value = n_int * args.steps * world / e2e_total
+    e2e_value = aggregate_rate(n_int, args.steps, world, max_over_ranks(e2e_total, device="cuda"))
 
     # ---------------------------------------------------------------- the same step replayed as a graph
     per_graph = timed(b32, args.steps, args.warmup, graph=step_graph)
@@ -355,8 +353,9 @@ def main():
     # ---------------------------------------------------------------- roofline
     fp32_peak, mufu_peak, fp64_peak = ctx.measure_peaks()
     pts_per_s = points / (statistics.mean(per32) / 1e3)
-    fp32_achieved = FLOPS_PER_POINT * pts_per_s / 1e12
-    xu_achieved = SPECIALS_PER_POINT * pts_per_s / 1e9
+    flops_pp, specials_pp = PER_POINT[args.workload]
+    fp32_achieved = flops_pp * pts_per_s / 1e12
+    xu_achieved = specials_pp * pts_per_s / 1e9
     frac32 = fp32_achieved / fp32_peak
     fracxu = xu_achieved / mufu_peak
     traffic = TRAFFIC_BYTES_PER_LAUNCH.get(args.workload)
@@ -367,7 +366,7 @@ def main():
             "frac": max(frac32, fracxu), "traffic": traffic,
             "fp32": {"achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": frac32},
             "xu": {"achieved": xu_achieved, "peak": mufu_peak, "unit": "Gop/s", "frac": fracxu},
-            "per_point": {"F": FLOPS_PER_POINT, "S": SPECIALS_PER_POINT},
+            "per_point": {"F": flops_pp, "S": specials_pp},
             "points_per_launch": points,
             "peak_source": "measured in this run by the library's FFMA/MUFU probes (gb_measure_peaks); "
                            "MEASURED_PEAKS.json lists only HBM and BF16",

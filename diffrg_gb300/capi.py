@@ -37,7 +37,7 @@ EXPORTS = [
     "gb_buffer_create", "gb_buffer_upload", "gb_buffer_destroy",
     "gb_slot_acquire", "gb_slot_wait", "gb_slot_release", "gb_device_info",
     "gb_graph_capture_begin", "gb_graph_capture_end", "gb_graph_launch", "gb_graph_info", "gb_graph_destroy",
-    "gb_autotune", "gb_tune_set",
+    "gb_autotune", "gb_tune_set", "gb_selftest_wait",
 ]
 
 
@@ -129,6 +129,7 @@ def load(path: str = LIB_PATH):
     L.gb_autotune.argtypes = [vp, C.POINTER(Integral), C.c_int, C.POINTER(vp), C.c_int, C.c_int, C.c_char_p, C.c_int,
                               C.POINTER(C.c_int)]
     L.gb_tune_set.argtypes = [vp, C.c_int, C.c_int]
+    L.gb_selftest_wait.argtypes = [vp, C.c_longlong]
     _lib = L
     return L
 

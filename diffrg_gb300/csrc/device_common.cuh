@@ -11,7 +11,7 @@ namespace gbint
   namespace dev
   {
     // error bits written to RunParams::err
-    enum : int { ERR_MBAR_TIMEOUT = 1, ERR_BAD_INDEX = 2 };
+    enum : int { ERR_MBAR_TIMEOUT = kErrMbarTimeout, ERR_BAD_INDEX = kErrBadIndex };
 
     __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -49,11 +49,12 @@ namespace gbint
     }
     // Bounded wait: gives up after ~2^31 SM cycles (about a second), records ERR_MBAR_TIMEOUT
     // and returns false; callers then skip the unit so that the kernel always terminates.
-    __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *err)
+    __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *err,
+                                                      long long limit = (1ll << 31))
     {
       const long long t0 = clock64();
       while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > (1ll << 31)) {
+        if (clock64() - t0 > limit) {
           atomicOr(err, ERR_MBAR_TIMEOUT);
           return false;
         }

@@ -1405,6 +1405,25 @@ int gb_cancel(gb_ctx *ctx, gb_ticket t) { return serve_cancel(ctx, t); }
 int gb_get_stats(gb_ctx *ctx, gb_stats *out) { return serve_stats(ctx, out); }
 int gb_reset_stats(gb_ctx *ctx) { return serve_reset_stats(ctx); }
 
+int gb_selftest_wait(gb_ctx *ctx, long long max_cycles)
+{
+  if (!ctx) return GB_EINVAL;
+  if (max_cycles < 1 || max_cycles > (1ll << 31)) return set_error(ctx, GB_EINVAL, "max_cycles must be 1..2^31");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  GB_CUDA(cudaSetDevice(ctx->device));
+  GB_CUDA(cudaStreamSynchronize(ctx->stream));
+  int before = 0;
+  GB_CUDA(cudaMemcpy(&before, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  GB_CUDA(launch_wait_selftest(ctx->d_err, max_cycles, ctx->stream));
+  GB_CUDA(cudaStreamSynchronize(ctx->stream));
+  int err = 0;
+  GB_CUDA(cudaMemcpy(&err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  GB_CUDA(cudaMemcpy(ctx->d_err, &before, sizeof(int), cudaMemcpyHostToDevice));
+  if (err & ~before & kErrMbarTimeout)
+    return set_error(ctx, GB_ETIMEDOUT, "bounded mbarrier wait gave up after " + std::to_string(max_cycles) + " cycles");
+  return GB_OK;
+}
+
 int gb_measure_peaks(gb_ctx *ctx, double *fp32_tflops, double *mufu_gops, double *fp64_tflops)
 {
   if (!ctx) return GB_EINVAL;

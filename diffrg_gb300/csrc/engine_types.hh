@@ -79,6 +79,10 @@ namespace gbint
 
   constexpr int kMaxTables = 256;
 
+  // bits of the context's device error word (RunParams::err)
+  constexpr int kErrMbarTimeout = 1;  // a bounded mbarrier wait gave up
+  constexpr int kErrBadIndex = 2;     // a work unit or table index out of range was skipped
+
   struct RunParams {
     const ItemDev *items;
     const UnitDev *units;

@@ -40,4 +40,6 @@ namespace gbint
   cudaError_t launch_peak_ffma(float *out, int ctas, int threads, int iters, cudaStream_t s);
   cudaError_t launch_peak_mufu(float *out, int ctas, int threads, int iters, cudaStream_t s);
   cudaError_t launch_peak_dfma(double *out, int ctas, int threads, int iters, cudaStream_t s);
+  // one bounded mbarrier wait that nothing completes (records ERR_MBAR_TIMEOUT after `limit` cycles)
+  cudaError_t launch_wait_selftest(int *err, long long limit, cudaStream_t s);
 } // namespace gbint

@@ -248,6 +248,26 @@ namespace gbint
     k_peak_mufu<<<ctas, threads, 0, s>>>(out, iters);
     return cudaGetLastError();
   }
+  // Self-test of the bounded waits: an mbarrier that expects one arrival nobody makes.  The
+  // wait gives up after `limit` cycles and records ERR_MBAR_TIMEOUT, as a stalled TMA copy would.
+  __global__ void k_wait_selftest(int *err, long long limit)
+  {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+      dev::mbar_init(&bar, 1);
+      dev::mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) dev::mbar_wait_bounded(&bar, 0, err, limit);
+    __syncthreads();
+  }
+
+  cudaError_t launch_wait_selftest(int *err, long long limit, cudaStream_t s)
+  {
+    k_wait_selftest<<<1, 32, 0, s>>>(err, limit);
+    return cudaGetLastError();
+  }
+
   cudaError_t launch_peak_dfma(double *out, int ctas, int threads, int iters, cudaStream_t s)
   {
     k_peak_dfma<<<ctas, threads, 0, s>>>(out, iters);

@@ -310,6 +310,10 @@ class Context:
     def reset_stats(self):
         self.check(capi.lib().gb_reset_stats(self.h))
 
+    def selftest_wait(self, max_cycles: int = 1 << 20) -> int:
+        """Status of gb_selftest_wait: GB_ETIMEDOUT (4) when the bounded wait gave up as designed."""
+        return capi.lib().gb_selftest_wait(self.h, max_cycles)
+
     def measure_peaks(self):
         """(FP32 TFLOP/s, MUFU G op/s, FP64 TFLOP/s) of this GPU from the library's probes."""
         a, b, c = C.c_double(), C.c_double(), C.c_double()

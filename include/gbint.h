@@ -297,6 +297,11 @@ int gb_reset_stats(gb_ctx *ctx);
  * MUFU lg2 (G ops/s) and FP64 FMA (TFLOP/s), each timed with CUDA events over the whole
  * device.  They are the denominators of the engine's roofline. */
 int gb_measure_peaks(gb_ctx *ctx, double *fp32_tflops, double *mufu_gops, double *fp64_tflops);
+/* Failure-detection self-test: one kernel waits on an mbarrier that nothing completes, with the
+ * same bounded wait the TMA staging uses but a limit of max_cycles (1..2^31) SM cycles.  Returns
+ * GB_ETIMEDOUT when the wait gave up and recorded its error flag (the expected outcome); the
+ * context stays usable and its error word is left as it was. */
+int gb_selftest_wait(gb_ctx *ctx, long long max_cycles);
 
 #ifdef __cplusplus
 }

@@ -327,6 +327,21 @@ def test_autotuner_choices_cache_and_accuracy(ctx, oracle, W, tmp_path):
             ctx.tune_set(k, 0)
 
 
+def test_bounded_wait_times_out_and_context_survives(ctx, W):
+    """A device-side wait that nothing completes gives up after its cycle limit, reports
+    GB_ETIMEDOUT through the error word, and the context keeps computing correct results."""
+    from diffrg_gb300 import capi
+
+    w = subset(W, "C1")
+    before = run_engine(ctx, W, w, "fp32c")
+    for cycles in (1 << 10, 1 << 20):
+        assert ctx.selftest_wait(cycles) == capi.GB_ETIMEDOUT
+        assert "gave up" in ctx.last_error()
+    assert ctx.selftest_wait(0) == capi.GB_EINVAL
+    after = run_engine(ctx, W, w, "fp32c")
+    assert np.array_equal(before, after)
+
+
 def test_table_update_is_seen_by_next_run(ctx, oracle, W):
     w = subset(W, "C1")
     items, tabs = W.engine_items(w)
