@@ -37,7 +37,7 @@ EXPORTS = [
     "gb_buffer_create", "gb_buffer_upload", "gb_buffer_destroy",
     "gb_slot_acquire", "gb_slot_wait", "gb_slot_release", "gb_device_info",
     "gb_graph_capture_begin", "gb_graph_capture_end", "gb_graph_launch", "gb_graph_info", "gb_graph_destroy",
-    "gb_autotune", "gb_tune_set", "gb_selftest_wait",
+    "gb_autotune", "gb_tune_set", "gb_selftest_wait", "gb_table_group_begin", "gb_table_group_end",
 ]
 
 
@@ -130,6 +130,8 @@ def load(path: str = LIB_PATH):
                               C.POINTER(C.c_int)]
     L.gb_tune_set.argtypes = [vp, C.c_int, C.c_int]
     L.gb_selftest_wait.argtypes = [vp, C.c_longlong]
+    L.gb_table_group_begin.argtypes = [vp]
+    L.gb_table_group_end.argtypes = [vp]
     _lib = L
     return L
 

@@ -316,7 +316,7 @@ namespace
       AxisRef r{};
       rc = pool_append(ctx, h, r);
       if (rc) return rc;
-      it = ctx->axis_cache.emplace(key, AxisEntry{r, 0}).first;
+      it = ctx->axis_cache.emplace(key, AxisEntry{r, 0, std::move(h.v)}).first;
     }
     ref = it->second.ref;
     ref.role = role;
@@ -511,6 +511,7 @@ namespace gbint
       cudaFree(b->d_units);
       cudaFree(b->d_segs);
       cudaFree(b->d_seg);
+      cudaFree(b->d_aux);
       cudaFree(b->d_partials);
       cudaFree(b->d_item_count);
       cudaFree(b->d_counters);
@@ -525,8 +526,57 @@ namespace gbint
   {
     const size_t n = b->n, nu = b->units.size();
     return n * sizeof(ItemDev) + nu * sizeof(UnitDev) + b->segs.size() * sizeof(SegDev) +
-           b->seg_total * sizeof(double) + nu * sizeof(double) + n * sizeof(int) + b->runs.size() * sizeof(int) +
-           n * sizeof(double);
+           b->seg_total * sizeof(double) + b->aux.size() * sizeof(float4) + nu * sizeof(double) + n * sizeof(int) +
+           b->runs.size() * sizeof(int) + n * sizeof(double);
+  }
+
+  // Per-item double-float constants of the S kinds, formed on the host in FP64 by the same
+  // expressions the kernels would otherwise evaluate for every row on the (1/64-rate) FP64
+  // pipe; for S2 also one record per (mode, sign): {cell, fraction, (+-w_m + W)^2 hi, lo} on
+  // the table's mode axis.  `modes` are the host node values of the item's mode axis.
+  void item_aux(const gb_ctx *ctx, const gb_integral &g, ItemDev &it, const std::vector<double> *modes,
+                std::vector<float4> &aux)
+  {
+    auto df2 = [](double a, double b) {
+      const dev::df x = dev::df_from(a), y = dev::df_from(b);
+      return make_float4(x.hi, x.lo, y.hi, y.lo);
+    };
+    it.aux_off = (int)aux.size();
+    const double p = g.args[1];
+    switch (kind_base(it.kind)) {
+    case K_S1:
+      aux.push_back(df2(p * p, 2.0 * p));
+      break;
+    case K_S2: {
+      aux.push_back(df2(p * p, 2.0 * p));
+      const double T = g.args[2], Om = g.args[3];
+      const double inv2piT = 1.0 / (2.0 * 3.14159265358979323846 * T);
+      const dev::AxisDev &a0 = ctx->h_dir[it.tab[0]].a0;
+      for (int m = 0; m < it.ax[0].n; ++m)
+        for (int sg = 0; sg < 2; ++sg) {
+          const double w = (*modes)[m];
+          const double ws = (sg == 0 ? w : -w) + Om;
+          int jj = 0;
+          const float f = (float)dev::axis_frac64(a0, std::fabs(ws) * inv2piT, jj);
+          const dev::df w2 = dev::df_from(ws * ws);
+          float jf;
+          std::memcpy(&jf, &jj, sizeof(jf));
+          aux.push_back(make_float4(jf, f, w2.hi, w2.lo));
+        }
+      break;
+    }
+    case K_S3:
+      aux.push_back(df2(p, g.args[2]));                   // P, cos(theta)
+      aux.push_back(df2(p * p, 0.25 * p * p));           // P^2, P^2 / 4
+      aux.push_back(df2(g.args[3], 0.0));                 // sin(theta)
+      break;
+    case K_S5:
+      aux.push_back(df2(p, p * p));                       // P, P^2
+      aux.push_back(df2(g.args[2], g.args[3]));           // cos(alpha), sin(alpha)
+      break;
+    default:
+      break;
+    }
   }
 
   int plan_batch(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *const *item_tables,
@@ -551,6 +601,7 @@ namespace gbint
       if (g.integrand != GB_IG_POLY && g.integrand != GB_IG_PROP1 && g.integrand != GB_IG_PROP3 &&
           g.integrand != GB_IG_VERT4 && g.integrand != GB_IG_FTLOOP)
         return set_error(ctx, GB_EINVAL, "unknown integrand");
+      const size_t held0 = b->held.size();
       int rc = family_axes(ctx, g, it.ax, it.n_axes, &b->held);
       if (rc) return rc;
       // tables
@@ -655,6 +706,7 @@ namespace gbint
         } else
           it.seg_off = b->segs[f->second].off;
       }
+      if (kind != K_GENERIC) item_aux(ctx, g, it, &ctx->axis_cache.at(b->held[held0]).v, b->aux);
       // reference-pattern geometry
       int loop_axis = -1;
       if (g.family == GB_FAM_4D) loop_axis = 2;
@@ -747,6 +799,7 @@ namespace gbint
     alloc((void **)&b->d_units, nu * sizeof(UnitDev));
     alloc((void **)&b->d_segs, b->segs.size() * sizeof(SegDev));
     alloc((void **)&b->d_seg, b->seg_total * sizeof(double));
+    alloc((void **)&b->d_aux, b->aux.size() * sizeof(float4));
     alloc((void **)&b->d_partials, nu * sizeof(double));
     alloc((void **)&b->d_item_count, n * sizeof(int));
     alloc((void **)&b->d_counters, b->runs.size() * sizeof(int));
@@ -757,6 +810,8 @@ namespace gbint
     if (e == cudaSuccess) e = cudaMemcpy(b->d_units, b->units.data(), nu * sizeof(UnitDev), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !b->segs.empty())
       e = cudaMemcpy(b->d_segs, b->segs.data(), b->segs.size() * sizeof(SegDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !b->aux.empty())
+      e = cudaMemcpy(b->d_aux, b->aux.data(), b->aux.size() * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(b->d_item_count, 0, n * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(b->d_out, 0, n * sizeof(double));
     if (e != cudaSuccess) {
@@ -778,6 +833,7 @@ namespace gbint
     P.prec = ctx->pool.d_rec;
     P.tabs = ctx->d_dir;
     P.seg = b->d_seg;
+    P.aux = b->d_aux;
     P.item_count = b->d_item_count;
     P.out = d_out ? d_out : b->d_out;
     P.err = ctx->d_err;
@@ -1109,6 +1165,23 @@ static int table_update_impl(gb_ctx *ctx, gb_table *t, const float *src, cudaMem
   GB_CUDA(cudaEventRecord(ctx->tables_event, s));
   t->front = back;
   t->epoch++;
+  return GB_OK;
+}
+
+int gb_table_group_begin(gb_ctx *ctx)
+{
+  if (!ctx) return GB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  ctx->update_depth++;
+  return GB_OK;
+}
+
+int gb_table_group_end(gb_ctx *ctx)
+{
+  if (!ctx) return GB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  if (ctx->update_depth <= 0) return set_error(ctx, GB_EINVAL, "gb_table_group_end without gb_table_group_begin");
+  ctx->update_depth--;
   return GB_OK;
 }
 

@@ -63,7 +63,8 @@ namespace gbint
 
   struct AxisEntry {
     AxisRef ref;
-    int refs = 0;  // batches (and in-progress calls) holding the axis
+    int refs = 0;           // batches (and in-progress calls) holding the axis
+    std::vector<double> v;  // host copy of the node values
   };
 
   struct Ticket;
@@ -88,6 +89,7 @@ struct gb_batch {
   std::vector<gbint::ItemDev> items;
   std::vector<gbint::UnitDev> units;
   std::vector<gbint::SegDev> segs;
+  std::vector<float4> aux;  // per-item constants (S kinds)
   struct KindRun {
     int kind = 0;
     int unit_begin = 0, n_units = 0;
@@ -104,6 +106,7 @@ struct gb_batch {
   gbint::UnitDev *d_units = nullptr;
   gbint::SegDev *d_segs = nullptr;
   double *d_seg = nullptr;
+  float4 *d_aux = nullptr;
   double *d_partials = nullptr;
   int *d_item_count = nullptr;
   int *d_counters = nullptr;  // one per kind run
@@ -138,6 +141,7 @@ struct gb_ctx {
   std::vector<gbint::TableDev> h_dir;
   std::vector<gb_table *> slots;
   cudaEvent_t tables_event = nullptr;  // recorded after every table update (serving orders on it)
+  int update_depth = 0;                // open gb_table_group_begin blocks (guarded by mu)
   int *d_err = nullptr;
   // kind -> thread override (autotuner)
   int threads_override[16] = {};  // [base kind + 8 * accurate]

@@ -56,7 +56,7 @@ namespace gbint
     int seg_off;     // hoisted FP64 factors (S kinds)
     int seg_stride;  // row stride inside the segment
     int tab[4];      // table directory slots
-    int pad;
+    int aux_off;     // per-item constants of the S kinds in RunParams::aux (float4 records)
     double k;
     double args[GB_MAX_ARGS];
   };
@@ -94,6 +94,7 @@ namespace gbint
     const NodeRec *prec;   // FP32 records
     const TableDev *tabs;  // directory
     const double *seg;     // hoisted factors
+    const float4 *aux;     // per-item double-float constants and S2 mode records
     double *partials;      // per unit
     int *item_count;       // per item arrival counters (reset by the finisher)
     int *unit_counter;     // work-stealing counter (reset by the finisher of the run)

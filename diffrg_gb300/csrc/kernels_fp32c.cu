@@ -200,9 +200,9 @@ namespace gbint
                                              const float *tab, const TableDev *sT)
     {
       const NodeRec qr = P.prec[it.ax[0].off + row];
-      const double p = it.args[1];
-      const df A = df_add(rec_a(qr), dfc(p * p));
-      const df B = df_mul(dfc(2.0 * p), rec_v(qr));
+      const float4 c = P.aux[it.aux_off];  // p^2, 2p
+      const df A = df_add(rec_a(qr), df{c.x, c.y});
+      const df B = df_mul(df{c.z, c.w}, rec_v(qr));
       const AxisDev ax = sT[0].a0;
       const int nc = it.ax[1].n;
       if constexpr (!ACC) {
@@ -238,30 +238,28 @@ namespace gbint
       const int nq = it.ax[1].n;
       const int m = row / nq, i = row - m * nq;
       const NodeRec qr = P.prec[it.ax[1].off + i];
-      const double p = it.args[1], T = it.args[2], Om = it.args[3];
-      const double w = P.pv[it.ax[0].off + m];
       const bool pm = m >= it.ax[0].pm_from;
-      const df A = df_add(rec_a(qr), dfc(p * p));
-      const df B = df_mul(dfc(2.0 * p), rec_v(qr));
+      const float4 *aux = P.aux + it.aux_off;  // p^2, 2p | per (mode, sign): cell, fraction, w^2
+      const float4 c = aux[0];
+      const df A = df_add(rec_a(qr), df{c.x, c.y});
+      const df B = df_mul(df{c.z, c.w}, rec_v(qr));
       const TableDev &Z = sT[0];
       AxisDev axq = Z.a1;  // |q| axis, fed with x2 = |q+p|^2 -> half the log2 scale
       axq.scale.hi *= 0.5f;
       axq.scale.lo *= 0.5f;
       const int n1 = Z.n1;
-      const double inv2piT = 1.0 / (2.0 * 3.14159265358979323846 * T);
       int j0[2];
       float fy0[2];
       df w2[2];
       // With Om = 0 the +-w evaluations read |w| and w^2 only: they are bitwise equal, so one
       // evaluation is doubled (exact) instead of computing the second.
-      const bool twin = pm && Om == 0.0;
+      const bool twin = pm && it.args[3] == 0.0;
       const int ns = pm && !twin ? 2 : 1;
       for (int s = 0; s < 2; ++s) {
-        const double ws = (s == 0 ? w : -w) + Om;
-        int jj;
-        fy0[s] = (float)axis_frac64(Z.a0, fabs(ws) * inv2piT, jj);
-        j0[s] = jj;
-        w2[s] = dfc(ws * ws);
+        const float4 r = aux[1 + 2 * m + s];
+        j0[s] = __float_as_int(r.x);
+        fy0[s] = r.y;
+        w2[s] = df{r.z, r.w};
       }
       const int nc = it.ax[2].n;
       if constexpr (!ACC) {
@@ -314,14 +312,15 @@ namespace gbint
       const int i = row / nc, j = row - i * nc;
       const NodeRec qr = P.prec[it.ax[0].off + i];
       const NodeRec cr = P.prec[it.ax[1].off + j];
-      const double Pm = it.args[1], ct = it.args[2], st = it.args[3];
+      const float4 *aux = P.aux + it.aux_off;  // (P, cos th), (P^2, P^2/4), (sin th, -)
+      const float4 c0 = aux[0], c1 = aux[1], c2 = aux[2];
       const df q2 = rec_a(qr);
-      const df qP = df_mul(rec_v(qr), dfc(Pm));
-      const df X = df_mul(qP, df_mul(rec_v(cr), dfc(ct)));  // q P c cos(th)
-      const df q2pp = df_add(q2, dfc(Pm * Pm));
+      const df qP = df_mul(rec_v(qr), df{c0.x, c0.y});
+      const df X = df_mul(qP, df_mul(rec_v(cr), df{c0.z, c0.w}));  // q P c cos(th)
+      const df q2pp = df_add(q2, df{c1.x, c1.y});
       const df A = df_add(q2pp, df_scale2(df_neg(X), 2.f));  // |q-p|^2 at cos(phi) = 0
-      const df Ap = df_add(df_add(q2, dfc(0.25 * Pm * Pm)), df_neg(X));
-      const df B = df_scale2(df_neg(df_mul(qP, df_mul(rec_a(cr), dfc(st)))), 2.f);  // -2 q P s sin(th)
+      const df Ap = df_add(df_add(q2, df{c1.z, c1.w}), df_neg(X));
+      const df B = df_scale2(df_neg(df_mul(qP, df_mul(rec_a(cr), df{c2.x, c2.y}))), 2.f);  // -2 q P s sin(th)
       const df Bh = df_scale2(B, 0.5f);
       const df third = dfc(1.0 / 3.0);
       const df sbd = df_mul(q2pp, third);
@@ -369,14 +368,15 @@ namespace gbint
       const int i = row / n1, j = row - i * n1;
       const NodeRec qr = P.prec[it.ax[0].off + i];
       const NodeRec cr = P.prec[it.ax[1].off + j];
-      const double Pm = it.args[1], ca = it.args[2], sa = it.args[3];
-      const df qP = df_mul(rec_v(qr), dfc(Pm));
-      const df q2pp = df_add(rec_a(qr), dfc(Pm * Pm));
+      const float4 *aux = P.aux + it.aux_off;  // (P, P^2), (cos a, sin a)
+      const float4 k0 = aux[0], k1 = aux[1];
+      const df qP = df_mul(rec_v(qr), df{k0.x, k0.y});
+      const df q2pp = df_add(rec_a(qr), df{k0.z, k0.w});
       const df c1 = rec_v(cr);
       const df qPc1 = df_mul(qP, c1);
       const df r1d = df_max(df_add(q2pp, df_scale2(df_neg(qPc1), 2.f)), 1e-30f);  // |q-p1|^2
-      const df A2 = df_add(q2pp, df_scale2(df_mul(qPc1, dfc(ca)), 2.f));
-      const df B2 = df_scale2(df_mul(qP, df_mul(rec_a(cr), dfc(sa))), 2.f);
+      const df A2 = df_add(q2pp, df_scale2(df_mul(qPc1, df{k1.x, k1.y}), 2.f));
+      const df B2 = df_scale2(df_mul(qP, df_mul(rec_a(cr), df{k1.z, k1.w})), 2.f);
       const TableDev &TA = sT[0];
       const float *DA = tab + toff[0], *DB = tab + toff[1];
       const int tn1 = TA.n1;

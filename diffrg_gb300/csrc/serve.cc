@@ -54,16 +54,18 @@ namespace gbint
       cudaStream_t s_hi = nullptr, s_lo = nullptr;
       cudaEvent_t done = nullptr;
       // device arena (bytes counted in the context's in_use)
-      size_t cap_items = 0, cap_units = 0, cap_segs = 0, cap_seg = 0, bytes = 0;
+      size_t cap_items = 0, cap_units = 0, cap_segs = 0, cap_seg = 0, cap_aux = 0, bytes = 0;
       ItemDev *d_items = nullptr;
       UnitDev *d_units = nullptr;
       SegDev *d_segs = nullptr;
       double *d_seg = nullptr, *d_partials = nullptr, *d_out = nullptr;
+      float4 *d_aux = nullptr;
       int *d_item_count = nullptr, *d_counters = nullptr;
       // pinned staging of the same capacities
       ItemDev *h_items = nullptr;
       UnitDev *h_units = nullptr;
       SegDev *h_segs = nullptr;
+      float4 *h_aux = nullptr;
       double *h_out = nullptr;
       gb_batch *plan = nullptr;
       std::vector<Request *> reqs;
@@ -97,6 +99,7 @@ namespace gbint
       cudaFree(sl.d_units);
       cudaFree(sl.d_segs);
       cudaFree(sl.d_seg);
+      cudaFree(sl.d_aux);
       cudaFree(sl.d_partials);
       cudaFree(sl.d_out);
       cudaFree(sl.d_item_count);
@@ -104,6 +107,7 @@ namespace gbint
       cudaFreeHost(sl.h_items);
       cudaFreeHost(sl.h_units);
       cudaFreeHost(sl.h_segs);
+      cudaFreeHost(sl.h_aux);
       cudaFreeHost(sl.h_out);
       ctx->in_use -= sl.bytes;
       const cudaStream_t a = sl.s_hi, b = sl.s_lo;
@@ -114,21 +118,23 @@ namespace gbint
       sl.done = d;
     }
 
-    size_t arena_bytes(size_t items, size_t units, size_t segs, size_t seg)
+    size_t arena_bytes(size_t items, size_t units, size_t segs, size_t seg, size_t aux)
     {
       return items * (sizeof(ItemDev) + sizeof(double) + sizeof(int)) + units * (sizeof(UnitDev) + sizeof(double)) +
-             segs * sizeof(SegDev) + seg * sizeof(double) + kMaxRunsPerBatch * sizeof(int);
+             segs * sizeof(SegDev) + seg * sizeof(double) + aux * sizeof(float4) + kMaxRunsPerBatch * sizeof(int);
     }
 
     // make the slot's arena hold a batch of the given sizes; GB_EBUDGET if the budget is short.
     // Caller holds ctx->mu and the slot is idle.
-    int reserve(gb_ctx *ctx, Slot &sl, size_t items, size_t units, size_t segs, size_t seg)
+    int reserve(gb_ctx *ctx, Slot &sl, size_t items, size_t units, size_t segs, size_t seg, size_t aux)
     {
-      if (items <= sl.cap_items && units <= sl.cap_units && segs <= sl.cap_segs && seg <= sl.cap_seg) return GB_OK;
+      if (items <= sl.cap_items && units <= sl.cap_units && segs <= sl.cap_segs && seg <= sl.cap_seg &&
+          aux <= sl.cap_aux)
+        return GB_OK;
       auto grow = [](size_t need, size_t cap) { return need <= cap ? cap : std::max(need, cap + cap / 2); };
       const size_t ni = grow(items, sl.cap_items), nu = grow(units, sl.cap_units), ns = grow(segs, sl.cap_segs),
-                   nseg = grow(seg, sl.cap_seg);
-      const size_t nb = arena_bytes(ni, nu, ns, nseg);
+                   nseg = grow(seg, sl.cap_seg), na = grow(aux, sl.cap_aux);
+      const size_t nb = arena_bytes(ni, nu, ns, nseg, na);
       if (ctx->in_use - sl.bytes + nb > ctx->budget)
         return set_error(ctx, GB_EBUDGET, "serving batch does not fit the HBM budget now");
       free_arena(ctx, sl);
@@ -143,6 +149,7 @@ namespace gbint
       dev((void **)&sl.d_units, nu * sizeof(UnitDev));
       dev((void **)&sl.d_segs, ns * sizeof(SegDev));
       dev((void **)&sl.d_seg, nseg * sizeof(double));
+      dev((void **)&sl.d_aux, na * sizeof(float4));
       dev((void **)&sl.d_partials, nu * sizeof(double));
       dev((void **)&sl.d_out, ni * sizeof(double));
       dev((void **)&sl.d_item_count, ni * sizeof(int));
@@ -150,6 +157,7 @@ namespace gbint
       host((void **)&sl.h_items, ni * sizeof(ItemDev));
       host((void **)&sl.h_units, nu * sizeof(UnitDev));
       host((void **)&sl.h_segs, ns * sizeof(SegDev));
+      host((void **)&sl.h_aux, na * sizeof(float4));
       host((void **)&sl.h_out, ni * sizeof(double));
       sl.bytes = nb;
       ctx->in_use += nb;
@@ -161,6 +169,7 @@ namespace gbint
       sl.cap_units = nu;
       sl.cap_segs = ns;
       sl.cap_seg = nseg;
+      sl.cap_aux = na;
       return GB_OK;
     }
 
@@ -240,11 +249,14 @@ namespace gbint
         }
       const int n = (int)items.size();
       std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+      // a group of table updates is in progress: launch after it, so that the batch sees all
+      // of the group or none of it
+      if (ctx->update_depth > 0) return GB_EAGAIN;
       cudaSetDevice(ctx->device);
       gb_batch *b = new gb_batch();
       int rc = plan_batch(ctx, items.data(), n, tl.data(), tn.data(), g[0]->precision, b);
       if (rc == GB_OK && b->runs.size() > (size_t)kMaxRunsPerBatch) rc = set_error(ctx, GB_EINVAL, "too many kind runs");
-      if (rc == GB_OK) rc = reserve(ctx, sl, n, b->units.size(), b->segs.size(), b->seg_total);
+      if (rc == GB_OK) rc = reserve(ctx, sl, n, b->units.size(), b->segs.size(), b->seg_total, b->aux.size());
       if (rc) {
         free_batch(ctx, b);
         return rc;
@@ -255,6 +267,7 @@ namespace gbint
       b->d_units = sl.d_units;
       b->d_segs = sl.d_segs;
       b->d_seg = sl.d_seg;
+      b->d_aux = sl.d_aux;
       b->d_partials = sl.d_partials;
       b->d_item_count = sl.d_item_count;
       b->d_counters = sl.d_counters;
@@ -263,6 +276,7 @@ namespace gbint
       std::memcpy(sl.h_items, b->items.data(), n * sizeof(ItemDev));
       std::memcpy(sl.h_units, b->units.data(), b->units.size() * sizeof(UnitDev));
       if (!b->segs.empty()) std::memcpy(sl.h_segs, b->segs.data(), b->segs.size() * sizeof(SegDev));
+      if (!b->aux.empty()) std::memcpy(sl.h_aux, b->aux.data(), b->aux.size() * sizeof(float4));
       const cudaStream_t s = b->points < kSmallBatchPoints ? sl.s_hi : sl.s_lo;
       cudaError_t e = cudaStreamWaitEvent(s, ctx->tables_event, 0);
       if (e == cudaSuccess) e = cudaMemcpyAsync(sl.d_items, sl.h_items, n * sizeof(ItemDev), cudaMemcpyHostToDevice, s);
@@ -270,6 +284,8 @@ namespace gbint
         e = cudaMemcpyAsync(sl.d_units, sl.h_units, b->units.size() * sizeof(UnitDev), cudaMemcpyHostToDevice, s);
       if (e == cudaSuccess && !b->segs.empty())
         e = cudaMemcpyAsync(sl.d_segs, sl.h_segs, b->segs.size() * sizeof(SegDev), cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess && !b->aux.empty())
+        e = cudaMemcpyAsync(sl.d_aux, sl.h_aux, b->aux.size() * sizeof(float4), cudaMemcpyHostToDevice, s);
       if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_item_count, 0, n * sizeof(int), s);
       if (e != cudaSuccess) {
         cudaStreamSynchronize(s);
@@ -340,6 +356,16 @@ namespace gbint
           if (S->busy_since < 0) S->busy_since = now_s();
         }
         int rc = launch_group(ctx, S, *slot, g);
+        if (rc == GB_EAGAIN) {
+          // table-update group open: the requests go back to the head of the queue
+          std::unique_lock<std::mutex> lk(S->mu);
+          for (auto it = g.rbegin(); it != g.rend(); ++it) {
+            (*it)->state = RQ_QUEUED;
+            S->queue.push_front(*it);
+          }
+          S->cv.wait_for(lk, std::chrono::microseconds(50));
+          continue;
+        }
         if (rc == GB_EBUDGET) {
           if (any_busy) {
             // wait for memory: the group goes back to the head of the queue
@@ -458,7 +484,7 @@ namespace gbint
     ServeState *S = ctx->serve;
     if (!S) return set_error(ctx, GB_EINVAL, "serving not started (gb_serve_start)");
     // a request whose descriptors alone exceed the budget can never be admitted
-    if (arena_bytes(n, n, 0, 0) > ctx->budget) {
+    if (arena_bytes(n, n, 0, 0, 0) > ctx->budget) {
       std::lock_guard<std::mutex> lk(S->mu);
       S->rejected++;
       return set_error(ctx, GB_EBUDGET, "request can never fit the HBM budget");

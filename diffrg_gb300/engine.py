@@ -246,6 +246,16 @@ class Context:
     def table(self, spec: dict, data=None) -> Table:
         return Table(self, spec, data)
 
+    def update_tables(self, pairs, stream=None):
+        """Update several tables as one group: served requests see all of them or none."""
+        L = capi.lib()
+        self.check(L.gb_table_group_begin(self.h))
+        try:
+            for t, data in pairs:
+                t.update(data, stream)
+        finally:
+            self.check(L.gb_table_group_end(self.h))
+
     def batch(self, integrals, tables=(), precision="fp32c") -> Batch:
         return Batch(self, integrals, tables, precision)
 

@@ -134,8 +134,7 @@ class Flow:
 
     def integrals_at(self, t: float, y: np.ndarray) -> np.ndarray:
         """Publish y as the tables and serve all N_FUNC x N_P integrals at RG time t."""
-        for i in range(N_FUNC):
-            self.tables[i].update(y[i])
+        self.ctx.update_tables([(self.tables[i], y[i]) for i in range(N_FUNC)])
         n = self.w["integrals_per_rhs"]
         self.items.at(math.exp(-t))
         sizes = request_sizes(self.rng, n, self.w["size_lo"], self.w["size_hi"])

@@ -163,6 +163,11 @@ int gb_quad_config(gb_ctx *ctx, int min_matsubara_size, int vacuum_quad_size, in
 int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out);
 int gb_table_update(gb_ctx *ctx, gb_table *t, const float *host_data, void *stream);
 int gb_table_update_device(gb_ctx *ctx, gb_table *t, const float *device_data, void *stream);
+/* Several tables updated as one step (a right-hand side's dressing functions): between
+ * gb_table_group_begin and gb_table_group_end the serving loop launches no new batch, so every
+ * served request sees all updates of the group or none of them.  Blocks nest. */
+int gb_table_group_begin(gb_ctx *ctx);
+int gb_table_group_end(gb_ctx *ctx);
 int gb_table_epoch(gb_ctx *ctx, gb_table *t, uint64_t *epoch);
 int gb_table_destroy(gb_ctx *ctx, gb_table *t);
 

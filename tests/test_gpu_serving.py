@@ -120,11 +120,10 @@ def test_request_reads_one_table_epoch(sctx, tabs, w):
     bB = sctx.batch(items, tlist).get()
     assert not np.array_equal(bA, bB)
     for rep in range(3):
-        for i in range(serving.N_FUNC):
-            ts[i].update(yA[i])
+        sctx.update_tables([(ts[i], yA[i]) for i in range(serving.N_FUNC)])
         t1 = sctx.submit(items, tlist)
-        for i in range(serving.N_FUNC):  # issued while t1 is queued or running
-            ts[i].update(yB[i])
+        # one group of updates, issued while t1 is queued or running
+        sctx.update_tables([(ts[i], yB[i]) for i in range(serving.N_FUNC)])
         t2 = sctx.submit(items, tlist)
         r1 = t1.wait(timeout=300)
         r2 = t2.wait(timeout=300)
