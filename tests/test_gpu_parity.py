@@ -160,6 +160,29 @@ def test_workload_fp32_fast_matches_oracle(ctx, oracle, W, name):
     assert err.max() <= TOL32F
 
 
+@pytest.mark.parametrize("name", ["C1", "C2", "C3", "C5"])
+def test_workloads_match_golden_values(ctx, W, name):
+    """Engine (FP64 and FP32C) against the committed oracle values of fixed subsets."""
+    import json
+    import os
+
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "workloads_oracle.json")))
+    rec = gold["workloads"][name]
+    sub = np.array(rec["subset"])
+    want = np.array([float(v) for v in rec["values"]])
+    w = getattr(W, name.lower())()
+    if name == "C2":
+        w["p"], w["T"] = w["p"][sub], w["T"][sub]
+    elif name == "C3":
+        w["orders"], w["P"] = w["orders"][sub], w["P"][sub]
+    elif name == "C5":
+        w["P"], w["alpha"] = w["P"][sub], w["alpha"][sub]
+    else:
+        w["p"] = w["p"][sub]
+    assert np.max(rel(run_engine(ctx, W, w, "fp64"), want)) <= TOL64
+    assert np.max(rel(run_engine(ctx, W, w, "fp32c"), want)) <= TOL32[name]
+
+
 @pytest.mark.parametrize("name", ["C1", "C5"])
 def test_reference_pattern_matches_oracle(ctx, oracle, W, name):
     w = subset(W, name)

@@ -69,6 +69,21 @@ def test_served_equals_batch_and_oracle(sctx, tabs, w, oracle):
     assert np.max(err) <= 1e-9, err
 
 
+def test_served_values_match_golden(sctx, tabs, w):
+    import json
+    import os
+
+    _, tlist = tabs
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "workloads_oracle.json")))
+    rec = gold["workloads"]["C4"]
+    items = serving.rhs_items(w, rec["k"])
+    sub = [items[i * 128 + j] for i, j in rec["pairs"]]
+    want = np.array([float(v) for v in rec["values"]])
+    for prec, tol in (("fp64", 1e-12), ("fp32c", 1e-9)):
+        got = sctx.submit(sub, tlist, prec).wait(timeout=300)
+        assert np.max(np.abs(got - want) / np.abs(want)) <= tol, prec
+
+
 def test_fp64_requests_match_oracle(sctx, tabs, w, oracle):
     _, tlist = tabs
     k = 0.9
