@@ -58,6 +58,7 @@ namespace
     }
     a.scale = dev::df_from(a.scale64);
     a.shift = dev::df_from(a.shift64);
+    a.kln = dev::df_from(a.scale64 / std::log(2.0));
     return a;
   }
 
@@ -1118,19 +1119,41 @@ int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
   auto t = std::make_unique<gb_table>();
   t->spec = *spec;
   t->elems = (int)elems;
-  t->bytes = (int)((elems * 4 + 15) / 16 * 16);
+  const int data_bytes = (int)((elems * 4 + 15) / 16 * 16);
+  // 1D log tables with cells at most 25 % wide carry, after the data, 1/c_j for the cell
+  // centres c_j = sqrt(x_j x_{j+1}) as double-float pairs: the FP32 kernels take a point's
+  // fraction relative to its cell centre (ln(x / c_j), a short series) instead of forming a
+  // double-float log2 of x
+  const dev::AxisDev ax0 = make_axis(spec->n0, spec->log0, spec->lo0, spec->hi0);
+  std::vector<float> rc;
+  if (spec->n1 == 0 && spec->log0 && ax0.scale64 >= 1.0 / std::log2(1.25)) {  // cells at most 25 % wide
+    rc.resize(2 * (spec->n0 - 1));
+    for (int j = 0; j + 1 < spec->n0; ++j) {
+      // log2 c_j = (j + 1/2 - shift) / scale
+      const long double l2c = ((long double)j + 0.5L - (long double)ax0.shift64) / (long double)ax0.scale64;
+      const dev::df r = dev::df_from((double)exp2l(-l2c));
+      rc[2 * j] = r.hi;
+      rc[2 * j + 1] = r.lo;
+    }
+  }
+  t->bytes = data_bytes + (int)((rc.size() * 4 + 15) / 16 * 16);
   GB_CUDA(cudaSetDevice(ctx->device));
   GB_CUDA(cudaMalloc(&t->buf[0], t->bytes));
   GB_CUDA(cudaMalloc(&t->buf[1], t->bytes));
   GB_CUDA(cudaMemset(t->buf[0], 0, t->bytes));
   GB_CUDA(cudaMemset(t->buf[1], 0, t->bytes));
+  if (!rc.empty())
+    for (int b = 0; b < 2; ++b)
+      GB_CUDA(cudaMemcpy(reinterpret_cast<char *>(t->buf[b]) + data_bytes, rc.data(), rc.size() * 4,
+                         cudaMemcpyHostToDevice));
   TableDev &D = ctx->h_dir[slot];
   D = TableDev{};
   D.data = t->buf[0];
   D.n0 = spec->n0;
   D.n1 = spec->n1;
   D.bytes = t->bytes;
-  D.a0 = make_axis(spec->n0, spec->log0, spec->lo0, spec->hi0);
+  D.rc_off = rc.empty() ? 0 : data_bytes / 4;
+  D.a0 = ax0;
   D.a1 = spec->n1 ? make_axis(spec->n1, spec->log1, spec->lo1, spec->hi1) : dev::AxisDev{};
   GB_CUDA(cudaMemcpy(ctx->d_dir + slot, &D, sizeof(TableDev), cudaMemcpyHostToDevice));
   t->slot = slot;

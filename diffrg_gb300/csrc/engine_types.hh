@@ -72,8 +72,8 @@ namespace gbint
   struct TableDev {
     const float *data;
     int n0, n1;  // n1 == 0: 1D
-    int bytes;   // data bytes (multiple of 16)
-    int pad;
+    int bytes;   // bytes staged per table (data, then the cell-centre reciprocals), multiple of 16
+    int rc_off;  // 1D log tables: float offset of n0-1 (hi, lo) reciprocals of the cell centres; 0: none
     dev::AxisDev a0, a1;
   };
 

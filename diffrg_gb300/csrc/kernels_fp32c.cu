@@ -74,6 +74,69 @@ namespace gbint
     __device__ __forceinline__ float rcp32(float x) { return __frcp_rn(x); }
 
     // G = 1/(Z x + R(x)) for a 1D table, fast and accurate forms
+    // Fraction of a double-float coordinate x in cell j of a 1D log table, relative to the cell
+    // centre c_j (rc[j] = 1/c_j as hi, lo): f = 1/2 + kln ln(x / c_j) with
+    // ln(1+t) = t + t^2 Q(t), t = x/c_j - 1 formed in double-float (p.hi - 1 is exact) and
+    // |t| <= sqrt(1.25) - 1 + (one cell when j is off by one near a cell edge); Q is the series
+    // through t^9/9, truncation < 3e-10 of a cell.
+    __device__ __forceinline__ float cell_frac_at(const AxisDev &a, const float2 *rc, df x, int j)
+    {
+      const float2 r = rc[j];
+      const df p = df_mul(x, df{r.x, r.y});
+      const df t = two_sum(__fsub_rn(p.hi, 1.0f), p.lo);
+      const float th = t.hi;
+      float Q = __fmaf_rn(th, 1.11111111e-01f, -1.25e-01f);  // 1/9, -1/8
+      Q = __fmaf_rn(th, Q, 1.42857143e-01f);                  // 1/7
+      Q = __fmaf_rn(th, Q, -1.66666667e-01f);                 // -1/6
+      Q = __fmaf_rn(th, Q, 2.0e-01f);                         // 1/5
+      Q = __fmaf_rn(th, Q, -2.5e-01f);                        // -1/4
+      Q = __fmaf_rn(th, Q, 3.33333343e-01f);                  // 1/3
+      Q = __fmaf_rn(th, Q, -0.5f);
+      const float rest = __fmaf_rn(__fmul_rn(th, th), Q, t.lo);  // ln(1+t) = th + rest
+      const float a0 = __fmaf_rn(a.kln.hi, th, 0.5f);
+      return __fadd_rn(a0, __fmaf_rn(a.kln.hi, rest, __fmul_rn(a.kln.lo, th)));
+    }
+    // cell i and fraction of x on a 1D log table with cell-centre reciprocals (clamped like
+    // axis_frac_df): a fast log2 finds the cell to within one, the fraction decides the rest
+    __device__ __forceinline__ float log_cell_frac(const AxisDev &a, const float2 *rc, df x, int &i)
+    {
+      const int n = a.n;
+      if (!(x.hi >= 1e-30f)) x = df{1e-30f, 0.f};  // also maps NaN
+      if (!(x.hi <= 3e38f)) x = df{3e38f, 0.f};
+      const float ua = __fmaf_rn(a.scale.hi, __log2f(x.hi), a.shift.hi);
+      if (ua < -0.01f) {
+        i = 0;
+        return 0.f;
+      }
+      if (ua > (float)(n - 1) + 0.01f) {
+        i = n - 2;
+        return 1.f;
+      }
+      int j = min(max((int)floorf(ua), 0), n - 2);
+      float f = cell_frac_at(a, rc, x, j);
+      if (f < 0.f) {
+        if (j > 0) {
+          j -= 1;
+          f = __fadd_rn(f, 1.f);
+        } else
+          f = 0.f;
+      } else if (f > 1.f) {
+        if (j < n - 2) {
+          j += 1;
+          f = __fsub_rn(f, 1.f);
+        } else
+          f = 1.f;
+      }
+      i = j;
+      return fminf(fmaxf(f, 0.f), 1.f);
+    }
+    // fraction on a 1D table: cell-relative for log tables that carry reciprocals
+    __device__ __forceinline__ float frac1_df(const float *T, const TableDev &D, df x, int &i)
+    {
+      if (D.rc_off) return log_cell_frac(D.a0, reinterpret_cast<const float2 *>(T + D.rc_off), x, i);
+      return axis_frac_df(D.a0, x.hi, x.lo, i);
+    }
+
     __device__ __forceinline__ float G1_32(const float *T, const AxisDev &a, float x)
     {
       int i;
@@ -86,6 +149,19 @@ namespace gbint
       const float f = axis_frac_df(a, x.hi, x.lo, i);
       const df z = lerp_df(T[i], T[i + 1], f);
       return df_rcp(df_add(df_mul(z, x), reg_R_df(x)));
+    }
+    __device__ __forceinline__ df G1_df(const float *T, const TableDev &D, df x)
+    {
+      int i;
+      const float f = frac1_df(T, D, x, i);
+      const df z = lerp_df(T[i], T[i + 1], f);
+      return df_rcp(df_add(df_mul(z, x), reg_R_df(x)));
+    }
+    __device__ __forceinline__ df V1_df(const float *T, const TableDev &D, df x)
+    {
+      int i;
+      const float f = frac1_df(T, D, x, i);
+      return lerp_df(T[i], T[i + 1], f);
     }
     __device__ __forceinline__ float V1_32(const float *T, const AxisDev &a, float x)
     {
@@ -349,7 +425,7 @@ namespace gbint
           const df r2 = df_max(lin_dd(A, B, r.a_hi, r.a_lo), 1e-30f);
           const df t2 = df_max(lin_dd(Ap, Bh, r.a_hi, r.a_lo), 1e-30f);
           const df sv = df_add(sbd, df_mul(r2, third));
-          const df g = df_mul(df_mul(G1_df(TB, aB, r2), V1_df(TC, aC, sv)), V1_df(TD, aD, t2));
+          const df g = df_mul(df_mul(G1_df(TB, sT[1], r2), V1_df(TC, sT[2], sv)), V1_df(TD, sT[3], t2));
           k.add(df_mul(rec_w(r), g));
         }
         inner = k.value();

@@ -245,6 +245,7 @@ namespace gbint
     // scale/shift are double-float so that the index carries no systematic rounding.
     struct AxisDev {
       df scale, shift;
+      df kln;   // scale / ln 2 (log axes): grid cells per unit of ln x
       int n;    // number of grid points
       int log;  // 1: log-spaced
       double scale64, shift64;
