@@ -1120,17 +1120,25 @@ int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
   t->spec = *spec;
   t->elems = (int)elems;
   const int data_bytes = (int)((elems * 4 + 15) / 16 * 16);
-  // 1D log tables with cells at most 25 % wide carry, after the data, 1/c_j for the cell
-  // centres c_j = sqrt(x_j x_{j+1}) as double-float pairs: the FP32 kernels take a point's
-  // fraction relative to its cell centre (ln(x / c_j), a short series) instead of forming a
-  // double-float log2 of x
+  // Tables with a log axis whose cells are at most 25 % wide carry, after the data, 1/c_j for
+  // that axis's cell centres c_j = sqrt(x_j x_{j+1}) as double-float pairs: the FP32 kernels
+  // take a point's fraction relative to its cell centre (ln(x / c_j), a short series) instead
+  // of forming a double-float log2 of x.
   const dev::AxisDev ax0 = make_axis(spec->n0, spec->log0, spec->lo0, spec->hi0);
+  const dev::AxisDev ax1 = spec->n1 ? make_axis(spec->n1, spec->log1, spec->lo1, spec->hi1) : dev::AxisDev{};
+  const double kMinScale = 1.0 / std::log2(1.25), kMinScaleSq = 1.0 / std::log2(1.12);
+  int rc_axis = -1;
+  if (spec->log0 && ax0.scale64 >= kMinScale)
+    rc_axis = 0;
+  else if (spec->n1 && spec->log1 && ax1.scale64 >= kMinScale)
+    rc_axis = 1;
   std::vector<float> rc;
-  if (spec->n1 == 0 && spec->log0 && ax0.scale64 >= 1.0 / std::log2(1.25)) {  // cells at most 25 % wide
-    rc.resize(2 * (spec->n0 - 1));
-    for (int j = 0; j + 1 < spec->n0; ++j) {
+  if (rc_axis >= 0) {
+    const dev::AxisDev &ax = rc_axis == 0 ? ax0 : ax1;
+    rc.resize(2 * (ax.n - 1));
+    for (int j = 0; j + 1 < ax.n; ++j) {
       // log2 c_j = (j + 1/2 - shift) / scale
-      const long double l2c = ((long double)j + 0.5L - (long double)ax0.shift64) / (long double)ax0.scale64;
+      const long double l2c = ((long double)j + 0.5L - (long double)ax.shift64) / (long double)ax.scale64;
       const dev::df r = dev::df_from((double)exp2l(-l2c));
       rc[2 * j] = r.hi;
       rc[2 * j + 1] = r.lo;
@@ -1153,8 +1161,10 @@ int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
   D.n1 = spec->n1;
   D.bytes = t->bytes;
   D.rc_off = rc.empty() ? 0 : data_bytes / 4;
+  D.rc_axis = std::max(rc_axis, 0);
+  D.rc_sq = rc_axis >= 0 && (rc_axis == 0 ? ax0 : ax1).scale64 >= kMinScaleSq;
   D.a0 = ax0;
-  D.a1 = spec->n1 ? make_axis(spec->n1, spec->log1, spec->lo1, spec->hi1) : dev::AxisDev{};
+  D.a1 = ax1;
   GB_CUDA(cudaMemcpy(ctx->d_dir + slot, &D, sizeof(TableDev), cudaMemcpyHostToDevice));
   t->slot = slot;
   ctx->slots[slot] = t.get();

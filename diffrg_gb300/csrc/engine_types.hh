@@ -73,7 +73,10 @@ namespace gbint
     const float *data;
     int n0, n1;  // n1 == 0: 1D
     int bytes;   // bytes staged per table (data, then the cell-centre reciprocals), multiple of 16
-    int rc_off;  // 1D log tables: float offset of n0-1 (hi, lo) reciprocals of the cell centres; 0: none
+    int rc_off;   // float offset of the (hi, lo) reciprocals of the cell centres of axis rc_axis; 0: none
+    int rc_axis;  // the log axis they belong to (cells at most 25 % wide)
+    int rc_sq;    // 1: cells at most 12 % wide, so the reciprocals also serve a squared coordinate
+    int pad;
     dev::AxisDev a0, a1;
   };
 

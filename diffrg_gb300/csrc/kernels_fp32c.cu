@@ -79,10 +79,14 @@ namespace gbint
     // ln(1+t) = t + t^2 Q(t), t = x/c_j - 1 formed in double-float (p.hi - 1 is exact) and
     // |t| <= sqrt(1.25) - 1 + (one cell when j is off by one near a cell edge); Q is the series
     // through t^9/9, truncation < 3e-10 of a cell.
+    // SQ: x is the square of the axis coordinate (1/c_j^2 formed from 1/c_j, half the scale)
+    template <bool SQ = false>
     __device__ __forceinline__ float cell_frac_at(const AxisDev &a, const float2 *rc, df x, int j)
     {
       const float2 r = rc[j];
-      const df p = df_mul(x, df{r.x, r.y});
+      df rr{r.x, r.y};
+      if constexpr (SQ) rr = df_mul(rr, rr);
+      const df p = df_mul(x, rr);
       const df t = two_sum(__fsub_rn(p.hi, 1.0f), p.lo);
       const float th = t.hi;
       float Q = __fmaf_rn(th, 1.11111111e-01f, -1.25e-01f);  // 1/9, -1/8
@@ -93,17 +97,39 @@ namespace gbint
       Q = __fmaf_rn(th, Q, 3.33333343e-01f);                  // 1/3
       Q = __fmaf_rn(th, Q, -0.5f);
       const float rest = __fmaf_rn(__fmul_rn(th, th), Q, t.lo);  // ln(1+t) = th + rest
-      const float a0 = __fmaf_rn(a.kln.hi, th, 0.5f);
-      return __fadd_rn(a0, __fmaf_rn(a.kln.hi, rest, __fmul_rn(a.kln.lo, th)));
+      const float kh = SQ ? 0.5f * a.kln.hi : a.kln.hi, kl = SQ ? 0.5f * a.kln.lo : a.kln.lo;
+      const float a0 = __fmaf_rn(kh, th, 0.5f);
+      return __fadd_rn(a0, __fmaf_rn(kh, rest, __fmul_rn(kl, th)));
+    }
+    // the same fraction as a double-float (its FP32 rounding, ~3e-8 of a cell, is otherwise the
+    // largest per-point error of a lookup; used where few points carry an integral)
+    __device__ __forceinline__ df cell_frac_at_df(const AxisDev &a, const float2 *rc, df x, int j)
+    {
+      const float2 r = rc[j];
+      const df p = df_mul(x, df{r.x, r.y});
+      const df t = two_sum(__fsub_rn(p.hi, 1.0f), p.lo);
+      const float th = t.hi;
+      float Q = __fmaf_rn(th, 1.11111111e-01f, -1.25e-01f);
+      Q = __fmaf_rn(th, Q, 1.42857143e-01f);
+      Q = __fmaf_rn(th, Q, -1.66666667e-01f);
+      Q = __fmaf_rn(th, Q, 2.0e-01f);
+      Q = __fmaf_rn(th, Q, -2.5e-01f);
+      Q = __fmaf_rn(th, Q, 3.33333343e-01f);
+      Q = __fmaf_rn(th, Q, -0.5f);
+      const float rest = __fmaf_rn(__fmul_rn(th, th), Q, t.lo);
+      const df m = two_prod(a.kln.hi, th);  // kln (th + rest) = m + kln.hi rest + kln.lo th
+      const df s0 = two_sum(0.5f, m.hi);
+      return fast_two_sum(s0.hi, __fadd_rn(s0.lo, __fadd_rn(m.lo, __fmaf_rn(a.kln.hi, rest, __fmul_rn(a.kln.lo, th)))));
     }
     // cell i and fraction of x on a 1D log table with cell-centre reciprocals (clamped like
     // axis_frac_df): a fast log2 finds the cell to within one, the fraction decides the rest
+    template <bool SQ = false>
     __device__ __forceinline__ float log_cell_frac(const AxisDev &a, const float2 *rc, df x, int &i)
     {
       const int n = a.n;
       if (!(x.hi >= 1e-30f)) x = df{1e-30f, 0.f};  // also maps NaN
       if (!(x.hi <= 3e38f)) x = df{3e38f, 0.f};
-      const float ua = __fmaf_rn(a.scale.hi, __log2f(x.hi), a.shift.hi);
+      const float ua = __fmaf_rn(SQ ? 0.5f * a.scale.hi : a.scale.hi, __log2f(x.hi), a.shift.hi);
       if (ua < -0.01f) {
         i = 0;
         return 0.f;
@@ -113,7 +139,7 @@ namespace gbint
         return 1.f;
       }
       int j = min(max((int)floorf(ua), 0), n - 2);
-      float f = cell_frac_at(a, rc, x, j);
+      float f = cell_frac_at<SQ>(a, rc, x, j);
       if (f < 0.f) {
         if (j > 0) {
           j -= 1;
@@ -130,10 +156,45 @@ namespace gbint
       i = j;
       return fminf(fmaxf(f, 0.f), 1.f);
     }
-    // fraction on a 1D table: cell-relative for log tables that carry reciprocals
+    // cell and double-float fraction on a 1D log table with reciprocals (clamped)
+    __device__ __forceinline__ df log_cell_frac_df(const AxisDev &a, const float2 *rc, df x, int &i)
+    {
+      const int n = a.n;
+      if (!(x.hi >= 1e-30f)) x = df{1e-30f, 0.f};
+      if (!(x.hi <= 3e38f)) x = df{3e38f, 0.f};
+      const float ua = __fmaf_rn(a.scale.hi, __log2f(x.hi), a.shift.hi);
+      if (ua < -0.01f) {
+        i = 0;
+        return df{0.f, 0.f};
+      }
+      if (ua > (float)(n - 1) + 0.01f) {
+        i = n - 2;
+        return df{1.f, 0.f};
+      }
+      int j = min(max((int)floorf(ua), 0), n - 2);
+      df f = cell_frac_at_df(a, rc, x, j);
+      if (f.hi < 0.f) {
+        if (j > 0) {
+          j -= 1;
+          f = df_add_f(f, 1.f);
+        } else
+          f = df{0.f, 0.f};
+      } else if (f.hi > 1.f) {
+        if (j < n - 2) {
+          j += 1;
+          f = df_add_f(f, -1.f);
+        } else
+          f = df{1.f, 0.f};
+      }
+      i = j;
+      if (f.hi < 0.f) f = df{0.f, 0.f};
+      if (f.hi > 1.f) f = df{1.f, 0.f};
+      return f;
+    }
+    // fraction on axis 0 of a table: cell-relative for log axes that carry reciprocals
     __device__ __forceinline__ float frac1_df(const float *T, const TableDev &D, df x, int &i)
     {
-      if (D.rc_off) return log_cell_frac(D.a0, reinterpret_cast<const float2 *>(T + D.rc_off), x, i);
+      if (D.rc_off && D.rc_axis == 0) return log_cell_frac(D.a0, reinterpret_cast<const float2 *>(T + D.rc_off), x, i);
       return axis_frac_df(D.a0, x.hi, x.lo, i);
     }
 
@@ -155,6 +216,20 @@ namespace gbint
       int i;
       const float f = frac1_df(T, D, x, i);
       const df z = lerp_df(T[i], T[i + 1], f);
+      return df_rcp(df_add(df_mul(z, x), reg_R_df(x)));
+    }
+    // G(x) with a double-float table fraction (S1: integrals of a few thousand points)
+    __device__ __forceinline__ df G1_dff(const float *T, const TableDev &D, df x)
+    {
+      int i;
+      df z;
+      if (D.rc_off && D.rc_axis == 0) {
+        const df f = log_cell_frac_df(D.a0, reinterpret_cast<const float2 *>(T + D.rc_off), x, i);
+        z = lerp_dff(T[i], T[i + 1], f);
+      } else {
+        const float f = axis_frac_df(D.a0, x.hi, x.lo, i);
+        z = lerp_df(T[i], T[i + 1], f);
+      }
       return df_rcp(df_add(df_mul(z, x), reg_R_df(x)));
     }
     __device__ __forceinline__ df V1_df(const float *T, const TableDev &D, df x)
@@ -297,7 +372,7 @@ namespace gbint
         for (int l = 0; l < nc; ++l) {
           const NodeRec r = rc[l];
           const df x2 = df_max(lin_dd(A, B, r.v_hi, r.v_lo), 1e-30f);
-          k.add(df_mul(rec_aw(r), G1_df(tab, ax, x2)));
+          k.add(df_mul(rec_aw(r), G1_dff(tab, sT[0], x2)));
         }
         return P.seg[it.seg_off + row] * k.value();
       }
@@ -324,6 +399,9 @@ namespace gbint
       axq.scale.hi *= 0.5f;
       axq.scale.lo *= 0.5f;
       const int n1 = Z.n1;
+      // cell-centre reciprocals of the |q| axis (fed with |q+p|^2), when the table has them
+      const float2 *rcq =
+          (Z.rc_off && Z.rc_axis == 1 && Z.rc_sq) ? reinterpret_cast<const float2 *>(tab + Z.rc_off) : nullptr;
       int j0[2];
       float fy0[2];
       df w2[2];
@@ -364,7 +442,7 @@ namespace gbint
           const NodeRec r = rc[l];
           const df x2 = df_max(lin_dd(A, B, r.v_hi, r.v_lo), 1e-30f);
           int jq;
-          const float fq = axis_frac_df(axq, x2.hi, x2.lo, jq);
+          const float fq = rcq ? log_cell_frac<true>(Z.a1, rcq, x2, jq) : axis_frac_df(axq, x2.hi, x2.lo, jq);
           const df R = reg_R_df(x2);
           df gsum{0.f, 0.f};
           for (int s = 0; s < ns; ++s) {
@@ -490,7 +568,7 @@ namespace gbint
         return P.seg[it.seg_off + row] * kmid.value();
       } else {
         int ir1;
-        const float fr1 = axis_frac_df(TA.a0, r1d.hi, r1d.lo, ir1);
+        const float fr1 = frac1_df(DA, TA, r1d, ir1);
         const df Rr1 = reg_R_df(r1d);
         AccDF kmid;
 #pragma unroll 1
@@ -506,7 +584,7 @@ namespace gbint
             const NodeRec rp = rphi[m];
             const df x = df_max(lin_dd(A2, Bs, rp.a_hi, rp.a_lo), 1e-30f);
             int ix;
-            const float fx = axis_frac_df(TA.a0, x.hi, x.lo, ix);
+            const float fx = frac1_df(DA, TA, x, ix);
             const df gv = df_rcp(df_add(df_mul(bil_df_v0(DA, tn1, ix, fx, jc1, fc1), x), reg_R_df(x)));
             const df g = df_mul(gv, bil_df_v0(DB, tn1, ix, fx, jc2, fc2));
             kin.add(df_mul(rec_w(rp), g));

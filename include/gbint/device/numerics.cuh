@@ -162,6 +162,14 @@ namespace gbint
       const df s = two_sum(y0, p.hi);
       return fast_two_sum(s.hi, __fadd_rn(s.lo, __fmaf_rn(f, d.lo, p.lo)));
     }
+    // the same with a double-float fraction f = fh + fl
+    __device__ __forceinline__ df lerp_dff(float y0, float y1, df f)
+    {
+      const df d = two_sum(y1, -y0);
+      const df p = two_prod(f.hi, d.hi);
+      const df s = two_sum(y0, p.hi);
+      return fast_two_sum(s.hi, __fadd_rn(s.lo, __fmaf_rn(f.hi, d.lo, __fmaf_rn(f.lo, d.hi, p.lo))));
+    }
     // a + f (b - a) for double-float a, b
     __device__ __forceinline__ df lerp_dd(df a, df b, float f)
     {
