@@ -444,12 +444,11 @@ namespace gbint
           int jq;
           const float fq = rcq ? log_cell_frac<true>(Z.a1, rcq, x2, jq) : axis_frac_df(axq, x2.hi, x2.lo, jq);
           const df R = reg_R_df(x2);
-          df gsum{0.f, 0.f};
-          for (int s = 0; s < ns; ++s) {
-            const df z = bil_df_v1(tab, n1, j0[s], fy0[s], jq, fq);
-            gsum = df_add(gsum, df_rcp(df_add(df_mul(z, df_add(w2[s], x2)), R)));
-          }
-          if (twin) gsum = df_add(gsum, gsum);
+          // first sign, then the second (ns == 2) or the exact doubling of the first (twin)
+          df gsum = df_rcp(df_add(df_mul(bil_df_v1(tab, n1, j0[0], fy0[0], jq, fq), df_add(w2[0], x2)), R));
+          if (ns == 2)
+            gsum = df_add(gsum, df_rcp(df_add(df_mul(bil_df_v1(tab, n1, j0[1], fy0[1], jq, fq), df_add(w2[1], x2)), R)));
+          if (twin) gsum = df_scale2(gsum, 2.f);
           k.add(df_mul(rec_w(r), gsum));
         }
         return P.seg[it.seg_off + row] * k.value();
