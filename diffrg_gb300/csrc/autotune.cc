@@ -9,6 +9,7 @@
 // so that a later process on the same model skips the timing.
 #include "engine.hh"
 #include "kernels.hh"
+#include "trace.hh"
 
 #include <algorithm>
 #include <cstdio>
@@ -154,6 +155,7 @@ extern "C" int gb_autotune(gb_ctx *ctx, const gb_integral *items, int n, gb_tabl
     }
     ctx->threads_override[slot] = best_t;
     best[slot] = {best_t, best_ms};
+    if (log_enabled()) log_event("autotune", jfields("\"slot\": %d, \"threads\": %d, \"ms\": %.4f", slot, best_t, best_ms));
   }
   if (!best.empty()) write_cache(cache_path, gpu, best);
   if (chosen)

@@ -2,6 +2,7 @@
 // and execution, and the reference-pattern FP64 path.
 #include "engine.hh"
 #include "kernels.hh"
+#include "trace.hh"
 
 #include <algorithm>
 #include <cmath>
@@ -121,6 +122,7 @@ namespace
   void pool_evict_unheld(gb_ctx *ctx)
   {
     NodePool &P = ctx->pool;
+    const uint64_t ev0 = P.evictions;
     for (auto it = ctx->axis_cache.begin(); it != ctx->axis_cache.end();) {
       if (it->second.refs == 0) {
         P.free_ranges[it->second.ref.off] = it->second.ref.n;
@@ -145,6 +147,9 @@ namespace
         P.free_ranges.erase(last);
       }
     }
+    if (log_enabled())
+      log_event("node_pool_evict", jfields("\"axes\": %llu, \"used\": %d, \"free_ranges\": %zu",
+                                           (unsigned long long)(P.evictions - ev0), P.used, P.free_ranges.size()));
   }
 
   int pool_append(gb_ctx *ctx, const HostAxis &h, AxisRef &ref)
@@ -819,12 +824,17 @@ namespace gbint
       free_batch(ctx, b);
       return cuda_fail(ctx, e, "batch device buffers");
     }
+    if (log_enabled())
+      log_event("batch_create", jfields("\"integrals\": %d, \"units\": %zu, \"points\": %llu, \"bytes\": %zu, "
+                                        "\"precision\": %d, \"runs\": %zu",
+                                        n, nu, (unsigned long long)b->points, bytes, precision, b->runs.size()));
     *out = b;
     return GB_OK;
   }
 
   int run_batch(gb_ctx *ctx, gb_batch *b, double *d_out, cudaStream_t s)
   {
+    TraceRange tr("gbint run_batch");
     RunParams P{};
     P.items = b->d_items;
     P.n_items = b->n;
@@ -1174,6 +1184,7 @@ int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
 
 static int table_update_impl(gb_ctx *ctx, gb_table *t, const float *src, cudaMemcpyKind kind, void *stream)
 {
+  TraceRange tr("gbint table_update");
   if (!ctx || !t || !src || t->slot < 0) return set_error(ctx, GB_EINVAL, "bad table update");
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
@@ -1405,6 +1416,7 @@ int gb_batch_destroy(gb_ctx *ctx, gb_batch *b)
 // host and synchronises (integrator_4D_gpu.hh:141-197).  In-flight buffers are bounded to 4 GiB.
 int gb_batch_run_plain(gb_ctx *ctx, gb_batch *b, double *host_out, int n_streams)
 {
+  TraceRange tr("gbint run_plain (reference pattern)");
   if (!ctx || !b || !host_out) return GB_EINVAL;
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   GB_CUDA(cudaSetDevice(ctx->device));

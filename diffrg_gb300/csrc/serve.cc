@@ -19,6 +19,7 @@
 // back buffer, so each batch reads one consistent epoch of every table.
 #include "engine.hh"
 #include "kernels.hh"
+#include "trace.hh"
 
 #include <algorithm>
 #include <chrono>
@@ -70,6 +71,7 @@ namespace gbint
       gb_batch *plan = nullptr;
       std::vector<Request *> reqs;
       bool busy = false;
+      double t_launch = 0;
     };
 
     constexpr int kMaxRunsPerBatch = 16;
@@ -177,6 +179,18 @@ namespace gbint
     void finish_slot(gb_ctx *ctx, ServeState *S, Slot &sl, bool ok, const std::string &err)
     {
       const double t = now_s();
+      if (log_enabled()) {
+        size_t n = 0;
+        double oldest = t;
+        for (Request *r : sl.reqs) {
+          n += r->items.size();
+          oldest = std::min(oldest, r->t_submit);
+        }
+        log_event("serve_done", jfields("\"slot\": %d, \"ok\": %d, \"requests\": %zu, \"integrals\": %zu, "
+                                        "\"gpu_ms\": %.3f, \"max_latency_ms\": %.3f",
+                                        (int)(&sl - S->slots.data()), ok ? 1 : 0, sl.reqs.size(), n,
+                                        (t - sl.t_launch) * 1e3, (t - oldest) * 1e3));
+      }
       {
         std::lock_guard<std::recursive_mutex> lk(ctx->mu);
         free_batch(ctx, sl.plan);  // arena batch: releases the held axes only
@@ -238,6 +252,7 @@ namespace gbint
     // plan the group's integrals and launch them on the slot (caller: dispatcher thread)
     int launch_group(gb_ctx *ctx, ServeState *S, Slot &sl, const std::vector<Request *> &g)
     {
+      TraceRange tr("gbint serve_launch");
       std::vector<gb_integral> items;
       std::vector<gb_table *const *> tl;
       std::vector<int> tn;
@@ -306,6 +321,12 @@ namespace gbint
       }
       sl.plan = b;
       sl.reqs = g;
+      sl.t_launch = now_s();
+      if (log_enabled())
+        log_event("serve_launch", jfields("\"slot\": %d, \"requests\": %zu, \"integrals\": %d, \"points\": %llu, "
+                                          "\"high_priority\": %d, \"queue_ms\": %.3f",
+                                          (int)(&sl - S->slots.data()), g.size(), n, (unsigned long long)b->points,
+                                          s == sl.s_hi ? 1 : 0, (sl.t_launch - g[0]->t_submit) * 1e3));
       std::lock_guard<std::mutex> lk2(S->mu);
       sl.busy = true;
       S->batches++;

@@ -244,3 +244,86 @@ def test_c4_flow_step_fp32c_vs_fp64(gblib, w):
         assert st["completed"] >= 2 * 6 * 2 and st["rejected"] == 0
     finally:
         c.close()
+
+
+def test_event_log_lines_are_json(gblib, tmp_path):
+    """GBINT_LOG=<file>: batch creation, serving launches/completions and autotuning are logged
+    as one JSON object per line."""
+    import json
+    import os
+    import subprocess
+    import sys
+
+    log = tmp_path / "gbint.jsonl"
+    code = r'''
+import numpy as np
+from diffrg_gb300 import serving
+from diffrg_gb300.engine import Context
+w = serving.c4()
+ctx = Context(0)
+ts = [ctx.table(w["spec"], w["y0"][i]) for i in range(serving.N_FUNC)]
+tl = [ts[i] for i in serving.table_order()]
+items = serving.rhs_items(w, 0.5)
+b = ctx.batch(items[:64], tl); b.get(); b.close()
+ctx.serve_start(2, 512)
+tk = [ctx.submit(items[i * 100:(i + 1) * 100], tl) for i in range(5)]
+for t in tk: t.wait(timeout=120)
+ctx.autotune(items[:256], tl)
+ctx.close()
+'''
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, GBINT_LOG=str(log), PYTHONPATH=root)
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    events = [json.loads(l) for l in log.read_text().splitlines()]
+    kinds = {e["event"] for e in events}
+    assert {"batch_create", "serve_launch", "serve_done", "autotune"} <= kinds
+    done = [e for e in events if e["event"] == "serve_done"]
+    assert sum(e["integrals"] for e in done) == 500 and all(e["ok"] == 1 for e in done)
+    assert all(e["t"] >= 0 for e in events)
+
+
+def test_concurrent_host_threads(gblib, w):
+    """Many host threads using one context at once (gets, batches, submits, table updates):
+    every result equals the serial one bit for bit."""
+    import threading
+
+    c = Context(0)
+    try:
+        c.serve_start(4, 1024)
+        ts = [c.table(w["spec"], w["y0"][i]) for i in range(serving.N_FUNC)]
+        tl = [ts[i] for i in serving.table_order()]
+        items = serving.rhs_items(w, 0.65)
+        picks = list(range(0, 4096, 97))
+        b = c.batch([items[i] for i in picks], tl, "fp32c")
+        ref = b.get()
+        b.close()
+        errors = []
+
+        def worker(tid):
+            try:
+                for rep in range(4):
+                    if (tid + rep) % 3 == 0:
+                        got = c.submit([items[i] for i in picks], tl).wait(timeout=300)
+                    elif (tid + rep) % 3 == 1:
+                        bb = c.batch([items[i] for i in picks], tl, "fp32c")
+                        got = bb.get()
+                        bb.close()
+                    else:
+                        got = np.array([c.batch([items[i]], tl, "fp32c").get()[0] for i in picks[:5]])
+                        if not np.array_equal(got, ref[:5]):
+                            errors.append((tid, rep, "single"))
+                        continue
+                    if not np.array_equal(got, ref):
+                        errors.append((tid, rep))
+            except Exception as e:  # surfaced below
+                errors.append((tid, repr(e)))
+
+        th = [threading.Thread(target=worker, args=(t,)) for t in range(8)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join(timeout=600)
+        assert not errors, errors[:5]
+    finally:
+        c.close()
