@@ -42,6 +42,7 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <cuda/std/complex>
 
 #include "gbint.h"
 #include "gbint/device/families.cuh"
@@ -54,11 +55,37 @@ namespace DiFfRG
 
   namespace get_type
   {
+    // coordinate type of a result type NT (the reference's get_type::ctype): NT itself for
+    // float/double, the value type for complex numbers; specialise for other NT
     template <typename NT> struct ctype_of {
       using type = NT;
     };
+    template <typename T> struct ctype_of<cuda::std::complex<T>> {
+      using type = T;
+    };
     template <typename NT> using ctype = typename ctype_of<NT>::type;
   } // namespace get_type
+
+  namespace gbint_detail
+  {
+    // Result types are reduced component by component: C scalar components of type S (float:
+    // Kahan-compensated FP32 per thread, double: FP64).  float and double have one component,
+    // cuda::std::complex two; specialise nt_traits for other result types (e.g. a dual number
+    // holding a value and a derivative) with C, S, get(v, c) and make(double[C]).
+    template <typename NT, typename = void> struct nt_traits;
+    template <typename NT> struct nt_traits<NT, std::enable_if_t<std::is_arithmetic_v<NT>>> {
+      static constexpr int C = 1;
+      using S = NT;
+      __host__ __device__ static S get(const NT &v, int) { return v; }
+      static NT make(const double *c) { return (NT)c[0]; }
+    };
+    template <typename T> struct nt_traits<cuda::std::complex<T>> {
+      static constexpr int C = 2;
+      using S = T;
+      __host__ __device__ static S get(const cuda::std::complex<T> &v, int c) { return c ? v.imag() : v.real(); }
+      static cuda::std::complex<T> make(const double *c) { return cuda::std::complex<T>((T)c[0], (T)c[1]); }
+    };
+  } // namespace gbint_detail
 
   namespace gbint_detail
   {
@@ -240,14 +267,18 @@ namespace DiFfRG
       return v;
     }
 
-    // persistent CTAs pull units of kUnit points; FP64 block sums per unit; the last unit to
-    // arrive adds the unit partials in order (deterministic) and writes the result
+    // persistent CTAs pull units of kUnit points; FP64 block sums per unit and component; the
+    // last unit to arrive adds the unit partials in order (deterministic) and writes the C result
+    // components to partials[n_units * C + c] (component 0 also to *result)
     template <class FAM, class KERNEL, typename NT, typename ctype, class... T>
     __global__ void __launch_bounds__(kThreads)
         k_user(const gbint::fam::Params<ctype> P, long long n_points, int n_units, double *partials, int *counters,
                double *result, T... t)
     {
-      __shared__ double red[32];
+      using TR = nt_traits<NT>;
+      constexpr int C = TR::C;
+      using S = typename TR::S;
+      __shared__ double red[C][32];
       __shared__ int s_unit, s_last;
       const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
       for (;;) {
@@ -256,50 +287,79 @@ namespace DiFfRG
         const int u = s_unit;
         if (u >= n_units) break;
         const long long begin = (long long)u * kUnit;
-        double acc;
-        if constexpr (std::is_same_v<NT, float>) {
-          float s = 0.f, c = 0.f;  // Kahan
+        double acc[C];
+        if constexpr (std::is_same_v<S, float>) {
+          float s[C], c[C];  // Kahan per component
+#pragma unroll
+          for (int m = 0; m < C; ++m) s[m] = c[m] = 0.f;
 #pragma unroll 1
           for (int k = 0; k < kPPT; ++k) {
             const long long idx = begin + threadIdx.x + k * kThreads;
             if (idx < n_points) {
-              const float y = __fsub_rn((float)FAM::template eval<KERNEL, NT>(P, idx, t...), c);
-              const float tt = __fadd_rn(s, y);
-              c = __fsub_rn(__fsub_rn(tt, s), y);
-              s = tt;
+              const NT v = FAM::template eval<KERNEL, NT>(P, idx, t...);
+#pragma unroll
+              for (int m = 0; m < C; ++m) {
+                const float y = __fsub_rn((float)TR::get(v, m), c[m]);
+                const float tt = __fadd_rn(s[m], y);
+                c[m] = __fsub_rn(__fsub_rn(tt, s[m]), y);
+                s[m] = tt;
+              }
             }
           }
-          acc = (double)s - (double)c;
+#pragma unroll
+          for (int m = 0; m < C; ++m) acc[m] = (double)s[m] - (double)c[m];
         } else {
-          acc = 0.0;
+#pragma unroll
+          for (int m = 0; m < C; ++m) acc[m] = 0.0;
 #pragma unroll 1
           for (int k = 0; k < kPPT; ++k) {
             const long long idx = begin + threadIdx.x + k * kThreads;
-            if (idx < n_points) acc += (double)FAM::template eval<KERNEL, NT>(P, idx, t...);
+            if (idx < n_points) {
+              const NT v = FAM::template eval<KERNEL, NT>(P, idx, t...);
+#pragma unroll
+              for (int m = 0; m < C; ++m) acc[m] += (double)TR::get(v, m);
+            }
           }
         }
-        acc = warp_sum(acc);
-        if (lane == 0) red[wid] = acc;
+#pragma unroll
+        for (int m = 0; m < C; ++m) {
+          acc[m] = warp_sum(acc[m]);
+          if (lane == 0) red[m][wid] = acc[m];
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
-          double s = 0;
-          for (int i = 0; i < kThreads / 32; ++i) s += red[i];
-          partials[u] = s;
+#pragma unroll
+          for (int m = 0; m < C; ++m) {
+            double s = 0;
+            for (int i = 0; i < kThreads / 32; ++i) s += red[m][i];
+            partials[(size_t)u * C + m] = s;
+          }
           __threadfence();
           s_last = (atomicAdd(&counters[1], 1) == n_units - 1);
         }
         __syncthreads();
         if (s_last) {
           __threadfence();
-          double v = 0;
-          for (int i = threadIdx.x; i < n_units; i += kThreads) v += __ldcg(&partials[i]);
-          v = warp_sum(v);
-          if (lane == 0) red[wid] = v;
+          double v[C];
+#pragma unroll
+          for (int m = 0; m < C; ++m) v[m] = 0.0;
+          for (int i = threadIdx.x; i < n_units; i += kThreads)
+#pragma unroll
+            for (int m = 0; m < C; ++m) v[m] += __ldcg(&partials[(size_t)i * C + m]);
+#pragma unroll
+          for (int m = 0; m < C; ++m) {
+            v[m] = warp_sum(v[m]);
+            if (lane == 0) red[m][wid] = v[m];
+          }
           __syncthreads();
           if (threadIdx.x == 0) {
-            double s = 0;
-            for (int i = 0; i < kThreads / 32; ++i) s += red[i];
-            *result = s;
+#pragma unroll
+            for (int m = 0; m < C; ++m) {
+              double s = 0;
+              for (int i = 0; i < kThreads / 32; ++i) s += red[m][i];
+              partials[(size_t)n_units * C + m] = s;
+              if (m == 0) *result = s;
+            }
           }
         }
         __syncthreads();
@@ -310,33 +370,44 @@ namespace DiFfRG
     template <typename NT> class Pending
     {
     public:
-      Pending(std::shared_ptr<gb_ctx> ctx, gb_slot slot, NT constant) : ctx_(std::move(ctx)), slot_(slot), c_(constant) {}
+      Pending(std::shared_ptr<gb_ctx> ctx, gb_slot slot, NT constant, int n_units)
+          : ctx_(std::move(ctx)), slot_(slot), c_(constant), n_units_(n_units)
+      {
+      }
       NT get()
       {
-        double v = 0;
-        const int rc = gb_slot_wait(ctx_.get(), &slot_, &v);
+        constexpr int C = nt_traits<NT>::C;
+        double v[C] = {};
+        int rc = gb_slot_wait(ctx_.get(), &slot_, &v[0]);
+        if (rc == GB_OK && C > 1) {  // the other components, from the partials tail (stream is idle)
+          const cudaError_t e = cudaMemcpy(&v[1], slot_.partials + (size_t)n_units_ * C + 1, (C - 1) * sizeof(double),
+                                           cudaMemcpyDeviceToHost);
+          if (e != cudaSuccess) rc = GB_ECUDA;
+        }
         gb_slot_release(ctx_.get(), &slot_);
         check(ctx_.get(), rc, "request");
-        return c_ + (NT)v;
+        return c_ + nt_traits<NT>::make(v);
       }
 
     private:
       std::shared_ptr<gb_ctx> ctx_;
       gb_slot slot_;
       NT c_;
+      int n_units_;
     };
 
     template <class FAM, class KERNEL, typename NT, typename ctype, class... T>
     std::shared_ptr<Pending<NT>> launch(QuadratureProvider &qp, std::shared_ptr<gb_ctx> keep,
                                         const gbint::fam::Params<ctype> &P, NT constant, const T &...t)
     {
+      constexpr int C = nt_traits<NT>::C;
       const long long n_points = FAM::points(P);
       if (n_points <= 0) throw std::runtime_error("integrator: empty quadrature grid");
       const long long units_ll = (n_points + kUnit - 1) / kUnit;
-      if (units_ll > (1ll << 30)) throw std::runtime_error("integrator: grid too large");
+      if (units_ll > (1ll << 28)) throw std::runtime_error("integrator: grid too large");
       const int n_units = (int)units_ll;
       gb_slot slot;
-      check(qp.ctx(), gb_slot_acquire(qp.ctx(), n_units, &slot), "gb_slot_acquire");
+      check(qp.ctx(), gb_slot_acquire(qp.ctx(), (n_units + 1) * C, &slot), "gb_slot_acquire");
       const int ctas = (int)std::min<long long>(n_units, (long long)qp.num_sms() * 8);
       k_user<FAM, KERNEL, NT, ctype, T...><<<ctas, kThreads, 0, (cudaStream_t)slot.stream>>>(
           P, n_points, n_units, slot.partials, slot.counters, slot.result, t...);
@@ -345,7 +416,7 @@ namespace DiFfRG
         gb_slot_release(qp.ctx(), &slot);
         check_cuda(e, "integrator kernel launch");
       }
-      return std::make_shared<Pending<NT>>(std::move(keep), slot, constant);
+      return std::make_shared<Pending<NT>>(std::move(keep), slot, constant, n_units);
     }
 
     template <typename NT> std::future<NT> as_future(std::shared_ptr<Pending<NT>> p)
@@ -363,7 +434,7 @@ namespace DiFfRG
     {
     public:
       using ctype = typename get_type::ctype<NT>;
-      static_assert(std::is_same_v<NT, double> || std::is_same_v<NT, float>, "NT must be double or float");
+      static_assert(nt_traits<NT>::C >= 1, "NT needs gbint_detail::nt_traits (float, double, complex built in)");
 
       IntegratorBase(QuadratureProvider &qp, const std::array<uint, NAX> &gs, ctype x_extent)
           : qp_(&qp), grid_sizes_(gs)

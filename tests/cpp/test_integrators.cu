@@ -154,6 +154,49 @@ template <typename NT> double run(QuadratureProvider &qp, const Case &c)
   throw std::runtime_error("unsupported d");
 }
 
+// complex result type: real part = the K2 polynomial with coefficients A, imaginary part = with B
+struct KComplex {
+  using CT = cuda::std::complex<double>;
+  static __host__ __device__ CT kernel(double q, double c, double k, const Coeffs &A, const Coeffs &B)
+  {
+    return CT(K2<double>::kernel(q, c, k, A), K2<double>::kernel(q, c, k, B));
+  }
+  static __host__ __device__ CT constant(double k, const Coeffs &A, const Coeffs &B) { return CT(A.a[0], B.a[0]); }
+};
+struct KComplexF {
+  using CT = cuda::std::complex<float>;
+  static __host__ __device__ CT kernel(float q, float c, float k, const Coeffs &A, const Coeffs &B)
+  {
+    return CT(K2<float>::kernel(q, c, k, A), K2<float>::kernel(q, c, k, B));
+  }
+  static __host__ __device__ CT constant(float k, const Coeffs &A, const Coeffs &B) { return CT((float)A.a[0], (float)B.a[0]); }
+};
+
+int complex_cases()
+{
+  QuadratureProvider qp;
+  Coeffs A{}, B{};
+  A.a[0] = 0.25;
+  A.a[1] = 1.0;
+  A.a[3] = 0.5;
+  A.a[7] = 1.0;
+  A.a[8] = 0.3;
+  B.a[0] = -0.5;
+  B.a[2] = 2.0;
+  B.a[7] = 0.2;
+  B.a[9] = 1.0;
+  IntegratorAngleGPU<4, cuda::std::complex<double>, KComplex> IC(qp, {{48, 16}}, 1.7);
+  IntegratorAngleGPU<4, double, K2<double>> ID(qp, {{48, 16}}, 1.7);
+  IntegratorAngleGPU<4, cuda::std::complex<float>, KComplexF> IF(qp, {{48, 16}}, 1.7);
+  for (double k : {0.5, 1.0, 1.3}) {
+    const auto z = IC.get(k, A, B);
+    const auto zf = IF.request((float)k, A, B).get();
+    std::printf("CPLX %.17g %.17g %.17g %.17g %.9g %.9g\n", z.real(), z.imag(), ID.get(k, A), ID.get(k, B),
+                (double)zf.real(), (double)zf.imag());
+  }
+  return 0;
+}
+
 // device evaluation of an interpolator at host-given points (checks the device branch)
 template <typename I> __global__ void eval_pts3(I f, const double *x, int n, double *out)
 {
@@ -258,6 +301,7 @@ int interp3_cases()
 int main(int argc, char **argv)
 {
   if (argc > 1 && std::string(argv[1]) == "--interp3") return interp3_cases();
+  if (argc > 1 && std::string(argv[1]) == "--complex") return complex_cases();
   QuadratureProvider qp;
   std::string line;
   std::vector<Case> cases;

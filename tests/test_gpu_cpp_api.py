@@ -113,3 +113,14 @@ def test_3d_and_stacked_interpolators(binary):
         assert abs(dev - ana) <= 1e-12 * max(1, abs(ana))
     for dev, host, ana in rows["STACK"]:
         assert abs(dev - host) <= 1e-6 * abs(ana) and abs(dev - ana) <= 2e-6 * abs(ana)
+
+
+def test_complex_result_type(binary):
+    """NT = cuda::std::complex<double/float>: the components are reduced separately and equal
+    the two real integrals (FP64 to rounding, FP32 to 1e-5)."""
+    out = run(binary, [], extra=["--complex"])
+    rows = [list(map(float, l.split()[1:])) for l in out if l.startswith("CPLX")]
+    assert len(rows) == 3
+    for re, im, ra, rb, fre, fim in rows:
+        assert abs(re - ra) <= 1e-13 * max(1, abs(ra)) and abs(im - rb) <= 1e-13 * max(1, abs(rb))
+        assert abs(fre - ra) <= 1e-5 * max(1, abs(ra)) and abs(fim - rb) <= 1e-5 * max(1, abs(rb))
