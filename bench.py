@@ -51,7 +51,7 @@ PER_POINT = {"C1": (12, 4), "C2": (18, 4), "C3": (30, 6), "C5": (25, 4)}
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant kernel, from the
 # ncu captures summarised in profiles/ (k_fp32c_S2acc_C2_finiteT.md, k_fp32c_S3acc_C3_uneven3D.md,
 # k_fp32c_S5acc_C5_vertex4D.md)
-TRAFFIC_BYTES_PER_LAUNCH = {"C2": 381952, "C3": 8823552, "C5": 323072}
+TRAFFIC_BYTES_PER_LAUNCH = {"C2": 1175808, "C3": 8965888, "C5": 316928}
 
 
 def parse():
