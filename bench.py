@@ -52,6 +52,10 @@ PER_POINT = {"C1": (12, 4), "C2": (18, 4), "C3": (30, 6), "C5": (25, 4)}
 # ncu captures summarised in profiles/ (k_fp32c_S2acc_C2_finiteT.md, k_fp32c_S3acc_C3_uneven3D.md,
 # k_fp32c_S5acc_C5_vertex4D.md)
 TRAFFIC_BYTES_PER_LAUNCH = {"C2": 1175808, "C3": 8965888, "C5": 316928}
+# thread instructions executed per integrand point by the dominant kernel (smsp__inst_executed.sum
+# x 32 / points, same captures): with the measured step time they give the issue rate, the
+# bound this double-float code actually meets (one warp instruction per SM sub-partition and cycle)
+INSTR_PER_POINT = {"C2": 181, "C3": 499, "C5": 413}
 
 
 def parse():
@@ -371,6 +375,18 @@ def main():
             "peak_source": "measured in this run by the library's FFMA/MUFU probes (gb_measure_peaks); "
                            "MEASURED_PEAKS.json lists only HBM and BF16",
             "fp64_peak_tflops": fp64_peak}
+    ipp = INSTR_PER_POINT.get(args.workload)
+    sm_mhz = clocks.get("sm_mhz") or 0
+    if ipp and sm_mhz:
+        import ctypes as _C
+
+        dev, nsm = _C.c_int(), _C.c_int()
+        L.gb_device_info(ctx.h, _C.byref(dev), _C.byref(nsm))
+        issue_peak = nsm.value * 4 * sm_mhz * 1e6 / 1e9  # G warp instructions/s
+        issue_achieved = ipp * pts_per_s / 32 / 1e9
+        roof["issue"] = {"achieved": issue_achieved, "peak": issue_peak, "unit": "G warp-instr/s",
+                         "frac": issue_achieved / issue_peak, "instr_per_point": ipp,
+                         "note": "executed double-float instructions (ncu count per point) at the sampled SM clock"}
 
     # ---------------------------------------------------------------- accuracy + CPU baseline
     cpu = None

@@ -130,6 +130,7 @@ def load(path: str = LIB_PATH):
                               C.POINTER(C.c_int)]
     L.gb_tune_set.argtypes = [vp, C.c_int, C.c_int]
     L.gb_selftest_wait.argtypes = [vp, C.c_longlong]
+    L.gb_device_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.gb_table_group_begin.argtypes = [vp]
     L.gb_table_group_end.argtypes = [vp]
     _lib = L

@@ -670,7 +670,7 @@ namespace gbint
       const int kb = kind_base(kind);
       switch (kb) {
       case K_S1: rows = it.ax[0].n; break;
-      case K_S2: rows = (long long)it.ax[0].n * it.ax[1].n; break;
+      case K_S2: rows = (long long)it.ax[1].n * it.ax[2].n; break;  // (q, cos); inner: modes
       case K_S3: rows = (long long)it.ax[0].n * it.ax[1].n; break;
       case K_S5: rows = (long long)it.ax[0].n * it.ax[1].n; break;
       default: {

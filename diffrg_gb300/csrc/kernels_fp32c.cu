@@ -379,79 +379,93 @@ namespace gbint
     }
 
     // ---------------------------------------------------------------- S2: (mode, q, c) x FTLOOP
-    // row = (mode m, q node i); inner = c nodes, each at +w_m and (m >= pm_from) -w_m;
-    // hoisted F_{m,i} = w_m w_q Rdot(q^2) G(w_m, q^2) (FP64).  The second propagator sits at
-    // frequency +-w_m + W (W the external frequency).
+    // row = (q node i, c node l); inner = Matsubara modes m, each at +w_m and (m >= pm_from)
+    // -w_m.  x2 = |q+p|^2, its |q|-axis table fraction and R(x2) depend on the row only, so they
+    // are formed once per row instead of once per mode.  Per point: F_{m,i} G(+-w_m + W, x2)
+    // with the hoisted F_{m,i} = w_m w_q Rdot(q^2) G(w_m, q^2) (FP64, kept as a double-float
+    // pair) and W the external frequency; the row sum is multiplied by the cos weight.
     template <bool ACC>
     __device__ __forceinline__ double row_s2(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
                                              const float *tab, const TableDev *sT)
     {
-      const int nq = it.ax[1].n;
-      const int m = row / nq, i = row - m * nq;
+      const int nc = it.ax[2].n, nq = it.ax[1].n, nm = it.ax[0].n, pmf = it.ax[0].pm_from;
+      const int i = row / nc, l = row - i * nc;
       const NodeRec qr = P.prec[it.ax[1].off + i];
-      const bool pm = m >= it.ax[0].pm_from;
+      const NodeRec cr = rc[l];
       const float4 *aux = P.aux + it.aux_off;  // p^2, 2p | per (mode, sign): cell, fraction, w^2
       const float4 c = aux[0];
       const df A = df_add(rec_a(qr), df{c.x, c.y});
       const df B = df_mul(df{c.z, c.w}, rec_v(qr));
       const TableDev &Z = sT[0];
-      AxisDev axq = Z.a1;  // |q| axis, fed with x2 = |q+p|^2 -> half the log2 scale
-      axq.scale.hi *= 0.5f;
-      axq.scale.lo *= 0.5f;
       const int n1 = Z.n1;
-      // cell-centre reciprocals of the |q| axis (fed with |q+p|^2), when the table has them
-      const float2 *rcq =
-          (Z.rc_off && Z.rc_axis == 1 && Z.rc_sq) ? reinterpret_cast<const float2 *>(tab + Z.rc_off) : nullptr;
-      int j0[2];
-      float fy0[2];
-      df w2[2];
-      // With Om = 0 the +-w evaluations read |w| and w^2 only: they are bitwise equal, so one
+      // With W = 0 the +-w_m evaluations read |w| and w^2 only: they are bitwise equal, so one
       // evaluation is doubled (exact) instead of computing the second.
-      const bool twin = pm && it.args[3] == 0.0;
-      const int ns = pm && !twin ? 2 : 1;
-      for (int s = 0; s < 2; ++s) {
-        const float4 r = aux[1 + 2 * m + s];
-        j0[s] = __float_as_int(r.x);
-        fy0[s] = r.y;
-        w2[s] = df{r.z, r.w};
-      }
-      const int nc = it.ax[2].n;
+      const bool twin = it.args[3] == 0.0;
+      const float2 *F = reinterpret_cast<const float2 *>(P.seg + it.seg_off) + i;  // F_{m,i} at [m * nq]
       if constexpr (!ACC) {
+        AxisDev axq = Z.a1;  // |q| axis, fed with x2 = |q+p|^2 -> half the log2 scale
+        axq.scale.hi *= 0.5f;
+        axq.scale.lo *= 0.5f;
+        const float x2 = fmaxf(lin_df(A, B, cr.v_hi, cr.v_lo), 1e-30f);
+        int jq;
+        const float fq = axis_frac(axq, x2, jq);
+        const float R = reg_R(x2);
         Kahan k;
 #pragma unroll 1
-        for (int l = 0; l < nc; ++l) {
-          const NodeRec r = rc[l];
-          const float x2 = fmaxf(lin_df(A, B, r.v_hi, r.v_lo), 1e-30f);
-          int jq;
-          const float fq = axis_frac(axq, x2, jq);
-          const float R = reg_R(x2);
-          float gsum = 0.f;
-          for (int s = 0; s < ns; ++s) {
-            const float z = bil32_v1(tab, n1, j0[s], fy0[s], jq, fq);
-            const float den = __fmaf_rn(z, __fadd_rn(__fadd_rn(w2[s].hi, x2), w2[s].lo), R);
-            gsum = __fadd_rn(gsum, rcp32(den));
+        for (int m = 0; m < nm; ++m) {
+          const float4 r0 = aux[1 + 2 * m];
+          float g = rcp32(__fmaf_rn(bil32_v1(tab, n1, __float_as_int(r0.x), r0.y, jq, fq),
+                                    __fadd_rn(__fadd_rn(r0.z, x2), r0.w), R));
+          if (m >= pmf) {
+            if (twin) {
+              g = __fadd_rn(g, g);
+            } else {
+              const float4 r1 = aux[2 + 2 * m];
+              g = __fadd_rn(g, rcp32(__fmaf_rn(bil32_v1(tab, n1, __float_as_int(r1.x), r1.y, jq, fq),
+                                               __fadd_rn(__fadd_rn(r1.z, x2), r1.w), R)));
+            }
           }
-          if (twin) gsum = __fadd_rn(gsum, gsum);
-          k.add(__fmaf_rn(r.w_hi, gsum, __fmul_rn(r.w_lo, gsum)));
+          const float2 f = F[(size_t)m * nq];
+          k.add(__fmaf_rn(f.x, g, __fmul_rn(f.y, g)));
         }
-        return P.seg[it.seg_off + row] * k.value();
+        return (double)df_round(rec_w(cr)) * k.value();
       } else {
+        // cell-centre reciprocals of the |q| axis (fed with |q+p|^2), when the table has them
+        const float2 *rcq =
+            (Z.rc_off && Z.rc_axis == 1 && Z.rc_sq) ? reinterpret_cast<const float2 *>(tab + Z.rc_off) : nullptr;
+        const df x2 = df_max(lin_dd(A, B, cr.v_hi, cr.v_lo), 1e-30f);
+        int jq;
+        float fq;
+        if (rcq) {
+          fq = log_cell_frac<true>(Z.a1, rcq, x2, jq);
+        } else {
+          AxisDev axq = Z.a1;
+          axq.scale.hi *= 0.5f;
+          axq.scale.lo *= 0.5f;
+          fq = axis_frac_df(axq, x2.hi, x2.lo, jq);
+        }
+        const df R = reg_R_df(x2);
         AccDF k;
 #pragma unroll 1
-        for (int l = 0; l < nc; ++l) {
-          const NodeRec r = rc[l];
-          const df x2 = df_max(lin_dd(A, B, r.v_hi, r.v_lo), 1e-30f);
-          int jq;
-          const float fq = rcq ? log_cell_frac<true>(Z.a1, rcq, x2, jq) : axis_frac_df(axq, x2.hi, x2.lo, jq);
-          const df R = reg_R_df(x2);
-          // first sign, then the second (ns == 2) or the exact doubling of the first (twin)
-          df gsum = df_rcp(df_add(df_mul(bil_df_v1(tab, n1, j0[0], fy0[0], jq, fq), df_add(w2[0], x2)), R));
-          if (ns == 2)
-            gsum = df_add(gsum, df_rcp(df_add(df_mul(bil_df_v1(tab, n1, j0[1], fy0[1], jq, fq), df_add(w2[1], x2)), R)));
-          if (twin) gsum = df_scale2(gsum, 2.f);
-          k.add(df_mul(rec_w(r), gsum));
+        for (int m = 0; m < nm; ++m) {
+          const float4 r0 = aux[1 + 2 * m];
+          // first sign, then the second or the exact doubling of the first (twin)
+          df g = df_rcp(df_add(df_mul(bil_df_v1(tab, n1, __float_as_int(r0.x), r0.y, jq, fq), df_add(df{r0.z, r0.w}, x2)), R));
+          if (m >= pmf) {
+            if (twin) {
+              g = df_scale2(g, 2.f);
+            } else {
+              const float4 r1 = aux[2 + 2 * m];
+              g = df_add(g, df_rcp(df_add(df_mul(bil_df_v1(tab, n1, __float_as_int(r1.x), r1.y, jq, fq),
+                                                 df_add(df{r1.z, r1.w}, x2)),
+                                          R)));
+            }
+          }
+          const float2 f = F[(size_t)m * nq];
+          k.add(df_mul(df{f.x, f.y}, g));
         }
-        return P.seg[it.seg_off + row] * k.value();
+        const df row_sum = df_mul(rec_w(cr), k.sum());
+        return (double)row_sum.hi + (double)row_sum.lo;
       }
     }
 

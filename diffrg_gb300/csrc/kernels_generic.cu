@@ -153,7 +153,10 @@ namespace gbint
       const int nm = S.ax0.off + m, nq = S.ax1.off + i;
       const double q = pv[nq], q2 = q * q;
       F = pw[nm] * pw[nq] * reg_Rdot(q2) * ft_G64(T, pv[nm], q2, S.par[0]);
-      break;
+      // the S2 kernel multiplies this factor per point: stored as a double-float pair
+      const dev::df f = dev::df_from(F);
+      reinterpret_cast<float2 *>(out)[S.off + e] = make_float2(f.hi, f.lo);
+      return;
     }
     case SEG_S3: {
       const int i = S.ax0.off + e;
