@@ -278,7 +278,6 @@ namespace gbint
       return lerp_dd(lerp_df(r0[0], r0[1], fy), lerp_df(r1[0], r1[1], fy), fx);
     }
 
-    // Kahan sum of the high parts plus a plain FP32 sum of the low parts of double-float terms
     // Double-float running sum of double-float terms (accurate form).  A Kahan sum of the high
     // parts loses ~one FP32 rounding of every term (the compensated difference x - c is itself
     // rounded): ~6e-8 per term, ~1e-8 per row and ~3e-10 on a 2048-point integral, measured; the
@@ -445,12 +444,37 @@ namespace gbint
           fq = axis_frac_df(axq, x2.hi, x2.lo, jq);
         }
         const df R = reg_R_df(x2);
+        // The |q| lerps of the table's mode rows j0 and j0+1 at this row's fraction fq are kept
+        // from one mode to the next: consecutive modes mostly move to the next pair of rows, so
+        // one new |q| lerp per mode remains (the mode lerp with fraction fy0 follows).
+        const float *Tq = tab + jq;
+        int jc = -2;
+        df zlo{0.f, 0.f}, zhi{0.f, 0.f};
         AccDF k;
+        // the mode record and hoisted factor of the next mode are loaded one iteration ahead
+        // (global/L1 latency would otherwise stall every mode)
+        float4 r0n = __ldg(aux + 1);
+        float2 fn = __ldg(F);
 #pragma unroll 1
         for (int m = 0; m < nm; ++m) {
-          const float4 r0 = aux[1 + 2 * m];
+          const float4 r0 = r0n;
+          const float2 f = fn;
+          if (m + 1 < nm) {
+            r0n = __ldg(aux + 1 + 2 * (m + 1));
+            fn = __ldg(F + (size_t)(m + 1) * nq);
+          }
+          const int j = __float_as_int(r0.x);
+          if (j != jc) {
+            if (j == jc + 1) {
+              zlo = zhi;
+            } else {
+              zlo = lerp_df(Tq[j * n1], Tq[j * n1 + 1], fq);
+            }
+            zhi = lerp_df(Tq[(j + 1) * n1], Tq[(j + 1) * n1 + 1], fq);
+            jc = j;
+          }
           // first sign, then the second or the exact doubling of the first (twin)
-          df g = df_rcp(df_add(df_mul(bil_df_v1(tab, n1, __float_as_int(r0.x), r0.y, jq, fq), df_add(df{r0.z, r0.w}, x2)), R));
+          df g = df_rcp(df_add(df_mul(lerp_dd(zlo, zhi, r0.y), df_add(df{r0.z, r0.w}, x2)), R));
           if (m >= pmf) {
             if (twin) {
               g = df_scale2(g, 2.f);
@@ -461,7 +485,6 @@ namespace gbint
                                           R)));
             }
           }
-          const float2 f = F[(size_t)m * nq];
           k.add(df_mul(df{f.x, f.y}, g));
         }
         const df row_sum = df_mul(rec_w(cr), k.sum());
