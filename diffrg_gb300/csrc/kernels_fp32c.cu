@@ -517,30 +517,35 @@ namespace gbint
       const float *TB = tab + toff[1], *TC = tab + toff[2], *TD = tab + toff[3];
       const AxisDev aB = sT[1].a0, aC = sT[2].a0, aD = sT[3].a0;
       const int nf = it.ax[2].n;
+      // The integrand reads phi only through cos(phi), and the phi rule is symmetric
+      // (phi_l + phi_{n-1-l} = 2 pi, equal weights): the first half of the nodes is summed with
+      // doubled weights (the middle node of an odd rule once).
+      const int nh = (nf + 1) >> 1;
       double inner;
       if constexpr (!ACC) {
         const float sb = df_round(sbd);
         Kahan k;
 #pragma unroll 1
-        for (int l = 0; l < nf; ++l) {
+        for (int l = 0; l < nh; ++l) {
           const NodeRec r = rc[l];  // a = cos(phi), w = 2 pi w_phi
           const float r2 = fmaxf(lin_df(A, B, r.a_hi, r.a_lo), 1e-30f);
           const float t2 = fmaxf(lin_df(Ap, Bh, r.a_hi, r.a_lo), 1e-30f);
           const float sv = __fmaf_rn(r2, third.hi, __fmaf_rn(r2, third.lo, sb));
           const float g = G1_32(TB, aB, r2) * V1_32(TC, aC, sv) * V1_32(TD, aD, t2);
-          k.add(__fmaf_rn(r.w_hi, g, __fmul_rn(r.w_lo, g)));
+          const float ws = 2 * l + 1 == nf ? 1.f : 2.f;
+          k.add(__fmaf_rn(ws * r.w_hi, g, __fmul_rn(ws * r.w_lo, g)));
         }
         inner = k.value();
       } else {
         AccDF k;
 #pragma unroll 1
-        for (int l = 0; l < nf; ++l) {
+        for (int l = 0; l < nh; ++l) {
           const NodeRec r = rc[l];
           const df r2 = df_max(lin_dd(A, B, r.a_hi, r.a_lo), 1e-30f);
           const df t2 = df_max(lin_dd(Ap, Bh, r.a_hi, r.a_lo), 1e-30f);
           const df sv = df_add(sbd, df_mul(r2, third));
           const df g = df_mul(df_mul(G1_df(TB, sT[1], r2), V1_df(TC, sT[2], sv)), V1_df(TD, sT[3], t2));
-          k.add(df_mul(rec_w(r), g));
+          k.add(df_mul(df_scale2(rec_w(r), 2 * l + 1 == nf ? 1.f : 2.f), g));
         }
         inner = k.value();
       }
@@ -573,6 +578,9 @@ namespace gbint
       int jc1;
       const float fc1 = axis_frac_lin_df(TA.a1, c1, jc1);
       const int n2 = it.ax[2].n, n3 = it.ax[3].n;
+      // the inner integrand reads phi only through cos(phi) and the phi rule is symmetric: the
+      // first half of the nodes with doubled weights (the middle node of an odd rule once)
+      const int nh3 = (n3 + 1) >> 1;
       const NodeRec *rphi = rc + n2;
       if constexpr (!ACC) {
         const float r1 = df_round(r1d);
@@ -589,14 +597,15 @@ namespace gbint
           const df Bs = df_mul(B2, rec_a(r2r));
           Kahan kin;
 #pragma unroll 2
-          for (int m = 0; m < n3; ++m) {
+          for (int m = 0; m < nh3; ++m) {
             const NodeRec rp = rphi[m];  // a = cos(phi), w = 2 pi w_phi
             const float x = fmaxf(lin_df(A2, Bs, rp.a_hi, rp.a_lo), 1e-30f);
             int ix;
             const float fx = axis_frac(TA.a0, x, ix);
             const float gv = rcp32(__fmaf_rn(bil32_v0(DA, tn1, ix, fx, jc1, fc1), x, reg_R(x)));
             const float g = gv * bil32_v0(DB, tn1, ix, fx, jc2, fc2);
-            kin.add(__fmaf_rn(rp.w_hi, g, __fmul_rn(rp.w_lo, g)));
+            const float ws = 2 * m + 1 == n3 ? 1.f : 2.f;
+            kin.add(__fmaf_rn(ws * rp.w_hi, g, __fmul_rn(ws * rp.w_lo, g)));
           }
           const float mt = __fmul_rn((float)kin.value(), gr1);
           kmid.add(__fmaf_rn(r2r.w_hi, mt, __fmul_rn(r2r.w_lo, mt)));
@@ -616,14 +625,14 @@ namespace gbint
           const df Bs = df_mul(B2, rec_a(r2r));
           AccDF kin;
 #pragma unroll 1
-          for (int m = 0; m < n3; ++m) {
+          for (int m = 0; m < nh3; ++m) {
             const NodeRec rp = rphi[m];
             const df x = df_max(lin_dd(A2, Bs, rp.a_hi, rp.a_lo), 1e-30f);
             int ix;
             const float fx = frac1_df(DA, TA, x, ix);
             const df gv = df_rcp(df_add(df_mul(bil_df_v0(DA, tn1, ix, fx, jc1, fc1), x), reg_R_df(x)));
             const df g = df_mul(gv, bil_df_v0(DB, tn1, ix, fx, jc2, fc2));
-            kin.add(df_mul(rec_w(rp), g));
+            kin.add(df_mul(df_scale2(rec_w(rp), 2 * m + 1 == n3 ? 1.f : 2.f), g));
           }
           const df si = kin.sum();
           kmid.add(df_mul(rec_w(r2r), df_mul(si, gr1)));
