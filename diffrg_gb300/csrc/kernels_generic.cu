@@ -180,8 +180,11 @@ namespace gbint
   {
     (void)pa;
     if (n_segs == 0) return cudaSuccess;
-    dim3 grid((max_entries + 255) / 256, n_segs);
-    k_seg<<<grid, 256, 0, s>>>(segs, pv, pw, tabs, seg_out);
+    // each entry is a chain of FP64 operations on the low-rate FP64 pipe: small CTAs spread the
+    // entries over all SMs instead of queueing them on a few
+    constexpr int kSegThreads = 64;
+    dim3 grid((max_entries + kSegThreads - 1) / kSegThreads, n_segs);
+    k_seg<<<grid, kSegThreads, 0, s>>>(segs, pv, pw, tabs, seg_out);
     return cudaGetLastError();
   }
 
