@@ -144,6 +144,14 @@ def cpu_baseline(w, W, reps=2):
                            % (w["name"], n, reps)}
 
 
+def workload_name(name):
+    """The workload label both arms print in config.workload."""
+    return {"C1": "C1 d=4 loop: 64 p x 64 q x 32 cos",
+            "C2": "C2 finite-T 3+1D loop: 3 T x 128 p, n=-64..64 x 64 q x 32 cos",
+            "C3": "C3 4096 uneven 3D loops, GL orders 16..256 per axis",
+            "C5": "C5 4D vertex loop: 128 x (128 q x 64 cos1 x 32 cos2 x 16 phi)"}.get(name, name)
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -168,8 +176,8 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)",
-            "config": {"workload": "%s finite-T 3+1D loop" % args.workload if args.workload == "C2" else args.workload,
-                       "integrals_per_step": int(sub.size), "l2": "n/a (CPU)"},
+            "config": {"workload": workload_name(args.workload), "integrals_per_step": int(sub.size),
+                       "l2": "n/a (CPU)"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "%d of %d %s integrals per step (every 4th), FP64 restatement of the "
                                        "reference CPU integrators, OpenMP over integrals" % (sub.size, n, args.workload)},
@@ -412,8 +420,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": statistics.mean(per32), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (compensated) + f64 reduction",
             "data": "synthetic (seeded tables and momenta, no dataset)",
-            "config": {"workload": "C2 finite-T 3+1D loop: 3 T x 128 p, n=-64..64 x 64 q x 32 cos"
-                       if args.workload == "C2" else args.workload,
+            "config": {"workload": workload_name(args.workload),
                        "integrals_per_step": n_int, "points_per_step": points,
                        "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1 else "1 GPU"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
