@@ -5,14 +5,14 @@
 //     (cp.async.bulk + mbarrier complete_tx) and restaged only when an item uses others;
 //   * work units (item, row range) come from an atomic counter; the node records of the unit's
 //     inner axes are TMA-prefetched into a second buffer while the current unit computes;
-//   * one thread per row loops over the inner axes in FP32 with double-float constants and a
-//     Kahan sum, multiplies by the row's hoisted FP64 factor, and the unit is reduced in FP64;
+//   * one thread per row loops over the inner axes on the FP32 pipe with double-float constants,
+//     combines with the row's hoisted factor, and the unit is reduced in FP64;
 //   * the last unit of an item sums the item's unit partials in a fixed order (deterministic).
 // Two arithmetic variants per kind:
-//   fast (ACC = false): per-point factors in FP32 (rms error ~5e-8 per factor, no bias);
-//   accurate (ACC = true): the same factors in double-float -- coordinate, table index and
-//     interpolation, regulator, reciprocal and weighted term -- for integrals whose weight sits
-//     on few points (rms error a few 1e-9 per factor).
+//   fast (ACC = false): per-point factors in FP32 and a Kahan sum (~1e-8 of FP64);
+//   accurate (ACC = true, GB_PREC_FP32C): coordinate, table fraction and interpolation,
+//     regulator, reciprocal, weighted term and row sum in double-float (3e-12 .. 1.2e-10 of FP64
+//     on the benchmark workloads).
 // Tensor cores are not used: this is a reduction, not a dense contraction.
 #include "device_common.cuh"
 #include "integrands.cuh"
@@ -73,7 +73,6 @@ namespace gbint
 
     __device__ __forceinline__ float rcp32(float x) { return __frcp_rn(x); }
 
-    // G = 1/(Z x + R(x)) for a 1D table, fast and accurate forms
     // Fraction of a double-float coordinate x in cell j of a 1D log table, relative to the cell
     // centre c_j (rc[j] = 1/c_j as hi, lo): f = 1/2 + kln ln(x / c_j) with
     // ln(1+t) = t + t^2 Q(t), t = x/c_j - 1 formed in double-float (p.hi - 1 is exact) and
@@ -282,11 +281,19 @@ namespace gbint
     // parts loses ~one FP32 rounding of every term (the compensated difference x - c is itself
     // rounded): ~6e-8 per term, ~1e-8 per row and ~3e-10 on a 2048-point integral, measured; the
     // double-float sum keeps ~2^-44 per term.
+    // The high parts are summed exactly (two_sum), their rounding errors and the terms' low parts
+    // collect in an FP32 low word that is renormalised only when read (it stays ~2^-24 of the
+    // sum, so its own rounding is ~2^-48 per term).
     struct AccDF {
-      df s{0.f, 0.f};
-      __device__ __forceinline__ void add(df t) { s = df_add(s, t); }
-      __device__ __forceinline__ df sum() const { return s; }
-      __device__ __forceinline__ double value() const { return (double)s.hi + (double)s.lo; }
+      float hi = 0.f, lo = 0.f;
+      __device__ __forceinline__ void add(df t)
+      {
+        const df e = two_sum(hi, t.hi);
+        hi = e.hi;
+        lo = __fadd_rn(lo, __fadd_rn(e.lo, t.lo));
+      }
+      __device__ __forceinline__ df sum() const { return fast_two_sum(hi, lo); }
+      __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
     };
 
     // ---------------------------------------------------------------- per-kind traits
