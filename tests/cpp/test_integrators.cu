@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 
+#include "gbint/autodiff.hh"
 #include "gbint/integrators.hh"
 #include "gbint/interpolators.hh"
 
@@ -197,6 +198,102 @@ int complex_cases()
   return 0;
 }
 
+// dual result type (the role of autodiff::real): the polynomial integrands times e^{-s u},
+// u = q^2/k^2 (Cartesian: qx^2/k^2), with s the seeded variable.  The value and the
+// s-derivative are compared with two plain FP64 integrals of e^{-s u} f and -u e^{-s u} f.
+template <typename T> struct KDualAngle {
+  using R = gbint::dual<T>;
+  static __host__ __device__ R kernel(T q, T c, T k, const Coeffs &C, const R &s)
+  {
+    return K2<T>::kernel(q, c, k, C) * exp(-s * (q * q / (k * k)));
+  }
+  static __host__ __device__ R constant(T, const Coeffs &C, const R &) { return R(C.a[0]); }
+};
+struct KDualCart {
+  using R = gbint::real;
+  static __host__ __device__ R kernel(double qx, double k, const Coeffs &C, const R &s)
+  {
+    return K1<double>::kernel(qx, k, C) * exp(-s * (qx * qx / (k * k)));
+  }
+  static __host__ __device__ R constant(double, const Coeffs &C, const R &) { return R(C.a[0]); }
+};
+struct KDualFT {
+  using R = gbint::real;
+  static __host__ __device__ R kernel(double q, double c, double q0, double k, const Coeffs &C, const R &s)
+  {
+    return KT2<double>::kernel(q, c, q0, k, C) * exp(-s * (q * q / (k * k)));
+  }
+  static __host__ __device__ R constant(double, const Coeffs &C, const R &) { return R(C.a[0]); }
+};
+template <int DER> __host__ __device__ inline double damped(double f, double u, double s)
+{
+  const double e = ::exp(-s * u) * f;
+  return DER ? -u * e : e;
+}
+template <int DER> struct PDualAngle {
+  static __host__ __device__ double kernel(double q, double c, double k, const Coeffs &C, double s)
+  {
+    return damped<DER>(K2<double>::kernel(q, c, k, C), q * q / (k * k), s);
+  }
+  static __host__ __device__ double constant(double, const Coeffs &C, double) { return DER ? 0.0 : C.a[0]; }
+};
+template <int DER> struct PDualCart {
+  static __host__ __device__ double kernel(double qx, double k, const Coeffs &C, double s)
+  {
+    return damped<DER>(K1<double>::kernel(qx, k, C), qx * qx / (k * k), s);
+  }
+  static __host__ __device__ double constant(double, const Coeffs &C, double) { return DER ? 0.0 : C.a[0]; }
+};
+template <int DER> struct PDualFT {
+  static __host__ __device__ double kernel(double q, double c, double q0, double k, const Coeffs &C, double s)
+  {
+    return damped<DER>(KT2<double>::kernel(q, c, q0, k, C), q * q / (k * k), s);
+  }
+  static __host__ __device__ double constant(double, const Coeffs &C, double) { return DER ? 0.0 : C.a[0]; }
+};
+
+// prints "DUAL <family> value derivative plain_value plain_derivative" per case
+int dual_cases()
+{
+  QuadratureProvider qp;
+  Coeffs A{};
+  A.a[0] = 0.25;
+  A.a[1] = 1.0;
+  A.a[3] = 0.5;
+  A.a[7] = 1.0;
+  A.a[8] = 0.3;
+  A.a[19] = 1.0;  // q0 factor 1 + q0^2 (finite T)
+  A.a[21] = 1.0;
+  IntegratorAngleGPU<4, gbint::real, KDualAngle<double>> IA(qp, {{48, 16}}, 1.7);
+  IntegratorAngleGPU<4, gbint::dual<float>, KDualAngle<float>> IAf(qp, {{48, 16}}, 1.7);
+  IntegratorAngleGPU<4, double, PDualAngle<0>> PA0(qp, {{48, 16}}, 1.7);
+  IntegratorAngleGPU<4, double, PDualAngle<1>> PA1(qp, {{48, 16}}, 1.7);
+  Integrator1DCartesianGPU<gbint::real, KDualCart> IC(qp, {{32}});
+  Integrator1DCartesianGPU<double, PDualCart<0>> PC0(qp, {{32}});
+  Integrator1DCartesianGPU<double, PDualCart<1>> PC1(qp, {{32}});
+  PC0.set_qx_min(-1.5), PC0.set_qx_max(1.2);
+  PC1.set_qx_min(-1.5), PC1.set_qx_max(1.2);
+  IC.set_qx_min(-1.5), IC.set_qx_max(1.2);
+  IntegratorAngleFiniteTq0GPU<4, gbint::real, KDualFT> IT(qp, {{32, 12}}, 1.5, 0.2);
+  IntegratorAngleFiniteTq0GPU<4, double, PDualFT<0>> PT0(qp, {{32, 12}}, 1.5, 0.2);
+  IntegratorAngleFiniteTq0GPU<4, double, PDualFT<1>> PT1(qp, {{32, 12}}, 1.5, 0.2);
+  for (double k : {0.6, 1.1}) {
+    for (double s : {0.3, 1.7}) {
+      const gbint::real sd = gbint::seed(s);
+      const gbint::real a = IA.get(k, A, sd);
+      const gbint::dual<float> af = IAf.request((float)k, A, gbint::seed((float)s)).get();
+      std::printf("DUAL ANGLE %.17g %.17g %.17g %.17g\n", val(a), derivative(a), PA0.get(k, A, s), PA1.get(k, A, s));
+      std::printf("DUAL ANGLEF %.9g %.9g %.17g %.17g\n", (double)val(af), (double)derivative(af), PA0.get(k, A, s),
+                  PA1.get(k, A, s));
+      const gbint::real c = IC.request(k, A, sd).get();
+      std::printf("DUAL CART1 %.17g %.17g %.17g %.17g\n", val(c), derivative(c), PC0.get(k, A, s), PC1.get(k, A, s));
+      const gbint::real t = IT.get(k, A, sd);
+      std::printf("DUAL FTQ0 %.17g %.17g %.17g %.17g\n", val(t), derivative(t), PT0.get(k, A, s), PT1.get(k, A, s));
+    }
+  }
+  return 0;
+}
+
 // device evaluation of an interpolator at host-given points (checks the device branch)
 template <typename I> __global__ void eval_pts3(I f, const double *x, int n, double *out)
 {
@@ -302,6 +399,7 @@ int main(int argc, char **argv)
 {
   if (argc > 1 && std::string(argv[1]) == "--interp3") return interp3_cases();
   if (argc > 1 && std::string(argv[1]) == "--complex") return complex_cases();
+  if (argc > 1 && std::string(argv[1]) == "--dual") return dual_cases();
   QuadratureProvider qp;
   std::string line;
   std::vector<Case> cases;

@@ -124,3 +124,23 @@ def test_complex_result_type(binary):
     for re, im, ra, rb, fre, fim in rows:
         assert abs(re - ra) <= 1e-13 * max(1, abs(ra)) and abs(im - rb) <= 1e-13 * max(1, abs(rb))
         assert abs(fre - ra) <= 1e-5 * max(1, abs(ra)) and abs(fim - rb) <= 1e-5 * max(1, abs(rb))
+
+
+def test_dual_result_type(binary):
+    """NT = gbint::dual<double/float> (the role of autodiff::real in the reference, e.g.
+    DiFfRG/tests/physics/integration/integrator_1D_cartesian_gpu.cu:133-184): value and
+    derivative components are reduced separately and equal the two plain FP64 integrals of
+    e^{-s u} f and -u e^{-s u} f (FP64 to rounding, FP32 to 1e-5), for the angle, Cartesian 1D
+    and finite-T q0 families, through get() and request()."""
+    out = run(binary, [], extra=["--dual"])
+    rows = [l.split()[1:] for l in out if l.startswith("DUAL")]
+    assert len(rows) == 16
+    fams = set()
+    for fam, *vals in rows:
+        v, d, pv, pd = map(float, vals)
+        fams.add(fam)
+        tol = 1e-5 if fam == "ANGLEF" else 1e-13
+        assert abs(v - pv) <= tol * max(1, abs(pv)), (fam, v, pv)
+        assert abs(d - pd) <= tol * max(1, abs(pd)), (fam, d, pd)
+        assert abs(pd) > 1e-6  # the derivative is not trivially zero (integrals here are ~1e-4..1e-2)
+    assert fams == {"ANGLE", "ANGLEF", "CART1", "FTQ0"}

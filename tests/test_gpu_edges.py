@@ -1,0 +1,101 @@
+"""Edge cases of the catalogue paths through the C ABI, against the FP64 oracle.
+
+* extreme and ragged quadrature orders of the 3D family (workload C3's integrand): the largest
+  order (256^3 = 16.8M points in one integral), the smallest, and phi orders 1 and 2 and odd /
+  even mixes (the phi fold sums the first half of a symmetric rule with doubled weights and
+  the middle node of an odd rule once);
+* external momentum p = 0 (C1, C3);
+* a NaN-filled dressing table poisons only the integrals that read it (per-item tables via
+  table_base), in a batch with clean ones;
+* an empty batch is an argument error (status code), not a launch.
+
+Tolerances as in test_gpu_parity.py: FP64 1e-12, FP32C 1e-9.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 1e-9
+
+
+@pytest.fixture(scope="module")
+def W():
+    from diffrg_gb300 import workloads
+
+    return workloads
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=float)
+    b = np.asarray(b, dtype=float)
+    return np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+
+
+def run(ctx, W, w, prec):
+    items, tabs = W.engine_items(w)
+    T = [ctx.table(s, d) for s, d in tabs]
+    b = ctx.batch(items, T, prec)
+    out = b.get()
+    b.close()
+    for t in T:
+        t.close()
+    return out
+
+
+C3_ORDERS = [(256, 256, 256), (16, 16, 16), (16, 256, 17), (33, 16, 1), (16, 40, 2), (255, 17, 3), (1, 1, 1),
+             (64, 1, 64)]
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32c", TOL32)])
+def test_c3_extreme_and_ragged_orders(ctx, oracle, W, prec, tol):
+    w = W.c3(8)
+    w["orders"] = np.array(C3_ORDERS, dtype=np.int32)
+    w["P"] = np.array([0.7, 0.01, 3.9, 0.0, 1.3, 0.2, 0.5, 2.0])
+    got = run(ctx, W, w, prec)
+    ref = W.oracle_values(w, oracle)
+    err = rel(got, ref)
+    print(prec, "C3 edge orders max rel err %.3e" % err.max())
+    assert np.all(np.isfinite(got))
+    assert err.max() <= tol
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32c", TOL32)])
+def test_zero_external_momentum(ctx, oracle, W, prec, tol):
+    w = W.c1()
+    w["p"] = np.array([0.0, 1e-3, 0.0, 2.0])
+    got = run(ctx, W, w, prec)
+    ref = W.oracle_values(w, oracle)
+    assert rel(got, ref).max() <= tol
+    assert got[0] == got[2]  # same integral, same bits
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_nan_table_poisons_only_its_items(ctx, oracle, W, prec):
+    w = W.c1()
+    w["p"] = w["p"][:4]
+    spec, Z = w["tables"][0]
+    Znan = np.full_like(Z, np.nan)
+    items, _ = W.engine_items(w)
+    # items 0 and 2 read the NaN table (table_base 0), items 1 and 3 the clean one (table_base 1)
+    for i, g in enumerate(items):
+        g.table_base = i % 2
+    tn, tc = ctx.table(spec, Znan), ctx.table(spec, Z)
+    b = ctx.batch(items, [tn, tc], prec)
+    out = b.get()
+    b.close()
+    tn.close()
+    tc.close()
+    ref = W.oracle_values(w, oracle)
+    assert np.isnan(out[0]) and np.isnan(out[2])
+    tol = TOL64 if prec == "fp64" else TOL32
+    assert rel(out[[1, 3]], ref[[1, 3]]).max() <= tol
+
+
+def test_empty_batch_is_an_argument_error(ctx):
+    from diffrg_gb300 import GbError
+
+    with pytest.raises(GbError) as e:
+        ctx.batch([], (), "fp32c")
+    assert e.value.code == 1
