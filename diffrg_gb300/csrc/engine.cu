@@ -595,6 +595,7 @@ namespace gbint
     b->src.assign(items, items + n);
     b->items.resize(n);
     std::map<std::tuple<int, int, int, int, double>, int> seg_index;  // dedupe
+    std::map<std::tuple<int, int, int, double, double>, int> slice_index;
     std::vector<int> item_kind(n);
     for (int i = 0; i < n; ++i) {
       const gb_integral &g = items[i];
@@ -712,6 +713,32 @@ namespace gbint
         } else
           it.seg_off = b->segs[f->second].off;
       }
+      // S2, accurate form: the table interpolated along its mode axis at each (mode, sign)
+      // frequency, per |q| cell, so that a point lerps along |q| only; shared by the items with
+      // the same table, mode axis, T and external frequency
+      if (kind == (K_S2 | K_ACC)) {
+        const double Tt = g.args[2], Om = g.args[3];
+        auto key = std::make_tuple(it.tab[0], it.ax[0].off, it.ax[0].n, Tt, Om);
+        auto f = slice_index.find(key);
+        if (f == slice_index.end()) {
+          SegDev S{};
+          S.kind = SEG_S2Z;
+          S.tab = it.tab[0];
+          S.ax0 = it.ax[0];
+          S.n0 = 2 * it.ax[0].n;               // (mode, sign) records
+          S.n1 = tables[0]->spec.n1 - 1;        // |q| cells
+          S.par[0] = Om;
+          S.par[1] = 1.0 / (2.0 * 3.14159265358979323846 * Tt);
+          b->seg_total += b->seg_total & 1;    // float4 entries: 16-byte aligned
+          S.off = (int)b->seg_total;
+          b->seg_total += 2 * (size_t)S.n0 * S.n1;
+          b->seg_max_entries = std::max(b->seg_max_entries, S.n0 * S.n1);
+          slice_index[key] = S.off;
+          b->segs.push_back(S);
+          it.slice_off = S.off;
+        } else
+          it.slice_off = f->second;
+      }
       if (kind != K_GENERIC) item_aux(ctx, g, it, &ctx->axis_cache.at(b->held[held0]).v, b->aux);
       // reference-pattern geometry
       int loop_axis = -1;
@@ -749,7 +776,11 @@ namespace gbint
         }
         if (kind != K_GENERIC) {
           int tb = 0;
-          for (int t = 0; t < tables_needed(it.integrand); ++t) tb += ctx->slots[it.tab[t]]->bytes;
+          for (int t = 0; t < tables_needed(it.integrand); ++t) {
+            const TableDev &D = ctx->h_dir[it.tab[t]];
+            // S2 accurate form: only the cell-centre reciprocals are staged
+            tb += kind == (K_S2 | K_ACC) ? (D.rc_off ? D.bytes - 4 * D.rc_off : 0) : ctx->slots[it.tab[t]]->bytes;
+          }
           tab_cap = std::max(tab_cap, tb);
           int rc_n = 0;
           if (kb == K_S1) rc_n = it.ax[1].n;

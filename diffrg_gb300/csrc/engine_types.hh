@@ -57,6 +57,7 @@ namespace gbint
     int seg_stride;  // row stride inside the segment
     int tab[4];      // table directory slots
     int aux_off;     // per-item constants of the S kinds in RunParams::aux (float4 records)
+    int slice_off;   // S2 (accurate form): mode-interpolated table slices in the segment arena (doubles)
     double k;
     double args[GB_MAX_ARGS];
   };
@@ -107,7 +108,9 @@ namespace gbint
   };
 
   // hoisted-factor segment kinds
-  enum SegKind : int { SEG_S1 = 1, SEG_S2 = 2, SEG_S3 = 3, SEG_S5 = 5 };
+  // SEG_S2Z: the S2 dressing table interpolated along its mode axis at every (mode, sign)
+  // frequency of an item, per |q| cell: float4 {z hi, lo, dz hi, lo} (two doubles per entry)
+  enum SegKind : int { SEG_S1 = 1, SEG_S2 = 2, SEG_S3 = 3, SEG_S5 = 5, SEG_S2Z = 6 };
   struct SegDev {
     int kind;
     int off;       // output offset

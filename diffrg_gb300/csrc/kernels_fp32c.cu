@@ -2,7 +2,9 @@
 //
 // Structure shared by all kinds (persistent CTAs):
 //   * the CTA's dressing tables are staged into shared memory by non-tensor TMA bulk copies
-//     (cp.async.bulk + mbarrier complete_tx) and restaged only when an item uses others;
+//     (cp.async.bulk + mbarrier complete_tx) and restaged only when an item uses others (S2's
+//     accurate form reads its table through mode-interpolated slices formed by k_seg and
+//     stages only the cell-centre reciprocals);
 //   * work units (item, row range) come from an atomic counter; the node records of the unit's
 //     inner axes are TMA-prefetched into a second buffer while the current unit computes;
 //   * one thread per row loops over the inner axes on the FP32 pipe with double-float constants,
@@ -249,6 +251,13 @@ namespace gbint
       const float f = axis_frac_df(a, x.hi, x.lo, i);
       return lerp_df(T[i], T[i + 1], f);
     }
+    // z + f dz for a double-float pair (z, dz) packed as {z hi, z lo, dz hi, dz lo}
+    __device__ __forceinline__ df lerp_zd(float4 s, float f)
+    {
+      const df p = two_prod(f, s.z);
+      const df t = two_sum(s.x, p.hi);
+      return fast_two_sum(t.hi, __fadd_rn(t.lo, __fadd_rn(s.y, __fmaf_rn(f, s.w, p.lo))));
+    }
     // bilinear in a row-major [n0][n1] table: lerp along the point-varying axis first and along
     // the fixed one last, so that the rounding of the first lerps is not shared by many points
     // (varying = 0: axis 0 first)
@@ -270,12 +279,6 @@ namespace gbint
       const float *r1 = r0 + n1;
       return lerp_dd(lerp_df(r0[0], r1[0], fx), lerp_df(r0[1], r1[1], fx), fy);
     }
-    __device__ __forceinline__ df bil_df_v1(const float *d, int n1, int i, float fx, int j, float fy)
-    {
-      const float *r0 = d + i * n1 + j;
-      const float *r1 = r0 + n1;
-      return lerp_dd(lerp_df(r0[0], r0[1], fy), lerp_df(r1[0], r1[1], fy), fx);
-    }
 
     // Double-float running sum of double-float terms (accurate form).  A Kahan sum of the high
     // parts loses ~one FP32 rounding of every term (the compensated difference x - c is itself
@@ -295,6 +298,9 @@ namespace gbint
       __device__ __forceinline__ df sum() const { return fast_two_sum(hi, lo); }
       __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
     };
+
+    // bytes of a table's cell-centre reciprocals (staged at the end of its data; 16-byte multiple)
+    __device__ __forceinline__ int rc_bytes(const TableDev &T) { return T.rc_off ? T.bytes - 4 * T.rc_off : 0; }
 
     // ---------------------------------------------------------------- per-kind traits
     template <int KIND> struct Traits;
@@ -437,8 +443,8 @@ namespace gbint
         return (double)df_round(rec_w(cr)) * k.value();
       } else {
         // cell-centre reciprocals of the |q| axis (fed with |q+p|^2), when the table has them
-        const float2 *rcq =
-            (Z.rc_off && Z.rc_axis == 1 && Z.rc_sq) ? reinterpret_cast<const float2 *>(tab + Z.rc_off) : nullptr;
+        // (staged alone, at the start of this table's shared-memory block)
+        const float2 *rcq = (Z.rc_off && Z.rc_axis == 1 && Z.rc_sq) ? reinterpret_cast<const float2 *>(tab) : nullptr;
         const df x2 = df_max(lin_dd(A, B, cr.v_hi, cr.v_lo), 1e-30f);
         int jq;
         float fq;
@@ -451,50 +457,74 @@ namespace gbint
           fq = axis_frac_df(axq, x2.hi, x2.lo, jq);
         }
         const df R = reg_R_df(x2);
-        // The |q| lerps of the table's mode rows j0 and j0+1 at this row's fraction fq are kept
-        // from one mode to the next: consecutive modes mostly move to the next pair of rows, so
-        // one new |q| lerp per mode remains (the mode lerp with fraction fy0 follows).
-        const float *Tq = tab + jq;
-        int jc = -2;
-        df zlo{0.f, 0.f}, zhi{0.f, 0.f};
-        AccDF k;
-        // the mode record and hoisted factor of the next mode are loaded one iteration ahead
-        // (global/L1 latency would otherwise stall every mode)
-        float4 r0n = __ldg(aux + 1);
-        float2 fn = __ldg(F);
+        // The table interpolated along its mode axis at every (mode, sign) frequency of this
+        // item was formed per |q| cell in FP64 (segment SEG_S2Z): {z, dz} at [record * (n1 - 1)
+        // + cell], so a point lerps along |q| only.  Records are (mode m, sign) = 2 m, 2 m + 1.
+        const int ns = n1 - 1, zstep = 2 * ns;
+        const float4 *zp = reinterpret_cast<const float4 *>(P.seg + it.slice_off) + jq;  // record 2 m
+        const float2 *wp = reinterpret_cast<const float2 *>(aux + 1) + 1;  // its w^2 (record r at [2 r])
+        const float2 *fp = F;                                              // F_{m,i}, stride nq
+        const auto G = [&](const float4 &z, const float2 &w2) {
+          return df_rcp(df_add(df_mul(lerp_zd(z, fq), df_add(df{w2.x, w2.y}, x2)), R));
+        };
+        AccDF k1, k2;  // modes with one sign (below pm_from); modes with both signs
+        const int m1 = min(pmf, nm);
 #pragma unroll 1
-        for (int m = 0; m < nm; ++m) {
-          const float4 r0 = r0n;
-          const float2 f = fn;
-          if (m + 1 < nm) {
-            r0n = __ldg(aux + 1 + 2 * (m + 1));
-            fn = __ldg(F + (size_t)(m + 1) * nq);
-          }
-          const int j = __float_as_int(r0.x);
-          if (j != jc) {
-            if (j == jc + 1) {
-              zlo = zhi;
-            } else {
-              zlo = lerp_df(Tq[j * n1], Tq[j * n1 + 1], fq);
-            }
-            zhi = lerp_df(Tq[(j + 1) * n1], Tq[(j + 1) * n1 + 1], fq);
-            jc = j;
-          }
-          // first sign, then the second or the exact doubling of the first (twin)
-          df g = df_rcp(df_add(df_mul(lerp_dd(zlo, zhi, r0.y), df_add(df{r0.z, r0.w}, x2)), R));
-          if (m >= pmf) {
-            if (twin) {
-              g = df_scale2(g, 2.f);
-            } else {
-              const float4 r1 = aux[2 + 2 * m];
-              g = df_add(g, df_rcp(df_add(df_mul(bil_df_v1(tab, n1, __float_as_int(r1.x), r1.y, jq, fq),
-                                                 df_add(df{r1.z, r1.w}, x2)),
-                                          R)));
-            }
-          }
-          k.add(df_mul(df{f.x, f.y}, g));
+        for (int m = 0; m < m1; ++m) {
+          const float2 f = __ldg(fp);
+          k1.add(df_mul(df{f.x, f.y}, G(__ldg(zp), __ldg(wp))));
+          zp += zstep;
+          wp += 4;
+          fp += nq;
         }
-        const df row_sum = df_mul(rec_w(cr), k.sum());
+        if (m1 < nm) {
+          // the slice, w^2 and hoisted factor of the next mode are loaded one iteration ahead
+          // (L1/L2 latency would otherwise stall every mode); two modes per loop body interleave
+          // their independent double-float chains
+          float4 zn = __ldg(zp);
+          float2 wn = __ldg(wp), fn = __ldg(fp);
+          if (twin) {
+            // W = 0: the two signs read |w| and w^2 only and are bitwise equal, so each mode is
+            // evaluated once and the sum doubled (exact) at the end
+#pragma unroll 2
+            for (int m = m1; m < nm; ++m) {
+              const float4 z = zn;
+              const float2 w2 = wn, f = fn;
+              if (m + 1 < nm) {
+                zp += zstep;
+                wp += 4;
+                fp += nq;
+                zn = __ldg(zp);
+                wn = __ldg(wp);
+                fn = __ldg(fp);
+              }
+              k2.add(df_mul(df{f.x, f.y}, G(z, w2)));
+            }
+            k2.hi *= 2.f;
+            k2.lo *= 2.f;
+          } else {
+            float4 zn1 = __ldg(zp + ns);
+            float2 wn1 = __ldg(wp + 2);
+#pragma unroll 1
+            for (int m = m1; m < nm; ++m) {
+              const float4 z = zn, z1 = zn1;
+              const float2 w2 = wn, w21 = wn1, f = fn;
+              if (m + 1 < nm) {
+                zp += zstep;
+                wp += 4;
+                fp += nq;
+                zn = __ldg(zp);
+                zn1 = __ldg(zp + ns);
+                wn = __ldg(wp);
+                wn1 = __ldg(wp + 2);
+                fn = __ldg(fp);
+              }
+              k2.add(df_mul(df{f.x, f.y}, df_add(G(z, w2), G(z1, w21))));
+            }
+          }
+        }
+        const df ksum = df_add(k1.sum(), k2.sum());
+        const df row_sum = df_mul(rec_w(cr), ksum);
         return (double)row_sum.hi + (double)row_sum.lo;
       }
     }
@@ -665,6 +695,10 @@ namespace gbint
   {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr int NT = Traits<KIND>::kTables;
+    // S2, accurate form: the points read the mode-interpolated slices from the segment arena,
+    // so only the table's cell-centre reciprocals are staged (the rest of shared memory is
+    // left to L1, which holds the slices)
+    constexpr bool kRcOnly = KIND == K_S2 && ACC;
     float *tab_s = reinterpret_cast<float *>(smem);
     NodeRec *rec_s0 = reinterpret_cast<NodeRec *>(smem + tab_bytes_cap);
     NodeRec *rec_s1 = rec_s0 + rec_cap;
@@ -704,7 +738,7 @@ namespace gbint
             sT[t] = P.tabs[slot];
             s_slot[t] = slot;
             s_toff[t] = total / 4;
-            total += sT[t].bytes;
+            total += kRcOnly ? rc_bytes(sT[t]) : sT[t].bytes;
           }
           if (total > tab_bytes_cap) {
             atomicOr(P.err, ERR_BAD_INDEX);
@@ -712,7 +746,13 @@ namespace gbint
           }
           mbar_expect_tx(&bar[2], (uint32_t)total);
           if (total > 0)
-            for (int t = 0; t < NT; ++t) tma_bulk_g2s(tab_s + s_toff[t], sT[t].data, (uint32_t)sT[t].bytes, &bar[2]);
+            for (int t = 0; t < NT; ++t) {
+              if constexpr (kRcOnly) {
+                if (rc_bytes(sT[t]) > 0)
+                  tma_bulk_g2s(tab_s + s_toff[t], sT[t].data + sT[t].rc_off, (uint32_t)rc_bytes(sT[t]), &bar[2]);
+              } else
+                tma_bulk_g2s(tab_s + s_toff[t], sT[t].data, (uint32_t)sT[t].bytes, &bar[2]);
+            }
         }
         __syncthreads();
         ok = mbar_wait_bounded(&bar[2], ph_tab, P.err) && ok;

@@ -158,6 +158,20 @@ namespace gbint
       reinterpret_cast<float2 *>(out)[S.off + e] = make_float2(f.hi, f.lo);
       return;
     }
+    case SEG_S2Z: {
+      // record r = 2 m + sign at frequency +-w_m + W, |q| cell jq: the table lerped along its mode
+      // axis at columns jq and jq + 1, stored as {z, dz = z' - z} double-float pairs
+      const int r = e / S.n1, jq = e % S.n1;
+      const double w = pv[S.ax0.off + (r >> 1)];
+      const double ws = ((r & 1) ? -w : w) + S.par[0];
+      int j;
+      const double f = dev::axis_frac64(T.a0, fabs(ws) * S.par[1], j);
+      const float *d0 = T.data + (size_t)j * T.n1 + jq, *d1 = d0 + T.n1;
+      const double z0 = dev::lerp64(d0[0], d1[0], f), z1 = dev::lerp64(d0[1], d1[1], f);
+      const dev::df a = dev::df_from(z0), b = dev::df_from(z1 - z0);
+      reinterpret_cast<float4 *>(out + S.off)[e] = make_float4(a.hi, a.lo, b.hi, b.lo);
+      return;
+    }
     case SEG_S3: {
       const int i = S.ax0.off + e;
       const double q = pv[i], q2 = q * q;
