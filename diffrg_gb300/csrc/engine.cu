@@ -322,7 +322,7 @@ namespace
       AxisRef r{};
       rc = pool_append(ctx, h, r);
       if (rc) return rc;
-      it = ctx->axis_cache.emplace(key, AxisEntry{r, 0, std::move(h.v)}).first;
+      it = ctx->axis_cache.emplace(key, AxisEntry{r, 0, std::move(h.v), std::move(h.w)}).first;
     }
     ref = it->second.ref;
     ref.role = role;
@@ -704,6 +704,24 @@ namespace gbint
         auto key = std::make_tuple(kb, S.ax0.off, kb == K_S2 || kb == K_S5 ? S.ax1.off : -1, S.tab, par);
         auto f = seg_index.find(key);
         if (f == seg_index.end()) {
+          if (kb == K_S2) {
+            // q-only FP64 factors of the S2 segment, per q node: w_q Rdot(q^2), R(q^2), q^2 and
+            // the |q| fraction and cell on the table's second axis (6 doubles in 3 float4 slots)
+            const AxisEntry &qa = ctx->axis_cache.at(b->held[held0 + 1]);
+            if ((int)qa.v.size() != S.n1 || qa.w.size() != qa.v.size())
+              return set_error(ctx, GB_EINVAL, "S2 segment: unexpected q axis");
+            const TableDev &D = ctx->h_dir[S.tab];
+            S.aux_off = (int)b->aux.size();
+            for (int q = 0; q < S.n1; ++q) {
+              const double x2 = qa.v[q] * qa.v[q];
+              int jq = 0;
+              const double fq = dev::axis_frac64(D.a1, std::sqrt(x2), jq);
+              const double rec[6] = {qa.w[q] * dev::reg_Rdot(x2), dev::reg_R(x2), x2, fq, (double)jq, 0.0};
+              float4 f4[3];
+              std::memcpy(f4, rec, sizeof(rec));
+              b->aux.insert(b->aux.end(), f4, f4 + 3);
+            }
+          }
           S.off = (int)b->seg_total;
           b->seg_total += (size_t)S.n0 * S.n1;
           b->seg_max_entries = std::max(b->seg_max_entries, S.n0 * S.n1);
@@ -879,9 +897,12 @@ namespace gbint
     P.item_count = b->d_item_count;
     P.out = d_out ? d_out : b->d_out;
     P.err = ctx->d_err;
-    GB_CUDA(cudaMemsetAsync(b->d_counters, 0, b->runs.size() * sizeof(int), s));
+    // the segment kernel zeroes the run counters; without segments a memset does
     if (!b->segs.empty())
-      GB_CUDA(launch_seg(b->d_segs, (int)b->segs.size(), b->seg_max_entries, P.pv, P.pw, P.pa, P.tabs, b->d_seg, s));
+      GB_CUDA(launch_seg(b->d_segs, (int)b->segs.size(), b->seg_max_entries, P.pv, P.pw, P.aux, P.tabs, b->d_seg,
+                         b->d_counters, (int)b->runs.size(), s));
+    else
+      GB_CUDA(cudaMemsetAsync(b->d_counters, 0, b->runs.size() * sizeof(int), s));
     for (size_t r = 0; r < b->runs.size(); ++r) {
       const auto &run = b->runs[r];
       P.units = b->d_units + run.unit_begin;
@@ -1235,8 +1256,7 @@ static int table_update_impl(gb_ctx *ctx, gb_table *t, const float *src, cudaMem
   // publish the new buffer in the directory, ordered after the data on the same stream
   TableDev &D = ctx->h_dir[t->slot];
   D.data = t->buf[back];
-  GB_CUDA(cudaMemcpyAsync(ctx->d_dir + t->slot, &D, sizeof(TableDev), cudaMemcpyHostToDevice, s));
-  // the pageable host source (h_dir entry) is staged by the runtime before the call returns
+  GB_CUDA(launch_dir_set(ctx->d_dir + t->slot, D, s));
   GB_CUDA(cudaEventRecord(ctx->tables_event, s));
   t->front = back;
   t->epoch++;

@@ -65,6 +65,7 @@ namespace gbint
     AxisRef ref;
     int refs = 0;           // batches (and in-progress calls) holding the axis
     std::vector<double> v;  // host copy of the node values
+    std::vector<double> w;  // host copy of the weights
   };
 
   struct Ticket;

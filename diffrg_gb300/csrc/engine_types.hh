@@ -117,7 +117,7 @@ namespace gbint
     int n0, n1;    // entries = n0 * n1
     AxisRef ax0, ax1;
     int tab;       // table slot
-    int pad;
+    int aux_off;   // SEG_S2: per-q FP64 factors in RunParams::aux (3 float4 = 6 doubles per q node)
     double par[4];
   };
 } // namespace gbint

@@ -23,8 +23,12 @@ namespace gbint
   int kind_rows_per_unit(int kind, int threads_override);
 
   cudaError_t launch_generic(const RunParams &P, int ctas, cudaStream_t s);
+  // also zeroes the n_counters (<= 64) work counters of the batch's kind runs
   cudaError_t launch_seg(const SegDev *segs, int n_segs, int total_entries, const double *pv, const double *pw,
-                         const double *pa, const TableDev *tabs, double *seg_out, cudaStream_t s);
+                         const float4 *aux, const TableDev *tabs, double *seg_out, int *counters, int n_counters,
+                         cudaStream_t s);
+  // writes one table directory entry in stream order (the entry travels as a kernel parameter)
+  cudaError_t launch_dir_set(TableDev *dst, const TableDev &v, cudaStream_t s);
   // FP32-compensated persistent kernels (kinds K_S1..K_S5); threads in {128, 256, 512}
   cudaError_t launch_fp32c(int kind, const RunParams &P, int threads, int ctas, int tab_bytes_cap, int rec_cap,
                            cudaStream_t s);

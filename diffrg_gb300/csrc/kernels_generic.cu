@@ -134,8 +134,11 @@ namespace gbint
   // integrand that many points share, evaluated once per node in FP64.
   // ------------------------------------------------------------------------------------------
   __global__ void __launch_bounds__(256) k_seg(const SegDev *segs, const double *pv, const double *pw,
-                                               const TableDev *tabs, double *out)
+                                               const float4 *aux, const TableDev *tabs, double *out, int *counters,
+                                               int n_counters)
   {
+    // the work counters of the kernels that follow in stream order start from zero
+    if (blockIdx.x == 0 && blockIdx.y == 0 && (int)threadIdx.x < n_counters) counters[threadIdx.x] = 0;
     const SegDev S = segs[blockIdx.y];
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= S.n0 * S.n1) return;
@@ -149,10 +152,19 @@ namespace gbint
       break;
     }
     case SEG_S2: {
+      // F_{m,i} = w_m w_q Rdot(q^2) / (Z(|w_m| / 2 pi T, |q|) (w_m^2 + q^2) + R(q^2)); the q-only
+      // factors come from the host (FP64, per q node: w_q Rdot(q^2), R(q^2), q^2, |q| fraction
+      // and cell on the table), so an entry is one bilinear lookup and one division
       const int m = e / S.n1, i = e % S.n1;
-      const int nm = S.ax0.off + m, nq = S.ax1.off + i;
-      const double q = pv[nq], q2 = q * q;
-      F = pw[nm] * pw[nq] * reg_Rdot(q2) * ft_G64(T, pv[nm], q2, S.par[0]);
+      const double *Q = reinterpret_cast<const double *>(aux + S.aux_off) + 6 * i;
+      const double w = pv[S.ax0.off + m];
+      int jw;
+      const double fw = dev::axis_frac64(T.a0, fabs(w) / (2 * 3.14159265358979323846 * S.par[0]), jw);
+      const int jq = (int)Q[4], n1 = T.n1;
+      const float *d0 = T.data + (size_t)jw * n1 + jq, *d1 = d0 + n1;
+      const double lo = dev::lerp64(d0[0], d1[0], fw), hi = dev::lerp64(d0[1], d1[1], fw);
+      const double z = dev::lerp64(lo, hi, Q[3]);
+      F = pw[S.ax0.off + m] * Q[0] / (z * (w * w + Q[2]) + Q[1]);
       // the S2 kernel multiplies this factor per point: stored as a double-float pair
       const dev::df f = dev::df_from(F);
       reinterpret_cast<float2 *>(out)[S.off + e] = make_float2(f.hi, f.lo);
@@ -190,17 +202,26 @@ namespace gbint
   }
 
   cudaError_t launch_seg(const SegDev *segs, int n_segs, int max_entries, const double *pv, const double *pw,
-                         const double *pa, const TableDev *tabs, double *seg_out, cudaStream_t s)
+                         const float4 *aux, const TableDev *tabs, double *seg_out, int *counters, int n_counters,
+                         cudaStream_t s)
   {
-    (void)pa;
+    if (n_counters > 64) return cudaErrorInvalidValue;
     if (n_segs == 0) return cudaSuccess;
     // each entry is a chain of FP64 operations on the low-rate FP64 pipe: small CTAs spread the
     // entries over all SMs instead of queueing them on a few
     constexpr int kSegThreads = 64;
     dim3 grid((max_entries + kSegThreads - 1) / kSegThreads, n_segs);
-    k_seg<<<grid, kSegThreads, 0, s>>>(segs, pv, pw, tabs, seg_out);
+    k_seg<<<grid, kSegThreads, 0, s>>>(segs, pv, pw, aux, tabs, seg_out, counters, n_counters);
     return cudaGetLastError();
   }
+  __global__ void k_dir_set(TableDev *dst, const TableDev v) { *dst = v; }
+
+  cudaError_t launch_dir_set(TableDev *dst, const TableDev &v, cudaStream_t s)
+  {
+    k_dir_set<<<1, 1, 0, s>>>(dst, v);
+    return cudaGetLastError();
+  }
+
 
   // ------------------------------------------------------------------------------------------
   // Throughput probes: 8 independent dependency chains per thread.
