@@ -577,12 +577,38 @@ namespace gbint
       aux.push_back(df2(g.args[3], 0.0));                 // sin(theta)
       break;
     case K_S5:
+    case K_S5Z:
       aux.push_back(df2(p, p * p));                       // P, P^2
       aux.push_back(df2(g.args[2], g.args[3]));           // cos(alpha), sin(alpha)
       break;
     default:
       break;
     }
+  }
+
+  constexpr size_t kS5zSmemLimit = 200 * 1024;
+
+  // Shared memory of the S5Z kernel at rpu rows per unit: table A's cell-centre reciprocals and
+  // table B's slices at the c2 nodes (staged per item), then two per-unit buffers, each with the
+  // node records of c2 and phi and table A's slices at the unit's c1 nodes (rows are ordered
+  // (c1, q), so a unit spans at most (rpu - 1) / nq + 2 c1 nodes).
+  int s5z_tab_bytes(const gb_ctx *ctx, const ItemDev &it)
+  {
+    const TableDev &A = ctx->h_dir[it.tab[0]];
+    const int rcb = A.rc_off ? A.bytes - 4 * A.rc_off : 0;
+    return rcb + it.ax[2].n * (A.n0 - 1) * 16;
+  }
+  int s5z_rec_cap(const gb_ctx *ctx, const ItemDev &it, int rpu)
+  {
+    const int ns0 = ctx->h_dir[it.tab[0]].n0 - 1;
+    const int jspan = std::min(it.ax[1].n, (rpu - 1) / it.ax[0].n + 2);
+    return it.ax[2].n + it.ax[3].n + (jspan * ns0 + 1) / 2;  // NodeRec units (32 B = 2 slice entries)
+  }
+  size_t s5z_smem_bytes(const gb_ctx *ctx, const ItemDev &it, int rpu)
+  {
+    const size_t tab = ((size_t)s5z_tab_bytes(ctx, it) + 127) / 128 * 128;
+    const size_t rec = ((size_t)s5z_rec_cap(ctx, it, rpu) + 3) / 4 * 4;
+    return tab + 2 * rec * sizeof(NodeRec);
   }
 
   int plan_batch(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *const *item_tables,
@@ -596,6 +622,7 @@ namespace gbint
     b->items.resize(n);
     std::map<std::tuple<int, int, int, int, double>, int> seg_index;  // dedupe
     std::map<std::tuple<int, int, int, double, double>, int> slice_index;
+    std::map<std::tuple<int, int, int>, int> ax1_index;  // SEG_AX1 slices by (table, axis)
     std::vector<int> item_kind(n);
     for (int i = 0; i < n; ++i) {
       const gb_integral &g = items[i];
@@ -665,6 +692,10 @@ namespace gbint
         for (int t = 0; t < nt; ++t) tb += tables[t]->bytes;
         if (tb > 160 * 1024) kind = K_GENERIC;
       }
+      // 4D vertex, accurate form: the 2D tables read through slices along their cos axis when
+      // table B's slices at the c2 nodes and table A's at the c1 nodes of one work unit (double
+      // buffered) fit shared memory at the widest CTA
+      if (kind == (K_S5 | K_ACC) && s5z_smem_bytes(ctx, it, 512) <= kS5zSmemLimit) kind = K_S5Z | K_ACC;
       it.kind = kind;
       item_kind[i] = kind;
       long long rows;
@@ -673,7 +704,8 @@ namespace gbint
       case K_S1: rows = it.ax[0].n; break;
       case K_S2: rows = (long long)it.ax[1].n * it.ax[2].n; break;  // (q, cos); inner: modes
       case K_S3: rows = (long long)it.ax[0].n * it.ax[1].n; break;
-      case K_S5: rows = (long long)it.ax[0].n * it.ax[1].n; break;
+      case K_S5:
+      case K_S5Z: rows = (long long)it.ax[0].n * it.ax[1].n; break;  // S5Z: ordered (c1, q)
       default: {
         rows = 1;
         for (int a = 0; a < it.n_axes; ++a) rows *= it.ax[a].n;
@@ -684,7 +716,7 @@ namespace gbint
       // hoisted segment
       if (kind != K_GENERIC) {
         SegDev S{};
-        S.kind = kb;  // SEG_S* == K_S*
+        S.kind = kb == K_S5Z ? SEG_S5 : kb;  // SEG_S* == K_S*
         S.tab = it.tab[0];
         S.ax0 = it.ax[0];
         S.n0 = it.ax[0].n;
@@ -696,12 +728,12 @@ namespace gbint
           S.n1 = it.ax[1].n;
           par = g.args[2];
         }
-        if (kb == K_S5) {
+        if (kb == K_S5 || kb == K_S5Z) {
           S.ax1 = it.ax[1];
           S.n1 = it.ax[1].n;
         }
         S.par[0] = par;
-        auto key = std::make_tuple(kb, S.ax0.off, kb == K_S2 || kb == K_S5 ? S.ax1.off : -1, S.tab, par);
+        auto key = std::make_tuple(S.kind, S.ax0.off, S.kind == SEG_S2 || S.kind == SEG_S5 ? S.ax1.off : -1, S.tab, par);
         auto f = seg_index.find(key);
         if (f == seg_index.end()) {
           if (kb == K_S2) {
@@ -757,6 +789,32 @@ namespace gbint
         } else
           it.slice_off = f->second;
       }
+      // S5Z: tables A and B interpolated along their cos axis at the c1 and c2 nodes (shared by
+      // the items with the same table and axis)
+      if (kind == (K_S5Z | K_ACC)) {
+        const int ns0 = tables[0]->spec.n0 - 1;
+        auto ax1_slice = [&](int slot, const AxisRef &ax) -> int {
+          const auto key = std::make_tuple(slot, ax.off, ax.n);
+          auto f = ax1_index.find(key);
+          if (f != ax1_index.end()) return f->second;
+          SegDev S{};
+          S.kind = SEG_AX1;
+          S.tab = slot;
+          S.ax0 = ax;
+          S.n0 = ax.n;
+          S.n1 = ns0;
+          b->seg_total += b->seg_total & 1;  // float4 entries: 16-byte aligned
+          S.off = (int)b->seg_total;
+          b->seg_total += 2 * (size_t)S.n0 * S.n1;
+          b->seg_max_entries = std::max(b->seg_max_entries, S.n0 * S.n1);
+          b->segs.push_back(S);
+          ax1_index[key] = S.off;
+          return S.off;
+        };
+        it.slice_off = ax1_slice(it.tab[0], it.ax[1]);
+        it.slice_off2 = ax1_slice(it.tab[1], it.ax[2]);
+        it.slice_off3 = ax1_slice(it.tab[0], it.ax[2]);
+      }
       if (kind != K_GENERIC) item_aux(ctx, g, it, &ctx->axis_cache.at(b->held[held0]).v, b->aux);
       // reference-pattern geometry
       int loop_axis = -1;
@@ -769,7 +827,8 @@ namespace gbint
       b->plain_threads.push_back(pt);
     }
     // units grouped by kind
-    const int kinds[9] = {K_S1, K_S2, K_S3, K_S5, K_S1 | K_ACC, K_S2 | K_ACC, K_S3 | K_ACC, K_S5 | K_ACC, K_GENERIC};
+    const int kinds[10] = {K_S1,         K_S2,         K_S3,         K_S5,          K_S1 | K_ACC,
+                           K_S2 | K_ACC, K_S3 | K_ACC, K_S5 | K_ACC, K_S5Z | K_ACC, K_GENERIC};
     for (int kind : kinds) {
       gb_batch::KindRun run;
       run.kind = kind;
@@ -799,11 +858,13 @@ namespace gbint
             // S2 accurate form: only the cell-centre reciprocals are staged
             tb += kind == (K_S2 | K_ACC) ? (D.rc_off ? D.bytes - 4 * D.rc_off : 0) : ctx->slots[it.tab[t]]->bytes;
           }
+          if (kb == K_S5Z) tb = s5z_tab_bytes(ctx, it);
           tab_cap = std::max(tab_cap, tb);
           int rc_n = 0;
           if (kb == K_S1) rc_n = it.ax[1].n;
           if (kb == K_S2 || kb == K_S3) rc_n = it.ax[2].n;
           if (kb == K_S5) rc_n = it.ax[2].n + it.ax[3].n;
+          if (kb == K_S5Z) rc_n = s5z_rec_cap(ctx, it, rpu);
           rec_cap = std::max(rec_cap, rc_n);
         }
       }

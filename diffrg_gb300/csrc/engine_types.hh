@@ -39,6 +39,8 @@ namespace gbint
     K_S2 = 2,       // (mode, q, c) + FTLOOP, FP32c: rows (mode, q), inner c
     K_S3 = 3,       // (q, c, phi) + PROP3, FP32c: rows (q, c), inner phi
     K_S5 = 5,       // (q, c1, c2, phi) + VERT4, FP32c: rows (q, c1), mid c2, inner phi
+    K_S5Z = 6,      // K_S5, accurate form only, with the 2D tables read through slices along their
+                    // cos axis (rows ordered (c1, q); chosen when the slices fit shared memory)
     K_ACC = 16      // flag on K_S*: double-float evaluation of the per-point factors
   };
   constexpr int kind_base(int k) { return k & 15; }
@@ -57,7 +59,10 @@ namespace gbint
     int seg_stride;  // row stride inside the segment
     int tab[4];      // table directory slots
     int aux_off;     // per-item constants of the S kinds in RunParams::aux (float4 records)
-    int slice_off;   // S2 (accurate form): mode-interpolated table slices in the segment arena (doubles)
+    int slice_off;   // S2 (accurate form): mode-interpolated table slices in the segment arena (doubles);
+                     // S5Z: table A at the c1 nodes
+    int slice_off2;  // S5Z: table B at the c2 nodes
+    int slice_off3;  // S5Z: table A at the c2 nodes
     double k;
     double args[GB_MAX_ARGS];
   };
@@ -110,7 +115,9 @@ namespace gbint
   // hoisted-factor segment kinds
   // SEG_S2Z: the S2 dressing table interpolated along its mode axis at every (mode, sign)
   // frequency of an item, per |q| cell: float4 {z hi, lo, dz hi, lo} (two doubles per entry)
-  enum SegKind : int { SEG_S1 = 1, SEG_S2 = 2, SEG_S3 = 3, SEG_S5 = 5, SEG_S2Z = 6 };
+  // SEG_AX1: a 2D table interpolated along its second axis at the nodes of a quadrature axis,
+  // per first-axis cell: float4 {z hi, lo, dz hi, lo}
+  enum SegKind : int { SEG_S1 = 1, SEG_S2 = 2, SEG_S3 = 3, SEG_S5 = 5, SEG_S2Z = 6, SEG_AX1 = 7 };
   struct SegDev {
     int kind;
     int off;       // output offset

@@ -316,6 +316,9 @@ namespace gbint
     template <> struct Traits<K_S5> {
       static constexpr int kTables = 2;
     };
+    template <> struct Traits<K_S5Z> {
+      static constexpr int kTables = 2;
+    };
 
     // node records a unit needs (inner axes), staged back to back
     __device__ __forceinline__ int rec_axes(int kind, const ItemDev &it, int &a0, int &a1)
@@ -331,6 +334,7 @@ namespace gbint
         a1 = -1;
         return it.ax[2].n;
       case K_S5:
+      case K_S5Z:
         a0 = 2;
         a1 = 3;
         return it.ax[2].n + it.ax[3].n;
@@ -342,13 +346,24 @@ namespace gbint
     __device__ __forceinline__ void issue_records(int kind, const RunParams &P, int unit, NodeRec *dst,
                                                   uint64_t *bar)
     {
-      const ItemDev &it = P.items[P.units[unit].item];
+      const UnitDev U = P.units[unit];
+      const ItemDev &it = P.items[U.item];
       int a0, a1;
       const int n = rec_axes(kind, it, a0, a1);
-      mbar_expect_tx(bar, (uint32_t)(n * sizeof(NodeRec)));
+      // S5Z: table A's slices at the unit's c1 nodes follow the records (rows ordered (c1, q))
+      uint32_t zbytes = 0;
+      const float4 *zsrc = nullptr;
+      if (kind == K_S5Z) {
+        const int nq = it.ax[0].n, ns0 = P.tabs[it.tab[0]].n0 - 1;
+        const int j0 = U.row_begin / nq, j1 = (U.row_begin + U.row_count - 1) / nq;
+        zsrc = reinterpret_cast<const float4 *>(P.seg + it.slice_off) + (size_t)j0 * ns0;
+        zbytes = (uint32_t)((j1 - j0 + 1) * ns0 * sizeof(float4));
+      }
+      mbar_expect_tx(bar, (uint32_t)(n * sizeof(NodeRec)) + zbytes);
       tma_bulk_g2s(dst, P.prec + it.ax[a0].off, (uint32_t)(it.ax[a0].n * sizeof(NodeRec)), bar);
       if (a1 >= 0)
         tma_bulk_g2s(dst + it.ax[a0].n, P.prec + it.ax[a1].off, (uint32_t)(it.ax[a1].n * sizeof(NodeRec)), bar);
+      if (zbytes) tma_bulk_g2s(dst + n, zsrc, zbytes, bar);
     }
 
     __device__ __forceinline__ df rec_v(const NodeRec &r) { return df{r.v_hi, r.v_lo}; }
@@ -678,14 +693,79 @@ namespace gbint
       }
     }
 
+    // ---------------------------------------------------------------- S5Z: S5 through table slices
+    // The accurate S5 with tables A and B interpolated along their cos axis once per step (k_seg,
+    // SEG_AX1, FP64, {z, dz} double-float pairs per |q-p|^2 cell): A at the c1 nodes (this unit's
+    // rows, staged after the node records), B at the c2 nodes (staged per item after A's
+    // cell-centre reciprocals), A at the c2 nodes (global, once per (row, c2)).  A point then
+    // lerps along the |q-p|^2 axis only, twice, instead of two double-float bilinears.
+    // row = (c1 node j, q node i), q fastest, so a unit spans few c1 nodes.
+    __device__ __forceinline__ double row_s5z(const RunParams &P, const ItemDev &it, int row, int row0,
+                                              const NodeRec *rc, const float *tab, const TableDev *sT)
+    {
+      const int nq = it.ax[0].n, n1 = it.ax[1].n;
+      const int j = row / nq, i = row - j * nq;
+      const NodeRec qr = P.prec[it.ax[0].off + i];
+      const NodeRec cr = P.prec[it.ax[1].off + j];
+      const float4 *aux = P.aux + it.aux_off;  // (P, P^2), (cos a, sin a)
+      const float4 k0 = aux[0], k1 = aux[1];
+      const df qP = df_mul(rec_v(qr), df{k0.x, k0.y});
+      const df q2pp = df_add(rec_a(qr), df{k0.z, k0.w});
+      const df c1 = rec_v(cr);
+      const df qPc1 = df_mul(qP, c1);
+      const df r1d = df_max(df_add(q2pp, df_scale2(df_neg(qPc1), 2.f)), 1e-30f);  // |q-p1|^2
+      const df A2 = df_add(q2pp, df_scale2(df_mul(qPc1, df{k1.x, k1.y}), 2.f));
+      const df B2 = df_scale2(df_mul(qP, df_mul(rec_a(cr), df{k1.z, k1.w})), 2.f);
+      const TableDev &TA = sT[0];
+      const int ns0 = TA.n0 - 1;
+      // table A's cell-centre reciprocals (staged first) give the |q-p|^2 cell and fraction
+      const float2 *rca = (TA.rc_off && TA.rc_axis == 0) ? reinterpret_cast<const float2 *>(tab) : nullptr;
+      const int rcb = TA.rc_off ? TA.bytes - 4 * TA.rc_off : 0;
+      auto frac0 = [&](df x, int &ix) -> float {
+        return rca ? log_cell_frac(TA.a0, rca, x, ix) : axis_frac_df(TA.a0, x.hi, x.lo, ix);
+      };
+      const float4 *zb = reinterpret_cast<const float4 *>(tab + rcb / 4);  // B at c2 node l: [l * ns0]
+      const int n2 = it.ax[2].n, n3 = it.ax[3].n;
+      const float4 *za = reinterpret_cast<const float4 *>(rc + n2 + n3) + (j - row0 / nq) * ns0;  // A at c1 node j
+      const float4 *za2 = reinterpret_cast<const float4 *>(P.seg + it.slice_off3);  // A at c2 node l: [l * ns0]
+      const int nh3 = (n3 + 1) >> 1;
+      const NodeRec *rphi = rc + n2;
+      int ir1;
+      const float fr1 = frac0(r1d, ir1);
+      const df Rr1 = reg_R_df(r1d);
+      AccDF kmid;
+#pragma unroll 1
+      for (int l = 0; l < n2; ++l) {
+        const NodeRec r2r = rc[l];  // c2: v = c2, a = s2, w = 2 w_c2
+        const df gr1 = df_rcp(df_add(df_mul(lerp_zd(__ldg(za2 + (size_t)l * ns0 + ir1), fr1), r1d), Rr1));
+        const df Bs = df_mul(B2, rec_a(r2r));
+        const float4 *zbl = zb + l * ns0;
+        AccDF kin;
+#pragma unroll 1
+        for (int m = 0; m < nh3; ++m) {
+          const NodeRec rp = rphi[m];
+          const df x = df_max(lin_dd(A2, Bs, rp.a_hi, rp.a_lo), 1e-30f);
+          int ix;
+          const float fx = frac0(x, ix);
+          const df gv = df_rcp(df_add(df_mul(lerp_zd(za[ix], fx), x), reg_R_df(x)));
+          const df g = df_mul(gv, lerp_zd(zbl[ix], fx));
+          kin.add(df_mul(df_scale2(rec_w(rp), 2 * m + 1 == n3 ? 1.f : 2.f), g));
+        }
+        kmid.add(df_mul(rec_w(r2r), df_mul(kin.sum(), gr1)));
+      }
+      return P.seg[it.seg_off + i * n1 + j] * kmid.value();
+    }
+
     template <int KIND, bool ACC>
-    __device__ __forceinline__ double row_value(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
-                                                const float *tab, const TableDev *sT, const int *toff)
+    __device__ __forceinline__ double row_value(const RunParams &P, const ItemDev &it, int row, int row0,
+                                                const NodeRec *rc, const float *tab, const TableDev *sT,
+                                                const int *toff)
     {
       if constexpr (KIND == K_S1) return row_s1<ACC>(P, it, row, rc, tab + toff[0], sT);
       if constexpr (KIND == K_S2) return row_s2<ACC>(P, it, row, rc, tab + toff[0], sT);
       if constexpr (KIND == K_S3) return row_s3<ACC>(P, it, row, rc, tab, sT, toff);
       if constexpr (KIND == K_S5) return row_s5<ACC>(P, it, row, rc, tab, sT, toff);
+      if constexpr (KIND == K_S5Z) return row_s5z(P, it, row, row0, rc, tab, sT);
       return 0.0;
     }
   } // namespace
@@ -729,6 +809,7 @@ namespace gbint
       bool need = false;
 #pragma unroll
       for (int t = 0; t < NT; ++t) need |= (it.tab[t] != s_slot[t]);
+      if constexpr (KIND == K_S5Z) need |= (it.slice_off2 != s_slot[2]);
       if (need) {
         __syncthreads();  // everyone has read s_slot
         if (threadIdx.x == 0) {
@@ -738,21 +819,35 @@ namespace gbint
             sT[t] = P.tabs[slot];
             s_slot[t] = slot;
             s_toff[t] = total / 4;
-            total += kRcOnly ? rc_bytes(sT[t]) : sT[t].bytes;
+            if constexpr (KIND != K_S5Z) total += kRcOnly ? rc_bytes(sT[t]) : sT[t].bytes;
+          }
+          // S5Z: table A's cell-centre reciprocals, then table B's slices at the item's c2 nodes
+          int zb_bytes = 0;
+          if constexpr (KIND == K_S5Z) {
+            s_slot[2] = it.slice_off2;
+            zb_bytes = it.ax[2].n * (sT[0].n0 - 1) * (int)sizeof(float4);
+            total = rc_bytes(sT[0]) + zb_bytes;
           }
           if (total > tab_bytes_cap) {
             atomicOr(P.err, ERR_BAD_INDEX);
             total = 0;
           }
           mbar_expect_tx(&bar[2], (uint32_t)total);
-          if (total > 0)
-            for (int t = 0; t < NT; ++t) {
-              if constexpr (kRcOnly) {
-                if (rc_bytes(sT[t]) > 0)
-                  tma_bulk_g2s(tab_s + s_toff[t], sT[t].data + sT[t].rc_off, (uint32_t)rc_bytes(sT[t]), &bar[2]);
-              } else
-                tma_bulk_g2s(tab_s + s_toff[t], sT[t].data, (uint32_t)sT[t].bytes, &bar[2]);
+          if (total > 0) {
+            if constexpr (KIND == K_S5Z) {
+              if (rc_bytes(sT[0]) > 0)
+                tma_bulk_g2s(tab_s, sT[0].data + sT[0].rc_off, (uint32_t)rc_bytes(sT[0]), &bar[2]);
+              tma_bulk_g2s(tab_s + rc_bytes(sT[0]) / 4, P.seg + it.slice_off2, (uint32_t)zb_bytes, &bar[2]);
+            } else {
+              for (int t = 0; t < NT; ++t) {
+                if constexpr (kRcOnly) {
+                  if (rc_bytes(sT[t]) > 0)
+                    tma_bulk_g2s(tab_s + s_toff[t], sT[t].data + sT[t].rc_off, (uint32_t)rc_bytes(sT[t]), &bar[2]);
+                } else
+                  tma_bulk_g2s(tab_s + s_toff[t], sT[t].data, (uint32_t)sT[t].bytes, &bar[2]);
+              }
             }
+          }
         }
         __syncthreads();
         ok = mbar_wait_bounded(&bar[2], ph_tab, P.err) && ok;
@@ -773,7 +868,8 @@ namespace gbint
       }
       double acc = 0.0;
       if (ok && (int)threadIdx.x < U.row_count)
-        acc = row_value<KIND, ACC>(P, it, U.row_begin + threadIdx.x, buf ? rec_s1 : rec_s0, tab_s, sT, s_toff);
+        acc = row_value<KIND, ACC>(P, it, U.row_begin + threadIdx.x, U.row_begin, buf ? rec_s1 : rec_s0, tab_s, sT,
+                                   s_toff);
       const double tot = block_sum(acc, red);
       unit_finish(P, u, U.item, tot, red, &s_flag);
       buf ^= 1;
@@ -807,6 +903,8 @@ namespace gbint
         return acc ? sel_threads<K_S3, true>(threads) : sel_threads<K_S3, false>(threads);
       case K_S5:
         return acc ? sel_threads<K_S5, true>(threads) : sel_threads<K_S5, false>(threads);
+      case K_S5Z:
+        return acc ? sel_threads<K_S5Z, true>(threads) : nullptr;
       }
       return nullptr;
     }
@@ -818,6 +916,7 @@ namespace gbint
     case K_S1:
       return 128;
     case K_S5:
+    case K_S5Z:
       return 512;
     default:
       return 256;

@@ -170,6 +170,18 @@ namespace gbint
       reinterpret_cast<float2 *>(out)[S.off + e] = make_float2(f.hi, f.lo);
       return;
     }
+    case SEG_AX1: {
+      // node k of the axis, first-axis cell ix: the table lerped along its second axis at rows ix
+      // and ix + 1, stored as {z, dz = z' - z} double-float pairs
+      const int k = e / S.n1, ix = e % S.n1;
+      int jc;
+      const double fc = dev::axis_frac64(T.a1, pv[S.ax0.off + k], jc);
+      const float *d0 = T.data + (size_t)ix * T.n1 + jc, *d1 = d0 + T.n1;
+      const double z0 = dev::lerp64(d0[0], d0[1], fc), z1 = dev::lerp64(d1[0], d1[1], fc);
+      const dev::df a = dev::df_from(z0), b = dev::df_from(z1 - z0);
+      reinterpret_cast<float4 *>(out + S.off)[e] = make_float4(a.hi, a.lo, b.hi, b.lo);
+      return;
+    }
     case SEG_S2Z: {
       // record r = 2 m + sign at frequency +-w_m + W, |q| cell jq: the table lerped along its mode
       // axis at columns jq and jq + 1, stored as {z, dz = z' - z} double-float pairs

@@ -248,8 +248,10 @@ int gb_device_info(gb_ctx *ctx, int *device, int *num_sms);
  * file keyed by GPU model and SM count, and a cached kind is not timed again unless flags has
  * GB_TUNE_REFRESH.  chosen (may be NULL) receives the 16 per-kind widths (0 = default), indexed
  * by kind slot = GB_KIND_* (+ 8 for the double-float form used by GB_PREC_FP32C/FP32A).
+ * GB_KIND_S5Z is the 4D vertex kernel that reads its 2D tables through slices along their cos
+ * axis (double-float form only; used when the slices fit shared memory, else GB_KIND_S5).
  * gb_tune_set pins one slot by hand (0 = default width). */
-enum { GB_KIND_S1 = 1, GB_KIND_S2 = 2, GB_KIND_S3 = 3, GB_KIND_S5 = 5, GB_KIND_ACC = 8 };
+enum { GB_KIND_S1 = 1, GB_KIND_S2 = 2, GB_KIND_S3 = 3, GB_KIND_S5 = 5, GB_KIND_S5Z = 6, GB_KIND_ACC = 8 };
 #define GB_TUNE_REFRESH 1
 int gb_autotune(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
                 const char *cache_path, int flags, int *chosen);
