@@ -588,15 +588,14 @@ namespace gbint
 
   constexpr size_t kS5zSmemLimit = 200 * 1024;
 
-  // Shared memory of the S5Z kernel at rpu rows per unit: table A's cell-centre reciprocals and
-  // table B's slices at the c2 nodes (staged per item), then two per-unit buffers, each with the
-  // node records of c2 and phi and table A's slices at the unit's c1 nodes (rows are ordered
-  // (c1, q), so a unit spans at most (rpu - 1) / nq + 2 c1 nodes).
+  // Shared memory of the S5Z kernel at rpu rows per unit: table A's cell-centre reciprocals
+  // (staged per item), then two per-unit buffers, each with the node records of c2 and phi and
+  // table A's slices at the unit's c1 nodes (rows are ordered (c1, q), so a unit spans at most
+  // (rpu - 1) / nq + 2 c1 nodes).
   int s5z_tab_bytes(const gb_ctx *ctx, const ItemDev &it)
   {
     const TableDev &A = ctx->h_dir[it.tab[0]];
-    const int rcb = A.rc_off ? A.bytes - 4 * A.rc_off : 0;
-    return rcb + it.ax[2].n * (A.n0 - 1) * 16;
+    return A.rc_off ? A.bytes - 4 * A.rc_off : 0;
   }
   int s5z_rec_cap(const gb_ctx *ctx, const ItemDev &it, int rpu)
   {
@@ -693,8 +692,8 @@ namespace gbint
         if (tb > 160 * 1024) kind = K_GENERIC;
       }
       // 4D vertex, accurate form: the 2D tables read through slices along their cos axis when
-      // table B's slices at the c2 nodes and table A's at the c1 nodes of one work unit (double
-      // buffered) fit shared memory at the widest CTA
+      // table A's slices at the c1 nodes of one work unit (double buffered) fit shared memory at
+      // the widest CTA
       if (kind == (K_S5 | K_ACC) && s5z_smem_bytes(ctx, it, 512) <= kS5zSmemLimit) kind = K_S5Z | K_ACC;
       it.kind = kind;
       item_kind[i] = kind;

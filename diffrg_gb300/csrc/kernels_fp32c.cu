@@ -696,9 +696,10 @@ namespace gbint
     // ---------------------------------------------------------------- S5Z: S5 through table slices
     // The accurate S5 with tables A and B interpolated along their cos axis once per step (k_seg,
     // SEG_AX1, FP64, {z, dz} double-float pairs per |q-p|^2 cell): A at the c1 nodes (this unit's
-    // rows, staged after the node records), B at the c2 nodes (staged per item after A's
-    // cell-centre reciprocals), A at the c2 nodes (global, once per (row, c2)).  A point then
-    // lerps along the |q-p|^2 axis only, twice, instead of two double-float bilinears.
+    // rows, staged after the node records), B at the c2 nodes (read through L1: staging them
+    // too would hold a CTA's shared memory at ~180 KB and halve the resident warps, measured 13 %
+    // slower), A at the c2 nodes (through L1, once per (row, c2)).  A point then lerps along the
+    // |q-p|^2 axis only, twice, instead of two double-float bilinears.
     // row = (c1 node j, q node i), q fastest, so a unit spans few c1 nodes.
     __device__ __forceinline__ double row_s5z(const RunParams &P, const ItemDev &it, int row, int row0,
                                               const NodeRec *rc, const float *tab, const TableDev *sT)
@@ -720,11 +721,10 @@ namespace gbint
       const int ns0 = TA.n0 - 1;
       // table A's cell-centre reciprocals (staged first) give the |q-p|^2 cell and fraction
       const float2 *rca = (TA.rc_off && TA.rc_axis == 0) ? reinterpret_cast<const float2 *>(tab) : nullptr;
-      const int rcb = TA.rc_off ? TA.bytes - 4 * TA.rc_off : 0;
       auto frac0 = [&](df x, int &ix) -> float {
         return rca ? log_cell_frac(TA.a0, rca, x, ix) : axis_frac_df(TA.a0, x.hi, x.lo, ix);
       };
-      const float4 *zb = reinterpret_cast<const float4 *>(tab + rcb / 4);  // B at c2 node l: [l * ns0]
+      const float4 *zb = reinterpret_cast<const float4 *>(P.seg + it.slice_off2);  // B at c2 node l: [l * ns0]
       const int n2 = it.ax[2].n, n3 = it.ax[3].n;
       const float4 *za = reinterpret_cast<const float4 *>(rc + n2 + n3) + (j - row0 / nq) * ns0;  // A at c1 node j
       const float4 *za2 = reinterpret_cast<const float4 *>(P.seg + it.slice_off3);  // A at c2 node l: [l * ns0]
@@ -748,7 +748,7 @@ namespace gbint
           int ix;
           const float fx = frac0(x, ix);
           const df gv = df_rcp(df_add(df_mul(lerp_zd(za[ix], fx), x), reg_R_df(x)));
-          const df g = df_mul(gv, lerp_zd(zbl[ix], fx));
+          const df g = df_mul(gv, lerp_zd(__ldg(zbl + ix), fx));
           kin.add(df_mul(df_scale2(rec_w(rp), 2 * m + 1 == n3 ? 1.f : 2.f), g));
         }
         kmid.add(df_mul(rec_w(r2r), df_mul(kin.sum(), gr1)));
@@ -809,7 +809,6 @@ namespace gbint
       bool need = false;
 #pragma unroll
       for (int t = 0; t < NT; ++t) need |= (it.tab[t] != s_slot[t]);
-      if constexpr (KIND == K_S5Z) need |= (it.slice_off2 != s_slot[2]);
       if (need) {
         __syncthreads();  // everyone has read s_slot
         if (threadIdx.x == 0) {
@@ -821,13 +820,8 @@ namespace gbint
             s_toff[t] = total / 4;
             if constexpr (KIND != K_S5Z) total += kRcOnly ? rc_bytes(sT[t]) : sT[t].bytes;
           }
-          // S5Z: table A's cell-centre reciprocals, then table B's slices at the item's c2 nodes
-          int zb_bytes = 0;
-          if constexpr (KIND == K_S5Z) {
-            s_slot[2] = it.slice_off2;
-            zb_bytes = it.ax[2].n * (sT[0].n0 - 1) * (int)sizeof(float4);
-            total = rc_bytes(sT[0]) + zb_bytes;
-          }
+          // S5Z: table A's cell-centre reciprocals only (both tables share the |q-p|^2 fraction)
+          if constexpr (KIND == K_S5Z) total = rc_bytes(sT[0]);
           if (total > tab_bytes_cap) {
             atomicOr(P.err, ERR_BAD_INDEX);
             total = 0;
@@ -835,9 +829,7 @@ namespace gbint
           mbar_expect_tx(&bar[2], (uint32_t)total);
           if (total > 0) {
             if constexpr (KIND == K_S5Z) {
-              if (rc_bytes(sT[0]) > 0)
-                tma_bulk_g2s(tab_s, sT[0].data + sT[0].rc_off, (uint32_t)rc_bytes(sT[0]), &bar[2]);
-              tma_bulk_g2s(tab_s + rc_bytes(sT[0]) / 4, P.seg + it.slice_off2, (uint32_t)zb_bytes, &bar[2]);
+              tma_bulk_g2s(tab_s, sT[0].data + sT[0].rc_off, (uint32_t)total, &bar[2]);
             } else {
               for (int t = 0; t < NT; ++t) {
                 if constexpr (kRcOnly) {
