@@ -99,3 +99,51 @@ def test_empty_batch_is_an_argument_error(ctx):
     with pytest.raises(GbError) as e:
         ctx.batch([], (), "fp32c")
     assert e.value.code == 1
+
+
+def test_mixed_kinds_in_one_batch_are_bitwise_alone(ctx, W):
+    """C2 (finite-T loop, mode-interpolated slices) and C5 (4D vertex, cos-axis slices) items in
+    one batch, each reading its own tables through table_base: every result is bit-identical to
+    the same integral alone, and within 1e-9 of the oracle."""
+    from test_gpu_parity import subset
+
+    w2, w5 = subset(W, "C2"), subset(W, "C5")
+    i2, t2 = W.engine_items(w2)
+    i5, t5 = W.engine_items(w5)
+    for g in i5:
+        g.table_base = 1
+    T = [ctx.table(s, d) for s, d in t2 + t5]
+    items = [g for pair in zip(i2, i5) for g in pair] + i2[len(i5):]
+    b = ctx.batch(items, T, "fp32c")
+    mix = b.get()
+    b.close()
+    for k in (0, 1, 2, 3, 11):
+        b1 = ctx.batch([items[k]], T, "fp32c")
+        alone = b1.get()[0]
+        b1.close()
+        assert alone == mix[k]
+    got2 = np.concatenate([mix[0:2 * len(i5):2], mix[2 * len(i5):]])
+    got5 = mix[1:2 * len(i5):2]
+    assert rel(got2, W.oracle_values(w2, oracle_mod())).max() <= TOL32
+    assert rel(got5, W.oracle_values(w5, oracle_mod())).max() <= TOL32
+    for t in T:
+        t.close()
+
+
+def test_c5_small_q_order_falls_back_to_the_staged_table_kernel(ctx, oracle, W):
+    """With few q nodes a work unit spans many cos1 nodes and their slices do not fit shared
+    memory: the 4D vertex integrals then run on the kernel with the staged 2D tables, at the
+    same accuracy."""
+    w = W.c5()
+    w["P"], w["alpha"] = w["P"][[0, 40, 127]], w["alpha"][[0, 40, 127]]
+    w["n"] = (8, 64, 32, 16)
+    got = run(ctx, W, w, "fp32c")
+    ref = W.oracle_values(w, oracle)
+    assert rel(got, ref).max() <= TOL32
+
+
+def oracle_mod():
+    from oracle import oracle as O
+
+    O.build()
+    return O
