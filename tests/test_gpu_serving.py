@@ -327,3 +327,27 @@ def test_concurrent_host_threads(gblib, w):
         assert not errors, errors[:5]
     finally:
         c.close()
+
+
+def test_served_finite_t_and_vertex_requests(sctx):
+    """Requests of the finite-T loop (C2: mode-interpolated slices) and the 4D vertex (C5:
+    cos-axis slices) through the request loop, interleaved, in small requests: bit-identical to
+    one batch of the same integrals."""
+    from diffrg_gb300 import workloads as W
+    import test_gpu_parity as TP
+
+    w2, w5 = TP.subset(W, "C2"), TP.subset(W, "C5")
+    i2, t2 = W.engine_items(w2)
+    i5, t5 = W.engine_items(w5)
+    for g in i5:
+        g.table_base = 1
+    T = [sctx.table(s, d) for s, d in t2 + t5]
+    items = i2[:6] + i5 + i2[6:]
+    sizes = [3, 3, 2, 4, 5, 7, 6]
+    served = serve_all(sctx, items, T, sizes)
+    b = sctx.batch(items, T, "fp32c")
+    ref = b.get()
+    b.close()
+    for t in T:
+        t.close()
+    assert np.array_equal(served, ref)
