@@ -430,12 +430,17 @@ namespace gbint
       const bool twin = it.args[3] == 0.0;
       const float2 *F = reinterpret_cast<const float2 *>(P.seg + it.seg_off) + i;  // F_{m,i} at [m * nq]
       if constexpr (!ACC) {
-        AxisDev axq = Z.a1;  // |q| axis, fed with x2 = |q+p|^2 -> half the log2 scale
-        axq.scale.hi *= 0.5f;
-        axq.scale.lo *= 0.5f;
         const float x2 = fmaxf(lin_df(A, B, cr.v_hi, cr.v_lo), 1e-30f);
         int jq;
-        const float fq = axis_frac(axq, x2, jq);
+        float fq;
+        if (Z.a1.log) {
+          AxisDev axq = Z.a1;  // log |q| axis fed with x2 = |q+p|^2: half the log2 scale
+          axq.scale.hi *= 0.5f;
+          axq.scale.lo *= 0.5f;
+          fq = axis_frac(axq, x2, jq);
+        } else {
+          fq = axis_frac(Z.a1, __fsqrt_rn(x2), jq);  // linear |q| axis: the root itself
+        }
         const float R = reg_R(x2);
         Kahan k;
 #pragma unroll 1
@@ -465,11 +470,14 @@ namespace gbint
         float fq;
         if (rcq) {
           fq = log_cell_frac<true>(Z.a1, rcq, x2, jq);
-        } else {
-          AxisDev axq = Z.a1;
+        } else if (Z.a1.log) {
+          AxisDev axq = Z.a1;  // log |q| axis fed with x2 = |q+p|^2: half the log2 scale
           axq.scale.hi *= 0.5f;
           axq.scale.lo *= 0.5f;
           fq = axis_frac_df(axq, x2.hi, x2.lo, jq);
+        } else {
+          const df qa = df_sqrt(x2);  // linear |q| axis: the root itself
+          fq = axis_frac_df(Z.a1, qa.hi, qa.lo, jq);
         }
         const df R = reg_R_df(x2);
         // The table interpolated along its mode axis at every (mode, sign) frequency of this

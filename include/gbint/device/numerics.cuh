@@ -170,6 +170,15 @@ namespace gbint
       const df s = two_sum(y0, p.hi);
       return fast_two_sum(s.hi, __fadd_rn(s.lo, __fmaf_rn(f.hi, d.lo, __fmaf_rn(f.lo, d.hi, p.lo))));
     }
+    // sqrt of a double-float: the correctly rounded FP32 root plus one Newton correction,
+    // (x - s^2) / 2s with x - s^2 formed by fma (~2^-44 relative)
+    __device__ __forceinline__ df df_sqrt(df x)
+    {
+      if (!(x.hi > 0.f)) return df{0.f, 0.f};
+      const float s = __fsqrt_rn(x.hi);
+      const float e = __fadd_rn(__fmaf_rn(-s, s, x.hi), x.lo);
+      return fast_two_sum(s, __fdividef(e, __fadd_rn(s, s)));
+    }
     // a + f (b - a) for double-float a, b
     __device__ __forceinline__ df lerp_dd(df a, df b, float f)
     {

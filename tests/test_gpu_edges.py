@@ -147,3 +147,36 @@ def oracle_mod():
 
     O.build()
     return O
+
+
+@pytest.mark.parametrize("spec_q", [(48, 0, 0.0, 5.0), (24, 1, 1e-3, 20.0)], ids=["linear", "coarse-log"])
+def test_c2_tables_without_cell_reciprocals(ctx, oracle, W, spec_q):
+    """Finite-T loop on dressing tables whose |q| axis is linear, or logarithmic with cells
+    wider than the cell-centre reciprocals cover (54 %): the fraction comes from the
+    double-float index instead, at the same 1e-9 (and 2e-8 for the fast form).  A linear |q|
+    axis is fed the root of |q+p|^2, a log axis its square with half the scale."""
+    from diffrg_gb300.workloads import spec_2d, seeded_table
+
+    from test_gpu_parity import subset
+
+    w = subset(W, "C2")
+    n1, log1, lo1, hi1 = spec_q
+    Z = seeded_table((n1, 64), 77).T.copy()
+    w["tables"] = [(spec_2d(64, 0, 0.0, 64.0, n1, log1, lo1, hi1), Z)]
+    ref = W.oracle_values(w, oracle)
+    assert rel(run(ctx, W, w, "fp32c"), ref).max() <= TOL32
+    assert rel(run(ctx, W, w, "fp32f"), ref).max() <= 2e-8  # the fast form's tolerance
+
+
+def test_c5_tables_with_linear_momentum_axis(ctx, oracle, W):
+    """4D vertex on 2D tables whose momentum axis is linear (no cell-centre reciprocals)."""
+    from diffrg_gb300.workloads import spec_2d, seeded_table
+
+    w = W.c5()
+    w["P"], w["alpha"] = w["P"][[0, 63, 100]], w["alpha"][[0, 63, 100]]
+    sp = spec_2d(200, 0, 0.0, 40.0, 48, 0, -1.0, 1.0)
+    w["tables"] = [(sp, seeded_table((200, 48), 5, base=1.0, amp=0.5)),
+                   (sp, seeded_table((200, 48), 6, base=0.5, amp=1.0))]
+    got = run(ctx, W, w, "fp32c")
+    ref = W.oracle_values(w, oracle)
+    assert rel(got, ref).max() <= TOL32
