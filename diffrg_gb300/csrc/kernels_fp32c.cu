@@ -87,9 +87,13 @@ namespace gbint
       const float2 r = rc[j];
       df rr{r.x, r.y};
       if constexpr (SQ) rr = df_mul(rr, rr);
-      const df p = df_mul(x, rr);
-      const df t = two_sum(__fsub_rn(p.hi, 1.0f), p.lo);
-      const float th = t.hi;
+      // t = x rr - 1 = th + tl: th = fl(x.hi rr.hi) - 1 is exact (the product lies in [1/2, 2]),
+      // tl = the product's rounding error + the cross terms; ln(1 + th + tl) = ln(1 + th) +
+      // tl (1 - th) + O(tl^2, th^2 tl)
+      const float ph = __fmul_rn(x.hi, rr.hi);
+      const float th = __fsub_rn(ph, 1.0f);
+      const float tl0 = __fadd_rn(__fmaf_rn(x.hi, rr.hi, -ph), __fmaf_rn(x.hi, rr.lo, __fmul_rn(x.lo, rr.hi)));
+      const df t{th, __fmaf_rn(-th, tl0, tl0)};
       float Q = __fmaf_rn(th, 1.11111111e-01f, -1.25e-01f);  // 1/9, -1/8
       Q = __fmaf_rn(th, Q, 1.42857143e-01f);                  // 1/7
       Q = __fmaf_rn(th, Q, -1.66666667e-01f);                 // -1/6
