@@ -13,7 +13,7 @@
 // Two arithmetic variants per kind:
 //   fast (ACC = false): per-point factors in FP32 and a Kahan sum (~1e-8 of FP64);
 //   accurate (ACC = true, GB_PREC_FP32C): coordinate, table fraction and interpolation,
-//     regulator, reciprocal, weighted term and row sum in double-float (3e-12 .. 1.2e-10 of FP64
+//     regulator, reciprocal, weighted term and row sum in double-float (3e-12 .. 9e-11 of FP64
 //     on the benchmark workloads).
 // Tensor cores are not used: this is a reduction, not a dense contraction.
 #include "device_common.cuh"

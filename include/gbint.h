@@ -80,7 +80,7 @@ enum {
 enum {
   GB_PREC_FP32C = 0, /* FP32-compensated, the accurate form (double-float per-point factors
                         and sums on the FP32 pipe, FP64 cross-unit reduction): within 1e-9 of
-                        FP64 (measured 3e-12 .. 1.2e-10 on the benchmark workloads)          */
+                        FP64 (measured 3e-12 .. 9e-11 on the benchmark workloads)            */
   GB_PREC_FP64 = 1,  /* FP64 evaluation (generic fused kernel)                            */
   GB_PREC_FP32F = 2, /* FP32 per-point factors with Kahan sums: faster, ~1e-8 of FP64       */
   GB_PREC_FP32A = 3  /* the accurate form, as GB_PREC_FP32C                                 */
