@@ -128,6 +128,25 @@ namespace gbint
   {
     return a.v == b.v && a.d == b.d;
   }
+  // comparisons with plain numbers compare the value
+#define GBINT_DUAL_CMP(OP)                                                                                 \
+  template <typename T, typename S, std::enable_if_t<std::is_arithmetic_v<S>, int> = 0>                   \
+  __host__ __device__ bool operator OP(const dual<T> &a, S s)                                            \
+  {                                                                                                       \
+    return a.v OP T(s);                                                                                   \
+  }                                                                                                       \
+  template <typename T, typename S, std::enable_if_t<std::is_arithmetic_v<S>, int> = 0>                   \
+  __host__ __device__ bool operator OP(S s, const dual<T> &a)                                            \
+  {                                                                                                       \
+    return T(s) OP a.v;                                                                                   \
+  }
+  GBINT_DUAL_CMP(<)
+  GBINT_DUAL_CMP(>)
+  GBINT_DUAL_CMP(<=)
+  GBINT_DUAL_CMP(>=)
+#undef GBINT_DUAL_CMP
+  template <typename T> __host__ __device__ bool operator<=(const dual<T> &a, const dual<T> &b) { return a.v <= b.v; }
+  template <typename T> __host__ __device__ bool operator>=(const dual<T> &a, const dual<T> &b) { return a.v >= b.v; }
 
   // elementary functions: f(v), f'(v) d
   template <typename T> __host__ __device__ dual<T> exp(const dual<T> &a)

@@ -16,6 +16,7 @@
 #include "gbint/autodiff.hh"
 #include "gbint/integrators.hh"
 #include "gbint/interpolators.hh"
+#include "gbint/regulators.hh"
 
 using namespace DiFfRG;
 
@@ -294,6 +295,82 @@ int dual_cases()
   return 0;
 }
 
+// regulator shapes (gbint/regulators.hh): each function on the host and on the device, and the
+// derivatives once more by forward differentiation with gbint::dual (dq2RB: q^2 seeded;
+// RBdot = 2 k^2 dR/dk^2: k^2 seeded with derivative 2 k^2).  Prints
+// "REG <name> <k2> <q2> <fn> <host> <device> <dual>" (dual: nan where not applicable).
+constexpr int kRegFns = 6;  // RB, RBdot, dq2RB, RF, RFdot, dq2RF
+template <class R, bool DQ2> __host__ __device__ void reg_eval(double k2, double q2, double *o)
+{
+  o[0] = R::RB(k2, q2);
+  o[1] = R::RBdot(k2, q2);
+  o[3] = R::RF(k2, q2);
+  o[4] = R::RFdot(k2, q2);
+  if constexpr (DQ2) {
+    o[2] = R::dq2RB(k2, q2);
+    o[5] = R::dq2RF(k2, q2);
+  } else
+    o[2] = o[5] = NAN;
+}
+template <class R, bool DQ2> __global__ void reg_kernel(const double *kq, int n, double *out)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) reg_eval<R, DQ2>(kq[2 * t], kq[2 * t + 1], out + kRegFns * t);
+}
+struct Bos1 {
+  static constexpr double b = 1.;
+};
+struct Exp3 {
+  static constexpr double b = 3.;
+};
+struct Poly3 {
+  static constexpr int order = 3;
+};
+template <class R, bool DQ2> int reg_case(const char *name)
+{
+  std::vector<double> kq;
+  for (double k2 : {0.3, 1.0, 2.5})
+    for (double q2 : {1e-3, 0.2, 0.9, 1.7, 4.0}) kq.push_back(k2), kq.push_back(q2);
+  const int n = (int)kq.size() / 2;
+  double *dkq = nullptr, *dout = nullptr;
+  if (cudaMalloc(&dkq, kq.size() * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&dout, n * kRegFns * sizeof(double)) != cudaSuccess)
+    return 1;
+  cudaMemcpy(dkq, kq.data(), kq.size() * sizeof(double), cudaMemcpyHostToDevice);
+  reg_kernel<R, DQ2><<<1, 64>>>(dkq, n, dout);
+  std::vector<double> dev(n * kRegFns);
+  if (cudaMemcpy(dev.data(), dout, dev.size() * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
+  cudaFree(dkq);
+  cudaFree(dout);
+  for (int t = 0; t < n; ++t) {
+    const double k2 = kq[2 * t], q2 = kq[2 * t + 1];
+    double h[kRegFns];
+    reg_eval<R, DQ2>(k2, q2, h);
+    double ad[kRegFns];
+    for (double &v : ad) v = NAN;
+    ad[1] = gbint::derivative(R::RB(gbint::real(k2, 2 * k2), q2));
+    if constexpr (DQ2) ad[2] = gbint::derivative(R::RB(k2, gbint::seed(q2)));
+    ad[4] = gbint::derivative(R::RF(gbint::real(k2, 2 * k2), q2));
+    if constexpr (DQ2) ad[5] = gbint::derivative(R::RF(k2, gbint::seed(q2)));
+    for (int f = 0; f < kRegFns; ++f)
+      std::printf("REG %s %.17g %.17g %d %.17g %.17g %.17g\n", name, k2, q2, f, h[f], dev[t * kRegFns + f], ad[f]);
+  }
+  return 0;
+}
+int regulator_cases()
+{
+  int rc = 0;
+  rc |= reg_case<LitimRegulator<>, false>("litim");
+  rc |= reg_case<BosonicRegulator<>, true>("bosonic2");
+  rc |= reg_case<BosonicRegulator<Bos1>, true>("bosonic1");
+  rc |= reg_case<ExponentialRegulator<>, true>("exp2");
+  rc |= reg_case<ExponentialRegulator<Exp3>, true>("exp3");
+  rc |= reg_case<SmoothedLitimRegulator<>, false>("smoothlitim");
+  rc |= reg_case<PolynomialExpRegulator<>, true>("polyexp8");
+  rc |= reg_case<PolynomialExpRegulator<Poly3>, true>("polyexp3");
+  return rc;
+}
+
 // device evaluation of an interpolator at host-given points (checks the device branch)
 template <typename I> __global__ void eval_pts3(I f, const double *x, int n, double *out)
 {
@@ -400,6 +477,7 @@ int main(int argc, char **argv)
   if (argc > 1 && std::string(argv[1]) == "--interp3") return interp3_cases();
   if (argc > 1 && std::string(argv[1]) == "--complex") return complex_cases();
   if (argc > 1 && std::string(argv[1]) == "--dual") return dual_cases();
+  if (argc > 1 && std::string(argv[1]) == "--regulators") return regulator_cases();
   QuadratureProvider qp;
   std::string line;
   std::vector<Case> cases;

@@ -144,3 +144,65 @@ def test_dual_result_type(binary):
         assert abs(d - pd) <= tol * max(1, abs(pd)), (fam, d, pd)
         assert abs(pd) > 1e-6  # the derivative is not trivially zero (integrals here are ~1e-4..1e-2)
     assert fams == {"ANGLE", "ANGLEF", "CART1", "FTQ0"}
+
+
+def _reg_closed_forms(name, k2, q2):
+    """RB, RBdot, dq2RB, RF, RFdot, dq2RF of the regulator shapes, written out in numpy
+    (nan where the class does not define the function)."""
+    x = q2 / k2
+    nan = float("nan")
+    if name == "litim":
+        RB, RBdot, dRB = (k2 - q2) * (k2 > q2), 2 * k2 * (k2 > q2), nan
+    elif name.startswith("bosonic"):
+        b = float(name[-1])
+        y = x ** b
+        em = math.expm1(y)
+        RB = q2 * x ** (b - 1) / em
+        dRB = b * x ** (b - 1) * (em - y * math.exp(y)) / em ** 2
+        RBdot = 2 * k2 * y * (em * (1 - b) + b * y * math.exp(y)) / em ** 2
+    elif name.startswith("exp"):
+        b = float(name[-1])
+        y = x ** b
+        RB, dRB, RBdot = k2 * math.exp(-y), -b * x ** (b - 1) * math.exp(-y), 2 * k2 * math.exp(-y) * (1 + b * y)
+    elif name == "smoothlitim":
+        a = 2e-3
+        E = math.exp(min((x - 1) / a, 700.0))
+        RB = (k2 - q2) / (1 + E)
+        RBdot = 0.0 if E > 1e50 else 2 * k2 * (1 + E * (x - x * x + a) / a) / (1 + E) ** 2
+        dRB = nan
+    else:
+        n = int(name[len("polyexp"):])
+        f = sum(x ** m / m for m in range(1, n + 1))
+        fp = sum(x ** (m - 1) for m in range(1, n + 1))
+        RB, RBdot, dRB = k2 * math.exp(-f), 2 * k2 * math.exp(-f) * (1 + x * fp), -math.exp(-f) * fp
+    s = math.sqrt(RB + q2)
+    RF, RFdot = s - math.sqrt(q2), 0.5 * RBdot / s
+    dRF = (1 + dRB) / (2 * s) - 1 / (2 * math.sqrt(q2))
+    return [RB, RBdot, dRB, RF, RFdot, dRF]
+
+
+def test_regulators_host_device_and_derivatives(binary):
+    """gbint/regulators.hh (the reference's regulator classes, DiFfRG/include/DiFfRG/physics/
+    regulators.hh): every function on the host equals the device value and the numpy closed
+    form, and the analytic derivatives equal forward differentiation with gbint::dual
+    (dq2RB, dq2RF in q^2; RBdot, RFdot as 2 k^2 d/dk^2)."""
+    out = run(binary, [], extra=["--regulators"])
+    rows = [l.split()[1:] for l in out if l.startswith("REG")]
+    names = {r[0] for r in rows}
+    assert names == {"litim", "bosonic2", "bosonic1", "exp2", "exp3", "smoothlitim", "polyexp8", "polyexp3"}
+    checked_ad = 0
+    for name, k2, q2, fn, host, dev, ad in rows:
+        k2, q2, fn, host, dev, ad = float(k2), float(q2), int(fn), float(host), float(dev), float(ad)
+        want = _reg_closed_forms(name, k2, q2)[fn]
+        if math.isnan(want):
+            assert math.isnan(host) and math.isnan(dev)
+            continue
+        # relative 1e-9: the shape formulas cancel near q^2 -> 0 (e.g. the bosonic dq2RB,
+        # expm1(y) - y e^y ~ -y^2/2 at y = 1e-6 keeps ~9 digits); an absolute floor for values
+        # formed by cancellation of O(1) terms (dq2RF where R_B is negligible)
+        assert abs(host - want) <= 1e-9 * abs(want) + 1e-14, (name, k2, q2, fn, host, want)
+        assert abs(dev - host) <= 1e-13 * abs(host) + 1e-15, (name, k2, q2, fn, dev, host)
+        if not math.isnan(ad):
+            assert abs(ad - host) <= 1e-9 * abs(host) + 1e-13, (name, k2, q2, fn, ad, host)
+            checked_ad += 1
+    assert checked_ad > 100
