@@ -17,6 +17,7 @@
 #include "gbint/integrators.hh"
 #include "gbint/interpolators.hh"
 #include "gbint/regulators.hh"
+#include "gbint/flow_utils.hh"
 
 using namespace DiFfRG;
 
@@ -371,6 +372,68 @@ int regulator_cases()
   return rc;
 }
 
+// fan-out helpers (gbint/flow_utils.hh): request_data over a grid of external momenta (a
+// std::vector and a 2D coordinate pack), update_data, update_interpolator, get_data; every value
+// must equal the direct get() bit for bit.  Prints "FAN <what> <max abs diff> <n>".
+struct KExt1 {  // the K2 polynomial times (1 + p q^2): one external argument p per grid point
+  static __host__ __device__ double kernel(double q, double c, double k, double p, const Coeffs &C)
+  {
+    return K2<double>::kernel(q, c, k, C) * (1 + p * q * q);
+  }
+  static __host__ __device__ double constant(double, double p, const Coeffs &C) { return C.a[0] + p; }
+};
+struct KExt2 {  // two external arguments (p1, p2) from a 2D coordinate pack
+  static __host__ __device__ double kernel(double q, double c, double k, double p1, double p2, const Coeffs &C)
+  {
+    return K2<double>::kernel(q, c, k, C) * (1 + p1 * q * q + p2 * c);
+  }
+  static __host__ __device__ double constant(double, double, double, const Coeffs &C) { return C.a[0]; }
+};
+int fanout_cases()
+{
+  QuadratureProvider qp;
+  Coeffs A{};
+  A.a[0] = 0.25;
+  A.a[1] = 1.0;
+  A.a[3] = 0.5;
+  A.a[7] = 1.0;
+  A.a[8] = 0.3;
+  const double k = 0.8;
+  IntegratorAngleGPU<4, double, KExt1> I1(qp, {{32, 16}}, 1.5);
+  IntegratorAngleGPU<4, double, KExt2> I2(qp, {{32, 16}}, 1.5);
+  auto report = [](const char *what, const std::vector<double> &a, const std::vector<double> &b) {
+    double m = a.size() == b.size() ? 0.0 : 1e300;
+    for (size_t i = 0; i < a.size() && i < b.size(); ++i) m = std::max(m, std::fabs(a[i] - b[i]));
+    std::printf("FAN %s %.17g %zu\n", what, m, a.size());
+  };
+  // 1D grid (std::vector) and a 1D coordinates object
+  LogarithmicCoordinates1D<double> pc(24, 1e-3, 10.0, 0.0);
+  const auto grid = make_grid(pc);
+  std::vector<double> direct(grid.size()), viafut(grid.size()), viaget(grid.size()), viacoord(grid.size());
+  for (size_t i = 0; i < grid.size(); ++i) direct[i] = I1.get(k, grid[i], A);
+  update_data(request_data<double>(I1, grid, k, A), viafut.data());
+  report("request_data_vector", viafut, direct);
+  update_data(request_data<double>(I1, pc, k, std::make_tuple(A)), viacoord.data());
+  report("request_data_coordinates_tuple", viacoord, direct);
+  get_data<double>(viaget.data(), I1, grid, k, A);
+  report("get_data", viaget, direct);
+  // into an interpolator over the same coordinates
+  LinearInterpolator1D<double, LogarithmicCoordinates1D<double>> Zi(pc);
+  update_interpolator(request_data<double>(I1, grid, k, A), Zi);
+  std::vector<double> back(grid.size());
+  for (size_t i = 0; i < grid.size(); ++i) back[i] = Zi[i];
+  report("update_interpolator", back, direct);
+  // 2D coordinate pack
+  using LC = LinearCoordinates1D<double>;
+  CoordinatePackND<LC, LC> pack(LC(5, 0.0, 1.0), LC(4, -1.0, 1.0));
+  const auto g2 = make_grid(pack);
+  std::vector<double> d2(g2.size()), v2(g2.size());
+  for (size_t i = 0; i < g2.size(); ++i) d2[i] = I2.get(k, g2[i][0], g2[i][1], A);
+  update_data(request_data<double>(I2, pack, k, A), v2.data());
+  report("request_data_pack2d", v2, d2);
+  return 0;
+}
+
 // device evaluation of an interpolator at host-given points (checks the device branch)
 template <typename I> __global__ void eval_pts3(I f, const double *x, int n, double *out)
 {
@@ -478,6 +541,7 @@ int main(int argc, char **argv)
   if (argc > 1 && std::string(argv[1]) == "--complex") return complex_cases();
   if (argc > 1 && std::string(argv[1]) == "--dual") return dual_cases();
   if (argc > 1 && std::string(argv[1]) == "--regulators") return regulator_cases();
+  if (argc > 1 && std::string(argv[1]) == "--fanout") return fanout_cases();
   QuadratureProvider qp;
   std::string line;
   std::vector<Case> cases;
