@@ -26,6 +26,7 @@ def compile_program(src: str, out: str, extra=()) -> str:
               os.path.join(B.INCLUDE, "gbint", "interpolators.hh"), os.path.join(B.INCLUDE, "gbint", "autodiff.hh"),
               os.path.join(B.INCLUDE, "gbint", "regulators.hh"),
               os.path.join(B.INCLUDE, "gbint", "flow_utils.hh"),
+              os.path.join(B.INCLUDE, "gbint", "kernel_math.hh"),
               os.path.join(B.INCLUDE, "gbint", "device", "families.cuh")):
         h.update(open(p, "rb").read())
     h.update(open(lib, "rb").read()[:4096])

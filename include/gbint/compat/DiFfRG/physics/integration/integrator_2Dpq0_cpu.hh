@@ -1,0 +1,4 @@
+// Forwarding header at the path of DiFfRG/include/DiFfRG/physics/integration/integrator_2Dpq0_cpu.hh: the CPU (TBB)
+// class name is an alias of the GPU class in gbint/integrators.hh.
+#pragma once
+#include "gbint/integrators.hh"

@@ -793,4 +793,29 @@ namespace DiFfRG
   };
 
 #undef GBINT_JSON_CTOR
+
+  // The reference's CPU (TBB) integrators have the same constructors, get/request and set_T/set_E
+  // as its GPU ones (DiFfRG/include/DiFfRG/physics/integration/*_cpu.hh,
+  // .../integration_finiteT/*_cpu.hh); flows written against them run on the GPU classes here
+  // (their KERNELs are __host__ __device__ in the generated code).
+  template <int d, typename NT, typename KERNEL> using IntegratorTBB = IntegratorGPU<d, NT, KERNEL>;
+  template <int d, typename NT, typename KERNEL> using IntegratorAngleTBB = IntegratorAngleGPU<d, NT, KERNEL>;
+  template <typename NT, typename KERNEL> using Integrator3DTBB = Integrator3DGPU<NT, KERNEL>;
+  template <typename NT, typename KERNEL> using Integrator4D2AngTBB = Integrator4D2AngGPU<NT, KERNEL>;
+  template <typename NT, typename KERNEL> using Integrator4DTBB = Integrator4DGPU<NT, KERNEL>;
+  template <typename NT, typename KERNEL> using Integrator1DCartesianTBB = Integrator1DCartesianGPU<NT, KERNEL>;
+  template <typename NT, typename KERNEL> using Integrator2DCartesianTBB = Integrator2DCartesianGPU<NT, KERNEL>;
+  template <typename NT, typename KERNEL> using Integrator3DCartesianTBB = Integrator3DCartesianGPU<NT, KERNEL>;
+  template <typename NT, typename KERNEL> using Integrator2Dpq0TBB = Integrator2Dpq0GPU<NT, KERNEL>;
+  template <typename NT, typename KERNEL> using Integrator2Dpx0TBB = Integrator2Dpx0GPU<NT, KERNEL>;
+  template <typename NT, typename KERNEL> using Integrator3Dpq0TBB = Integrator3Dpq0GPU<NT, KERNEL>;
+  template <typename NT, typename KERNEL> using Integrator3Dpx0TBB = Integrator3Dpx0GPU<NT, KERNEL>;
+  template <int d, typename NT, typename KERNEL> using IntegratorFiniteTq0TBB = IntegratorFiniteTq0GPU<d, NT, KERNEL>;
+  template <int d, typename NT, typename KERNEL>
+  using IntegratorAngleFiniteTq0TBB = IntegratorAngleFiniteTq0GPU<d, NT, KERNEL>;
+  template <typename NT, typename KERNEL> using Integrator4DFiniteTq0TBB = Integrator4DFiniteTq0GPU<NT, KERNEL>;
+  template <int d, typename NT, typename KERNEL> using IntegratorFiniteTx0TBB = IntegratorFiniteTx0GPU<d, NT, KERNEL>;
+  template <int d, typename NT, typename KERNEL>
+  using IntegratorAngleFiniteTx0TBB = IntegratorAngleFiniteTx0GPU<d, NT, KERNEL>;
+  template <typename NT, typename KERNEL> using Integrator4DFiniteTx0TBB = Integrator4DFiniteTx0GPU<NT, KERNEL>;
 } // namespace DiFfRG

@@ -18,6 +18,7 @@
 #include "gbint/interpolators.hh"
 #include "gbint/regulators.hh"
 #include "gbint/flow_utils.hh"
+#include "gbint/kernel_math.hh"
 
 using namespace DiFfRG;
 
@@ -434,6 +435,52 @@ int fanout_cases()
   return 0;
 }
 
+// a KERNEL in the shape the reference's code generator writes (template on the regulator,
+// templated argument types, powr / complex / real, private RB.. forwarding to REG), used through
+// a CPU (TBB) class name, against the same integrand in plain real arithmetic on the GPU class:
+// Rdot(q^2) Re[(q^2 + R + m2 + (q0 + i mu)^2)^-2].  Prints "GEN <T> <generated> <plain>".
+template <typename REG> class GenKernel
+{
+public:
+  template <typename T1, typename T2>
+  static __forceinline__ __host__ __device__ auto kernel(const double q, const double q0, const double k, const T1 m2,
+                                                         const T2 mu)
+  {
+    const double R = RB(powr<2>(k), powr<2>(q));
+    const double Rd = RBdot(powr<2>(k), powr<2>(q));
+    return real(Rd * powr<-2>(complex<double>(powr<2>(q) + R + m2, 0.) + powr<2>(q0 + complex<double>(0., mu))));
+  }
+  template <typename T1, typename T2>
+  static __forceinline__ __host__ __device__ auto constant(const double k, const T1 m2, const T2 mu)
+  {
+    return 0.1 * m2 + 0. * k * mu;
+  }
+
+private:
+  static __forceinline__ __device__ __host__ auto RB(const double k2, const double p2) { return REG::RB(k2, p2); }
+  static __forceinline__ __device__ __host__ auto RBdot(const double k2, const double p2) { return REG::RBdot(k2, p2); }
+};
+struct PlainKernel {
+  static __host__ __device__ double kernel(double q, double q0, double k, double m2, double mu)
+  {
+    const double k2 = k * k, q2 = q * q;
+    const double R = BosonicRegulator<>::RB(k2, q2), Rd = BosonicRegulator<>::RBdot(k2, q2);
+    const double a = q2 + R + m2 + q0 * q0 - mu * mu, b = 2 * q0 * mu;
+    return Rd * (a * a - b * b) / ((a * a + b * b) * (a * a + b * b));
+  }
+  static __host__ __device__ double constant(double, double m2, double) { return 0.1 * m2; }
+};
+int generated_cases()
+{
+  QuadratureProvider qp;
+  for (double T : {0.15, 0.6}) {
+    IntegratorFiniteTq0TBB<4, double, GenKernel<BosonicRegulator<>>> G(qp, {{40}}, 2.5, T);
+    IntegratorFiniteTq0GPU<4, double, PlainKernel> P(qp, {{40}}, 2.5, T);
+    for (double mu : {0.0, 0.3}) std::printf("GEN %.3g %.17g %.17g\n", T, G.get(0.9, 0.4, mu), P.get(0.9, 0.4, mu));
+  }
+  return 0;
+}
+
 // device evaluation of an interpolator at host-given points (checks the device branch)
 template <typename I> __global__ void eval_pts3(I f, const double *x, int n, double *out)
 {
@@ -542,6 +589,7 @@ int main(int argc, char **argv)
   if (argc > 1 && std::string(argv[1]) == "--dual") return dual_cases();
   if (argc > 1 && std::string(argv[1]) == "--regulators") return regulator_cases();
   if (argc > 1 && std::string(argv[1]) == "--fanout") return fanout_cases();
+  if (argc > 1 && std::string(argv[1]) == "--generated") return generated_cases();
   QuadratureProvider qp;
   std::string line;
   std::vector<Case> cases;

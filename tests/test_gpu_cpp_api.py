@@ -219,3 +219,16 @@ def test_fanout_helpers_equal_direct_gets(binary):
                          "request_data_pack2d"}
     for what, (diff, n) in rows.items():
         assert n > 0 and diff == 0.0, (what, diff, n)
+
+
+def test_generated_style_kernel_through_cpu_class_name(binary):
+    """A KERNEL written the way the reference's code generator writes them (regulator template,
+    templated argument types, powr / complex / real from gbint/kernel_math.hh, private RB
+    forwarding), through the CPU class name IntegratorFiniteTq0TBB (an alias of the GPU class),
+    equals the same integrand in plain real arithmetic to rounding."""
+    out = run(binary, [], extra=["--generated"])
+    rows = [list(map(float, l.split()[1:])) for l in out if l.startswith("GEN")]
+    assert len(rows) == 4
+    for T, gen, plain in rows:
+        assert abs(gen - plain) <= 1e-13 * abs(plain), (T, gen, plain)
+        assert abs(plain) > 1e-6
