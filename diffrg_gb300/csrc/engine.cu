@@ -1220,6 +1220,44 @@ int gb_quad_config(gb_ctx *ctx, int min_size, int vacuum, int add)
 }
 
 // ------------------------------------------------------------------ tables
+namespace gbint
+{
+  // Taylor coefficients of R(x) = x / expm1(x) about the centres c_j of a log axis's cells, in
+  // t = x / c_j - 1: R(c (1 + t)) = sum_k a_k t^k, k <= 7, from the power-series quotient
+  // c (1 + t) / (expm1(c) + e^c sum_{k>=1} (c t)^k / k!) in long double (the divisor's higher
+  // terms are small against its constant, so the recurrence is stable for every c).  12 floats
+  // per cell: a0 and a1 as double-float pairs, a2..a7, two zeros.
+  std::vector<float> regulator_cell_coeffs(const dev::AxisDev &ax)
+  {
+    const int nc = ax.n - 1;
+    std::vector<float> out(12 * (size_t)nc, 0.f);
+    for (int j = 0; j < nc; ++j) {
+      const long double l2c = ((long double)j + 0.5L - (long double)ax.shift64) / (long double)ax.scale64;
+      const long double c = exp2l(l2c);
+      long double d[8], a[8];
+      d[0] = expm1l(c);
+      long double pw = 1.0L;
+      for (int k = 1; k < 8; ++k) {
+        pw *= c / k;
+        d[k] = expl(c) * pw;
+      }
+      for (int k = 0; k < 8; ++k) {
+        long double nk = k < 2 ? c : 0.0L;
+        for (int i = 0; i < k; ++i) nk -= a[i] * d[k - i];
+        a[k] = nk / d[0];
+      }
+      float *o = out.data() + 12 * (size_t)j;
+      for (int h = 0; h < 2; ++h) {
+        const dev::df v = dev::df_from((double)a[h]);
+        o[2 * h] = v.hi;
+        o[2 * h + 1] = v.lo;
+      }
+      for (int k = 2; k < 8; ++k) o[2 + k] = (float)a[k];
+    }
+    return out;
+  }
+} // namespace gbint
+
 int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
 {
   if (!ctx || !spec || !out) return set_error(ctx, GB_EINVAL, "bad table arguments");
@@ -1267,15 +1305,26 @@ int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
     }
   }
   t->bytes = data_bytes + (int)((rc.size() * 4 + 15) / 16 * 16);
+  // With the reciprocals, the Taylor coefficients of the regulator R(x) = x / expm1(x) about each
+  // cell centre in t = x / c_j - 1 (through t^7), behind them in global memory (not staged): a
+  // propagator 1 / (Z(x) x + R(x)) looked up at x gets R from the t of its table fraction.
+  // (cells at most 12 % wide, |t| <= 0.06: truncation < 1e-11 of the denominator)
+  const bool with_rq = rc_axis >= 0 && (rc_axis == 0 ? ax0 : ax1).scale64 >= kMinScaleSq;
+  const std::vector<float> rq = with_rq ? regulator_cell_coeffs(rc_axis == 0 ? ax0 : ax1) : std::vector<float>{};
+  const size_t alloc = (size_t)t->bytes + rq.size() * 4;
   GB_CUDA(cudaSetDevice(ctx->device));
-  GB_CUDA(cudaMalloc(&t->buf[0], t->bytes));
-  GB_CUDA(cudaMalloc(&t->buf[1], t->bytes));
-  GB_CUDA(cudaMemset(t->buf[0], 0, t->bytes));
-  GB_CUDA(cudaMemset(t->buf[1], 0, t->bytes));
-  if (!rc.empty())
-    for (int b = 0; b < 2; ++b)
+  GB_CUDA(cudaMalloc(&t->buf[0], alloc));
+  GB_CUDA(cudaMalloc(&t->buf[1], alloc));
+  GB_CUDA(cudaMemset(t->buf[0], 0, alloc));
+  GB_CUDA(cudaMemset(t->buf[1], 0, alloc));
+  for (int b = 0; b < 2; ++b) {
+    if (!rc.empty())
       GB_CUDA(cudaMemcpy(reinterpret_cast<char *>(t->buf[b]) + data_bytes, rc.data(), rc.size() * 4,
                          cudaMemcpyHostToDevice));
+    if (!rq.empty())
+      GB_CUDA(cudaMemcpy(reinterpret_cast<char *>(t->buf[b]) + t->bytes, rq.data(), rq.size() * 4,
+                         cudaMemcpyHostToDevice));
+  }
   TableDev &D = ctx->h_dir[slot];
   D = TableDev{};
   D.data = t->buf[0];
@@ -1283,6 +1332,7 @@ int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
   D.n1 = spec->n1;
   D.bytes = t->bytes;
   D.rc_off = rc.empty() ? 0 : data_bytes / 4;
+  D.rq_off = rq.empty() ? 0 : t->bytes / 4;
   D.rc_axis = std::max(rc_axis, 0);
   D.rc_sq = rc_axis >= 0 && (rc_axis == 0 ? ax0 : ax1).scale64 >= kMinScaleSq;
   D.a0 = ax0;

@@ -82,7 +82,7 @@ namespace gbint
     int rc_off;   // float offset of the (hi, lo) reciprocals of the cell centres of axis rc_axis; 0: none
     int rc_axis;  // the log axis they belong to (cells at most 25 % wide)
     int rc_sq;    // 1: cells at most 12 % wide, so the reciprocals also serve a squared coordinate
-    int pad;
+    int rq_off;   // float offset of the regulator's per-cell Taylor coefficients (global only); 0: none
     dev::AxisDev a0, a1;
   };
 

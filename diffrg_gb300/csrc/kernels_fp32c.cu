@@ -82,7 +82,7 @@ namespace gbint
     // through t^9/9, truncation < 3e-10 of a cell.
     // SQ: x is the square of the axis coordinate (1/c_j^2 formed from 1/c_j, half the scale)
     template <bool SQ = false>
-    __device__ __forceinline__ float cell_frac_at(const AxisDev &a, const float2 *rc, df x, int j)
+    __device__ __forceinline__ float cell_frac_at(const AxisDev &a, const float2 *rc, df x, int j, df *t_out = nullptr)
     {
       const float2 r = rc[j];
       df rr{r.x, r.y};
@@ -94,6 +94,7 @@ namespace gbint
       const float th = __fsub_rn(ph, 1.0f);
       const float tl0 = __fadd_rn(__fmaf_rn(x.hi, rr.hi, -ph), __fmaf_rn(x.hi, rr.lo, __fmul_rn(x.lo, rr.hi)));
       const df t{th, __fmaf_rn(-th, tl0, tl0)};
+      if (t_out) *t_out = df{th, tl0};  // x / c_j - 1 itself (the log's correction term aside)
       float Q = __fmaf_rn(th, 1.11111111e-01f, -1.25e-01f);  // 1/9, -1/8
       Q = __fmaf_rn(th, Q, 1.42857143e-01f);                  // 1/7
       Q = __fmaf_rn(th, Q, -1.66666667e-01f);                 // -1/6
@@ -128,10 +129,14 @@ namespace gbint
     }
     // cell i and fraction of x on a 1D log table with cell-centre reciprocals (clamped like
     // axis_frac_df): a fast log2 finds the cell to within one, the fraction decides the rest
+    // (jt, t): with jt non-null, the cell whose centre t = x / c_jt - 1 refers to (before the
+    // off-by-one correction), or -1 where x lies outside the table and was clamped
     template <bool SQ = false>
-    __device__ __forceinline__ float log_cell_frac(const AxisDev &a, const float2 *rc, df x, int &i)
+    __device__ __forceinline__ float log_cell_frac(const AxisDev &a, const float2 *rc, df x, int &i, int *jt = nullptr,
+                                                   df *t = nullptr)
     {
       const int n = a.n;
+      if (jt) *jt = -1;
       if (!(x.hi >= 1e-30f)) x = df{1e-30f, 0.f};  // also maps NaN
       if (!(x.hi <= 3e38f)) x = df{3e38f, 0.f};
       const float ua = __fmaf_rn(SQ ? 0.5f * a.scale.hi : a.scale.hi, __log2f(x.hi), a.shift.hi);
@@ -144,7 +149,8 @@ namespace gbint
         return 1.f;
       }
       int j = min(max((int)floorf(ua), 0), n - 2);
-      float f = cell_frac_at<SQ>(a, rc, x, j);
+      if (jt) *jt = j;
+      float f = cell_frac_at<SQ>(a, rc, x, j, t);
       if (f < 0.f) {
         if (j > 0) {
           j -= 1;
@@ -216,10 +222,39 @@ namespace gbint
       const df z = lerp_df(T[i], T[i + 1], f);
       return df_rcp(df_add(df_mul(z, x), reg_R_df(x)));
     }
+    // R(x) = x / expm1(x) from the Taylor coefficients about the centre of cell j of the table's
+    // log axis (3 float4 per cell: a0, a1 as double-float pairs, a2..a7), t = x / c_j - 1:
+    // ~30 instructions instead of the exp-based double-float form, no branch on x
+    __device__ __forceinline__ df reg_R_cell(const float4 *rq, int j, df t)
+    {
+      const float4 c0 = __ldg(rq + 3 * j), c1 = __ldg(rq + 3 * j + 1), c2 = __ldg(rq + 3 * j + 2);
+      const float th = t.hi;
+      float p = __fmaf_rn(th, c2.y, c2.x);
+      p = __fmaf_rn(th, p, c1.w);
+      p = __fmaf_rn(th, p, c1.z);
+      p = __fmaf_rn(th, p, c1.y);
+      p = __fmaf_rn(th, p, c1.x);                                // a2 + a3 t + ... + a7 t^5
+      const df q = fast_two_sum(c0.z, __fmaf_rn(th, p, c0.w));   // a1 + t (a2 + ...)
+      return df_add(df{c0.x, c0.y}, df_mul(t, q));               // a0 + t q
+    }
+    // R(x) through the table's cell expansion when x was located by its cell-centre reciprocals
+    // and lies inside the table, else the exp-based form
+    __device__ __forceinline__ df reg_R_tab(const TableDev &D, int jt, df t, df x)
+    {
+      if (D.rq_off && jt >= 0) return reg_R_cell(reinterpret_cast<const float4 *>(D.data + D.rq_off), jt, t);
+      return reg_R_df(x);
+    }
     __device__ __forceinline__ df G1_df(const float *T, const TableDev &D, df x)
     {
       int i;
-      const float f = frac1_df(T, D, x, i);
+      if (D.rc_off && D.rc_axis == 0) {
+        int jt;
+        df t;
+        const float f = log_cell_frac(D.a0, reinterpret_cast<const float2 *>(T + D.rc_off), x, i, &jt, &t);
+        const df z = lerp_df(T[i], T[i + 1], f);
+        return df_rcp(df_add(df_mul(z, x), reg_R_tab(D, jt, t, x)));
+      }
+      const float f = axis_frac_df(D.a0, x.hi, x.lo, i);
       const df z = lerp_df(T[i], T[i + 1], f);
       return df_rcp(df_add(df_mul(z, x), reg_R_df(x)));
     }
@@ -733,8 +768,10 @@ namespace gbint
       const int ns0 = TA.n0 - 1;
       // table A's cell-centre reciprocals (staged first) give the |q-p|^2 cell and fraction
       const float2 *rca = (TA.rc_off && TA.rc_axis == 0) ? reinterpret_cast<const float2 *>(tab) : nullptr;
-      auto frac0 = [&](df x, int &ix) -> float {
-        return rca ? log_cell_frac(TA.a0, rca, x, ix) : axis_frac_df(TA.a0, x.hi, x.lo, ix);
+      // the |q-p|^2 fraction, and with it the cell and t = x / c - 1 the regulator expansion uses
+      auto frac0 = [&](df x, int &ix, int &jt, df &t) -> float {
+        jt = -1;
+        return rca ? log_cell_frac(TA.a0, rca, x, ix, &jt, &t) : axis_frac_df(TA.a0, x.hi, x.lo, ix);
       };
       const float4 *zb = reinterpret_cast<const float4 *>(P.seg + it.slice_off2);  // B at c2 node l: [l * ns0]
       const int n2 = it.ax[2].n, n3 = it.ax[3].n;
@@ -742,9 +779,10 @@ namespace gbint
       const float4 *za2 = reinterpret_cast<const float4 *>(P.seg + it.slice_off3);  // A at c2 node l: [l * ns0]
       const int nh3 = (n3 + 1) >> 1;
       const NodeRec *rphi = rc + n2;
-      int ir1;
-      const float fr1 = frac0(r1d, ir1);
-      const df Rr1 = reg_R_df(r1d);
+      int ir1, jr1;
+      df tr1;
+      const float fr1 = frac0(r1d, ir1, jr1, tr1);
+      const df Rr1 = reg_R_tab(TA, jr1, tr1, r1d);
       AccDF kmid;
 #pragma unroll 1
       for (int l = 0; l < n2; ++l) {
@@ -757,9 +795,10 @@ namespace gbint
         for (int m = 0; m < nh3; ++m) {
           const NodeRec rp = rphi[m];
           const df x = df_max(lin_dd(A2, Bs, rp.a_hi, rp.a_lo), 1e-30f);
-          int ix;
-          const float fx = frac0(x, ix);
-          const df gv = df_rcp(df_add(df_mul(lerp_zd(za[ix], fx), x), reg_R_df(x)));
+          int ix, jx;
+          df tx;
+          const float fx = frac0(x, ix, jx, tx);
+          const df gv = df_rcp(df_add(df_mul(lerp_zd(za[ix], fx), x), reg_R_tab(TA, jx, tx, x)));
           const df g = df_mul(gv, lerp_zd(__ldg(zbl + ix), fx));
           kin.add(df_mul(df_scale2(rec_w(rp), 2 * m + 1 == n3 ? 1.f : 2.f), g));
         }
