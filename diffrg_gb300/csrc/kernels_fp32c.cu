@@ -109,11 +109,12 @@ namespace gbint
     }
     // the same fraction as a double-float (its FP32 rounding, ~3e-8 of a cell, is otherwise the
     // largest per-point error of a lookup; used where few points carry an integral)
-    __device__ __forceinline__ df cell_frac_at_df(const AxisDev &a, const float2 *rc, df x, int j)
+    __device__ __forceinline__ df cell_frac_at_df(const AxisDev &a, const float2 *rc, df x, int j, df *t_out = nullptr)
     {
       const float2 r = rc[j];
       const df p = df_mul(x, df{r.x, r.y});
       const df t = two_sum(__fsub_rn(p.hi, 1.0f), p.lo);
+      if (t_out) *t_out = t;
       const float th = t.hi;
       float Q = __fmaf_rn(th, 1.11111111e-01f, -1.25e-01f);
       Q = __fmaf_rn(th, Q, 1.42857143e-01f);
@@ -168,9 +169,11 @@ namespace gbint
       return fminf(fmaxf(f, 0.f), 1.f);
     }
     // cell and double-float fraction on a 1D log table with reciprocals (clamped)
-    __device__ __forceinline__ df log_cell_frac_df(const AxisDev &a, const float2 *rc, df x, int &i)
+    __device__ __forceinline__ df log_cell_frac_df(const AxisDev &a, const float2 *rc, df x, int &i, int *jt = nullptr,
+                                                   df *t = nullptr)
     {
       const int n = a.n;
+      if (jt) *jt = -1;
       if (!(x.hi >= 1e-30f)) x = df{1e-30f, 0.f};
       if (!(x.hi <= 3e38f)) x = df{3e38f, 0.f};
       const float ua = __fmaf_rn(a.scale.hi, __log2f(x.hi), a.shift.hi);
@@ -183,7 +186,8 @@ namespace gbint
         return df{1.f, 0.f};
       }
       int j = min(max((int)floorf(ua), 0), n - 2);
-      df f = cell_frac_at_df(a, rc, x, j);
+      if (jt) *jt = j;
+      df f = cell_frac_at_df(a, rc, x, j, t);
       if (f.hi < 0.f) {
         if (j > 0) {
           j -= 1;
@@ -239,10 +243,10 @@ namespace gbint
     }
     // R(x) through the table's cell expansion when x was located by its cell-centre reciprocals
     // and lies inside the table, else the exp-based form
-    __device__ __forceinline__ df reg_R_tab(const TableDev &D, int jt, df t, df x)
+    template <bool EXACT_LOW = false> __device__ __forceinline__ df reg_R_tab(const TableDev &D, int jt, df t, df x)
     {
       if (D.rq_off && jt >= 0) return reg_R_cell(reinterpret_cast<const float4 *>(D.data + D.rq_off), jt, t);
-      return reg_R_df(x);
+      return reg_R_df<EXACT_LOW>(x);
     }
     __device__ __forceinline__ df G1_df(const float *T, const TableDev &D, df x)
     {
@@ -262,14 +266,15 @@ namespace gbint
     __device__ __forceinline__ df G1_dff(const float *T, const TableDev &D, df x)
     {
       int i;
-      df z;
       if (D.rc_off && D.rc_axis == 0) {
-        const df f = log_cell_frac_df(D.a0, reinterpret_cast<const float2 *>(T + D.rc_off), x, i);
-        z = lerp_dff(T[i], T[i + 1], f);
-      } else {
-        const float f = axis_frac_df(D.a0, x.hi, x.lo, i);
-        z = lerp_df(T[i], T[i + 1], f);
+        int jt;
+        df t;
+        const df f = log_cell_frac_df(D.a0, reinterpret_cast<const float2 *>(T + D.rc_off), x, i, &jt, &t);
+        const df z = lerp_dff(T[i], T[i + 1], f);
+        return df_rcp(df_add(df_mul(z, x), reg_R_tab<true>(D, jt, t, x)));
       }
+      const float f = axis_frac_df(D.a0, x.hi, x.lo, i);
+      const df z = lerp_df(T[i], T[i + 1], f);
       return df_rcp(df_add(df_mul(z, x), reg_R_df<true>(x)));
     }
     __device__ __forceinline__ df V1_df(const float *T, const TableDev &D, df x)
