@@ -339,6 +339,16 @@ namespace gbint
         hi = e.hi;
         lo = __fadd_rn(lo, __fadd_rn(e.lo, t.lo));
       }
+      // add a * b: the product's high part joins the exact sum, its rounding error and cross terms
+      // go to the low word (the product is not renormalised first)
+      __device__ __forceinline__ void add_prod(df a, df b)
+      {
+        const df p = two_prod(a.hi, b.hi);
+        const float e = __fadd_rn(p.lo, __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi)));
+        const df s = two_sum(hi, p.hi);
+        hi = s.hi;
+        lo = __fadd_rn(lo, __fadd_rn(s.lo, e));
+      }
       __device__ __forceinline__ df sum() const { return fast_two_sum(hi, lo); }
       __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
     };
@@ -443,7 +453,7 @@ namespace gbint
         for (int l = 0; l < nc; ++l) {
           const NodeRec r = rc[l];
           const df x2 = df_max(lin_dd(A, B, r.v_hi, r.v_lo), 1e-30f);
-          k.add(df_mul(rec_aw(r), G1_dff(tab, sT[0], x2)));
+          k.add_prod(rec_aw(r), G1_dff(tab, sT[0], x2));
         }
         return P.seg[it.seg_off + row] * k.value();
       }
@@ -539,7 +549,7 @@ namespace gbint
 #pragma unroll 1
         for (int m = 0; m < m1; ++m) {
           const float2 f = __ldg(fp);
-          k1.add(df_mul(df{f.x, f.y}, G(__ldg(zp), __ldg(wp))));
+          k1.add_prod(df{f.x, f.y}, G(__ldg(zp), __ldg(wp)));
           zp += zstep;
           wp += 4;
           fp += nq;
@@ -565,7 +575,7 @@ namespace gbint
                 wn = __ldg(wp);
                 fn = __ldg(fp);
               }
-              k2.add(df_mul(df{f.x, f.y}, G(z, w2)));
+              k2.add_prod(df{f.x, f.y}, G(z, w2));
             }
             k2.hi *= 2.f;
             k2.lo *= 2.f;
@@ -586,7 +596,7 @@ namespace gbint
                 wn1 = __ldg(wp + 2);
                 fn = __ldg(fp);
               }
-              k2.add(df_mul(df{f.x, f.y}, df_add(G(z, w2), G(z1, w21))));
+              k2.add_prod(df{f.x, f.y}, df_add(G(z, w2), G(z1, w21)));
             }
           }
         }
@@ -649,7 +659,7 @@ namespace gbint
           const df t2 = df_max(lin_dd(Ap, Bh, r.a_hi, r.a_lo), 1e-30f);
           const df sv = df_add(sbd, df_mul(r2, third));
           const df g = df_mul(df_mul(G1_df(TB, sT[1], r2), V1_df(TC, sT[2], sv)), V1_df(TD, sT[3], t2));
-          k.add(df_mul(df_scale2(rec_w(r), 2 * l + 1 == nf ? 1.f : 2.f), g));
+          k.add_prod(df_scale2(rec_w(r), 2 * l + 1 == nf ? 1.f : 2.f), g);
         }
         inner = k.value();
       }
@@ -736,10 +746,10 @@ namespace gbint
             const float fx = frac1_df(DA, TA, x, ix);
             const df gv = df_rcp(df_add(df_mul(bil_df_v0(DA, tn1, ix, fx, jc1, fc1), x), reg_R_df(x)));
             const df g = df_mul(gv, bil_df_v0(DB, tn1, ix, fx, jc2, fc2));
-            kin.add(df_mul(df_scale2(rec_w(rp), 2 * m + 1 == n3 ? 1.f : 2.f), g));
+            kin.add_prod(df_scale2(rec_w(rp), 2 * m + 1 == n3 ? 1.f : 2.f), g);
           }
           const df si = kin.sum();
-          kmid.add(df_mul(rec_w(r2r), df_mul(si, gr1)));
+          kmid.add_prod(rec_w(r2r), df_mul(si, gr1));
         }
         return P.seg[it.seg_off + row] * kmid.value();
       }
@@ -805,9 +815,9 @@ namespace gbint
           const float fx = frac0(x, ix, jx, tx);
           const df gv = df_rcp(df_add(df_mul(lerp_zd(za[ix], fx), x), reg_R_tab(TA, jx, tx, x)));
           const df g = df_mul(gv, lerp_zd(__ldg(zbl + ix), fx));
-          kin.add(df_mul(df_scale2(rec_w(rp), 2 * m + 1 == n3 ? 1.f : 2.f), g));
+          kin.add_prod(df_scale2(rec_w(rp), 2 * m + 1 == n3 ? 1.f : 2.f), g);
         }
-        kmid.add(df_mul(rec_w(r2r), df_mul(kin.sum(), gr1)));
+        kmid.add_prod(rec_w(r2r), df_mul(kin.sum(), gr1));
       }
       return P.seg[it.seg_off + i * n1 + j] * kmid.value();
     }
