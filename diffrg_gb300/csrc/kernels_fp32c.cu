@@ -541,8 +541,19 @@ namespace gbint
         const float4 *zp = reinterpret_cast<const float4 *>(P.seg + it.slice_off) + jq;  // record 2 m
         const float2 *wp = reinterpret_cast<const float2 *>(aux + 1) + 1;  // its w^2 (record r at [2 r])
         const float2 *fp = F;                                              // F_{m,i}, stride nq
-        const auto G = [&](const float4 &z, const float2 &w2) {
-          return df_rcp(df_add(df_mul(lerp_zd(z, fq), df_add(df{w2.x, w2.y}, x2)), R));
+        // G = 1 / (z (w^2 + x2) + R) with the intermediate pairs left unnormalised (their low words
+        // stay a few ulp of the high ones; the products and the reciprocal's residual take both
+        // words, so only the renormalising additions are saved)
+        const auto G = [&](const float4 &zs, const float2 &w2) {
+          const df zp = two_prod(fq, zs.z);  // z = zs.x + fq dz: exact high sum, low word collected
+          const df zt = two_sum(zs.x, zp.hi);
+          const df z{zt.hi, __fadd_rn(zt.lo, __fadd_rn(zs.y, __fmaf_rn(fq, zs.w, zp.lo)))};
+          const df s0 = two_sum(w2.x, x2.hi);  // s = w^2 + x2
+          const float sl = __fadd_rn(s0.lo, __fadd_rn(w2.y, x2.lo));
+          const df p = two_prod(z.hi, s0.hi);  // D = z s + R
+          const float e = __fadd_rn(p.lo, __fmaf_rn(z.hi, sl, __fmul_rn(z.lo, s0.hi)));
+          const df d0 = two_sum(p.hi, R.hi);
+          return df_rcp(df{d0.hi, __fadd_rn(d0.lo, __fadd_rn(e, R.lo))});
         };
         AccDF k1, k2;  // modes with one sign (below pm_from); modes with both signs
         const int m1 = min(pmf, nm);
