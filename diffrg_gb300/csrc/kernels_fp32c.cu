@@ -226,6 +226,26 @@ namespace gbint
       const df z = lerp_df(T[i], T[i + 1], f);
       return df_rcp(df_add(df_mul(z, x), reg_R_df(x)));
     }
+    // 1 / (z x + R) for double-float z, x, R given as pairs whose low words may exceed half an ulp
+    // of the high ones: the product's high part and R's are summed exactly and the rest collects in
+    // the low word; the denominator is renormalised once before the reciprocal (one Newton step
+    // corrects a low word of a few ulp, not one of 1e-4 of the high word, which an unnormalised
+    // regulator can leave after its expansion cancels)
+    __device__ __forceinline__ df df_prop(df z, df x, df R)
+    {
+      const df p = two_prod(z.hi, x.hi);
+      const float e = __fadd_rn(p.lo, __fmaf_rn(z.hi, x.lo, __fmul_rn(z.lo, x.hi)));
+      const df d0 = two_sum(p.hi, R.hi);
+      return df_rcp(fast_two_sum(d0.hi, __fadd_rn(d0.lo, __fadd_rn(e, R.lo))));
+    }
+    // lerp_df / lerp_zd without the final renormalisation (for df_prop and products)
+    __device__ __forceinline__ df lerp_df_u(float y0, float y1, float f)
+    {
+      const df d = two_sum(y1, -y0);
+      const df p = two_prod(f, d.hi);
+      const df s = two_sum(y0, p.hi);
+      return df{s.hi, __fadd_rn(s.lo, __fmaf_rn(f, d.lo, p.lo))};
+    }
     // R(x) = x / expm1(x) from the Taylor coefficients about the centre of cell j of the table's
     // log axis (3 float4 per cell: a0, a1 as double-float pairs, a2..a7), t = x / c_j - 1:
     // ~30 instructions instead of the exp-based double-float form, no branch on x
@@ -238,8 +258,10 @@ namespace gbint
       p = __fmaf_rn(th, p, c1.z);
       p = __fmaf_rn(th, p, c1.y);
       p = __fmaf_rn(th, p, c1.x);                                // a2 + a3 t + ... + a7 t^5
-      const df q = fast_two_sum(c0.z, __fmaf_rn(th, p, c0.w));   // a1 + t (a2 + ...)
-      return df_add(df{c0.x, c0.y}, df_mul(t, q));               // a0 + t q
+      const df q{c0.z, __fmaf_rn(th, p, c0.w)};                  // a1 + t (a2 + ...), unnormalised
+      const df tq = two_prod(t.hi, q.hi);                        // a0 + t q, unnormalised
+      const df s = two_sum(c0.x, tq.hi);
+      return df{s.hi, __fadd_rn(s.lo, __fadd_rn(c0.y, __fadd_rn(tq.lo, __fmaf_rn(t.hi, q.lo, __fmul_rn(t.lo, q.hi)))))};
     }
     // R(x) through the table's cell expansion when x was located by its cell-centre reciprocals
     // and lies inside the table, else the exp-based form
@@ -255,8 +277,7 @@ namespace gbint
         int jt;
         df t;
         const float f = log_cell_frac(D.a0, reinterpret_cast<const float2 *>(T + D.rc_off), x, i, &jt, &t);
-        const df z = lerp_df(T[i], T[i + 1], f);
-        return df_rcp(df_add(df_mul(z, x), reg_R_tab(D, jt, t, x)));
+        return df_prop(lerp_df_u(T[i], T[i + 1], f), x, reg_R_tab(D, jt, t, x));
       }
       const float f = axis_frac_df(D.a0, x.hi, x.lo, i);
       const df z = lerp_df(T[i], T[i + 1], f);
@@ -270,8 +291,7 @@ namespace gbint
         int jt;
         df t;
         const df f = log_cell_frac_df(D.a0, reinterpret_cast<const float2 *>(T + D.rc_off), x, i, &jt, &t);
-        const df z = lerp_dff(T[i], T[i + 1], f);
-        return df_rcp(df_add(df_mul(z, x), reg_R_tab<true>(D, jt, t, x)));
+        return df_prop(lerp_dff(T[i], T[i + 1], f), x, reg_R_tab<true>(D, jt, t, x));
       }
       const float f = axis_frac_df(D.a0, x.hi, x.lo, i);
       const df z = lerp_df(T[i], T[i + 1], f);
@@ -824,7 +844,11 @@ namespace gbint
           int ix, jx;
           df tx;
           const float fx = frac0(x, ix, jx, tx);
-          const df gv = df_rcp(df_add(df_mul(lerp_zd(za[ix], fx), x), reg_R_tab(TA, jx, tx, x)));
+          const float4 zax = za[ix];
+          const df zp = two_prod(fx, zax.z);  // table A at (x, c1): zax.x + fx dz, unnormalised
+          const df zt = two_sum(zax.x, zp.hi);
+          const df gv = df_prop(df{zt.hi, __fadd_rn(zt.lo, __fadd_rn(zax.y, __fmaf_rn(fx, zax.w, zp.lo)))}, x,
+                                reg_R_tab(TA, jx, tx, x));
           const df g = df_mul(gv, lerp_zd(__ldg(zbl + ix), fx));
           kin.add_prod(df_scale2(rec_w(rp), 2 * m + 1 == n3 ? 1.f : 2.f), g);
         }
