@@ -238,7 +238,7 @@ namespace gbint
       const df d0 = two_sum(p.hi, R.hi);
       return df_rcp(fast_two_sum(d0.hi, __fadd_rn(d0.lo, __fadd_rn(e, R.lo))));
     }
-    // lerp_df / lerp_zd without the final renormalisation (for df_prop and products)
+    // lerp_df without the final renormalisation (its result feeds df_prop, which takes both words)
     __device__ __forceinline__ df lerp_df_u(float y0, float y1, float f)
     {
       const df d = two_sum(y1, -y0);
