@@ -303,6 +303,20 @@ namespace gbint
       const float f = frac1_df(T, D, x, i);
       return lerp_df(T[i], T[i + 1], f);
     }
+    // the same, unnormalised (for products)
+    __device__ __forceinline__ df V1_df_u(const float *T, const TableDev &D, df x)
+    {
+      int i;
+      const float f = frac1_df(T, D, x, i);
+      return lerp_df_u(T[i], T[i + 1], f);
+    }
+    // a * b for pairs whose low words may exceed half an ulp, result unnormalised (its consumer
+    // takes both words)
+    __device__ __forceinline__ df df_mul_u(df a, df b)
+    {
+      const df p = two_prod(a.hi, b.hi);
+      return df{p.hi, __fadd_rn(p.lo, __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi)))};
+    }
     __device__ __forceinline__ float V1_32(const float *T, const AxisDev &a, float x)
     {
       int i;
@@ -689,7 +703,7 @@ namespace gbint
           const df r2 = df_max(lin_dd(A, B, r.a_hi, r.a_lo), 1e-30f);
           const df t2 = df_max(lin_dd(Ap, Bh, r.a_hi, r.a_lo), 1e-30f);
           const df sv = df_add(sbd, df_mul(r2, third));
-          const df g = df_mul(df_mul(G1_df(TB, sT[1], r2), V1_df(TC, sT[2], sv)), V1_df(TD, sT[3], t2));
+          const df g = df_mul_u(df_mul_u(G1_df(TB, sT[1], r2), V1_df_u(TC, sT[2], sv)), V1_df_u(TD, sT[3], t2));
           k.add_prod(df_scale2(rec_w(r), 2 * l + 1 == nf ? 1.f : 2.f), g);
         }
         inner = k.value();
@@ -849,7 +863,10 @@ namespace gbint
           const df zt = two_sum(zax.x, zp.hi);
           const df gv = df_prop(df{zt.hi, __fadd_rn(zt.lo, __fadd_rn(zax.y, __fmaf_rn(fx, zax.w, zp.lo)))}, x,
                                 reg_R_tab(TA, jx, tx, x));
-          const df g = df_mul(gv, lerp_zd(__ldg(zbl + ix), fx));
+          const float4 zbx = __ldg(zbl + ix);
+          const df bp = two_prod(fx, zbx.z);  // table B at (x, c2), unnormalised
+          const df bt = two_sum(zbx.x, bp.hi);
+          const df g = df_mul_u(gv, df{bt.hi, __fadd_rn(bt.lo, __fadd_rn(zbx.y, __fmaf_rn(fx, zbx.w, bp.lo)))});
           kin.add_prod(df_scale2(rec_w(rp), 2 * m + 1 == n3 ? 1.f : 2.f), g);
         }
         kmid.add_prod(rec_w(r2r), df_mul(kin.sum(), gr1));
