@@ -51,11 +51,11 @@ PER_POINT = {"C1": (12, 4), "C2": (18, 4), "C3": (30, 6), "C5": (25, 4)}
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant kernel, from the
 # ncu captures summarised in profiles/ (k_fp32c_S2acc_C2_finiteT.md, k_fp32c_S3acc_C3_uneven3D.md,
 # k_fp32c_S5Z_C5_vertex4D.md)
-TRAFFIC_BYTES_PER_LAUNCH = {"C2": 1495808, "C3": 7070976, "C5": 733952}
+TRAFFIC_BYTES_PER_LAUNCH = {"C2": 1495808, "C3": 7070720, "C5": 733184}
 # thread instructions executed per integrand point by the dominant kernel (smsp__inst_executed.sum
 # x 32 / points, same captures): with the measured step time they give the issue rate, the
 # bound this double-float code actually meets (one warp instruction per SM sub-partition and cycle)
-INSTR_PER_POINT = {"C2": 44, "C3": 224, "C5": 116}
+INSTR_PER_POINT = {"C2": 44, "C3": 218, "C5": 113}
 
 
 def parse():
