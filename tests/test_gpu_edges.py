@@ -48,7 +48,7 @@ C3_ORDERS = [(256, 256, 256), (16, 16, 16), (16, 256, 17), (33, 16, 1), (16, 40,
              (64, 1, 64)]
 
 
-@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32c", TOL32)])
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32c", TOL32), ("fp32f", 2e-8)])
 def test_c3_extreme_and_ragged_orders(ctx, oracle, W, prec, tol):
     w = W.c3(8)
     w["orders"] = np.array(C3_ORDERS, dtype=np.int32)
@@ -64,7 +64,7 @@ def test_c3_extreme_and_ragged_orders(ctx, oracle, W, prec, tol):
     # held to 5e-9, the others to the 1e-9 target.
     few = np.prod(w["orders"].astype(np.int64), axis=1) < 1024
     assert err[~few].max() <= tol
-    assert err[few].max() <= (5e-9 if prec == "fp32c" else tol)
+    assert err[few].max() <= {"fp32c": 5e-9, "fp32f": 1e-6}.get(prec, tol)  # fast form: FP32 per point
 
 
 @pytest.mark.parametrize("prec,tol", [("fp64", TOL64), ("fp32c", TOL32)])
@@ -183,6 +183,6 @@ def test_c5_tables_with_linear_momentum_axis(ctx, oracle, W):
     sp = spec_2d(200, 0, 0.0, 40.0, 48, 0, -1.0, 1.0)
     w["tables"] = [(sp, seeded_table((200, 48), 5, base=1.0, amp=0.5)),
                    (sp, seeded_table((200, 48), 6, base=0.5, amp=1.0))]
-    got = run(ctx, W, w, "fp32c")
     ref = W.oracle_values(w, oracle)
-    assert rel(got, ref).max() <= TOL32
+    assert rel(run(ctx, W, w, "fp32c"), ref).max() <= TOL32
+    assert rel(run(ctx, W, w, "fp32f"), ref).max() <= 2e-8  # the fast form (staged-table kernel)
