@@ -20,6 +20,10 @@
 #include "integrands.cuh"
 #include "kernels.hh"
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 namespace gbint
 {
   using namespace dev;
@@ -1047,13 +1051,30 @@ namespace gbint
     return s;
   }
 
+  // the kernels' dynamic shared-memory limit is raised once per (kernel, device) to the largest
+  // size launched so far, instead of a driver call on every launch
+  static cudaError_t ensure_max_smem(const void *fn, size_t smem)
+  {
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, size_t> set;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    size_t &have = set[{fn, dev}];
+    if (smem <= have) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) have = smem;
+    return e;
+  }
+
   cudaError_t launch_fp32c(int kind, const RunParams &P, int threads, int ctas, int tab_bytes_cap, int rec_cap,
                            cudaStream_t s)
   {
     const void *fn = select(kind, threads);
     if (!fn) return cudaErrorInvalidValue;
     const size_t smem = (size_t)tab_bytes_cap + 2 * (size_t)rec_cap * sizeof(NodeRec);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = ensure_max_smem(fn, smem);
     if (e != cudaSuccess) return e;
     RunParams p = P;
     void *args[] = {(void *)&p, (void *)&tab_bytes_cap, (void *)&rec_cap};
@@ -1065,7 +1086,7 @@ namespace gbint
     const void *fn = select(kind, threads);
     if (!fn) return 0;
     const size_t smem = (size_t)tab_bytes_cap + 2 * (size_t)rec_cap * sizeof(NodeRec);
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+    if (ensure_max_smem(fn, smem) != cudaSuccess) return 0;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess) return 0;
     return nb;
