@@ -29,7 +29,8 @@ GB_MAX_ARGS = 24
 EXPORTS = [
     "gb_version", "gb_status_string", "gb_ctx_create", "gb_ctx_destroy", "gb_last_error",
     "gb_quad_gl", "gb_quad_matsubara", "gb_quad_config",
-    "gb_table_create", "gb_table_update", "gb_table_update_device", "gb_table_epoch", "gb_table_destroy",
+    "gb_table_create", "gb_table_update", "gb_table_update_device", "gb_table_update_many", "gb_table_epoch",
+    "gb_table_destroy",
     "gb_batch_create", "gb_batch_run", "gb_batch_run_graph", "gb_batch_results", "gb_batch_get",
     "gb_batch_run_plain", "gb_batch_info", "gb_batch_destroy", "gb_get", "gb_get_noalloc",
     "gb_serve_start", "gb_serve_stop", "gb_submit", "gb_poll", "gb_wait", "gb_cancel",
@@ -99,6 +100,7 @@ def load(path: str = LIB_PATH):
     L.gb_table_create.argtypes = [vp, C.POINTER(TableSpec), C.POINTER(vp)]
     L.gb_table_update.argtypes = [vp, vp, C.POINTER(C.c_float), vp]
     L.gb_table_update_device.argtypes = [vp, vp, vp, vp]
+    L.gb_table_update_many.argtypes = [vp, C.c_int, vp, vp, vp]
     L.gb_table_epoch.argtypes = [vp, vp, C.POINTER(C.c_uint64)]
     L.gb_table_destroy.argtypes = [vp, vp]
     L.gb_batch_create.argtypes = [vp, C.POINTER(Integral), C.c_int, C.POINTER(vp), C.c_int, C.c_int, C.POINTER(vp)]

@@ -1400,6 +1400,49 @@ int gb_table_update_device(gb_ctx *ctx, gb_table *t, const float *device_data, v
   return table_update_impl(ctx, t, device_data, cudaMemcpyDeviceToDevice, stream);
 }
 
+int gb_table_update_many(gb_ctx *ctx, int n, gb_table *const *tables, const float *const *host_data, void *stream)
+{
+  TraceRange tr("gbint table_update_many");
+  if (!ctx || n < 0 || (n > 0 && (!tables || !host_data))) return set_error(ctx, GB_EINVAL, "bad table update list");
+  if (n == 0) return GB_OK;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  GB_CUDA(cudaSetDevice(ctx->device));
+  {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone)
+      return set_error(ctx, GB_EINVAL, "table updates cannot be captured in a graph (update before gb_graph_launch)");
+  }
+  std::vector<int> slots(n);
+  for (int i = 0; i < n; ++i) {
+    if (!tables[i] || tables[i]->slot < 0 || !host_data[i]) return set_error(ctx, GB_EINVAL, "bad table update list");
+    slots[i] = tables[i]->slot;
+    for (int j = 0; j < i; ++j)
+      if (slots[j] == slots[i]) return set_error(ctx, GB_EINVAL, "a table appears twice in one update list");
+  }
+  // serving batches still reading the back buffers (an older epoch) finish first
+  if (ctx->serve) {
+    const int rc = serve_fence_tables(ctx, s);
+    if (rc) return rc;
+  }
+  std::vector<TableDev> dir(n);
+  for (int i = 0; i < n; ++i) {
+    gb_table *t = tables[i];
+    const int back = t->front ^ 1;
+    GB_CUDA(cudaMemcpyAsync(t->buf[back], host_data[i], (size_t)t->elems * 4, cudaMemcpyHostToDevice, s));
+    TableDev &D = ctx->h_dir[t->slot];
+    D.data = t->buf[back];
+    dir[i] = D;
+  }
+  GB_CUDA(launch_dir_set_many(ctx->d_dir, slots.data(), dir.data(), n, s));
+  GB_CUDA(cudaEventRecord(ctx->tables_event, s));
+  for (int i = 0; i < n; ++i) {
+    tables[i]->front ^= 1;
+    tables[i]->epoch++;
+  }
+  return GB_OK;
+}
+
 int gb_table_epoch(gb_ctx *ctx, gb_table *t, uint64_t *epoch)
 {
   if (!ctx || !t || !epoch) return GB_EINVAL;

@@ -29,6 +29,8 @@ namespace gbint
                          cudaStream_t s);
   // writes one table directory entry in stream order (the entry travels as a kernel parameter)
   cudaError_t launch_dir_set(TableDev *dst, const TableDev &v, cudaStream_t s);
+  // writes n directory entries dir[slot[i]] = v[i] in stream order (chunks travel as parameters)
+  cudaError_t launch_dir_set_many(TableDev *dir, const int *slot, const TableDev *v, int n, cudaStream_t s);
   // FP32-compensated persistent kernels (kinds K_S1..K_S5); threads in {128, 256, 512}
   cudaError_t launch_fp32c(int kind, const RunParams &P, int threads, int ctas, int tab_bytes_cap, int rec_cap,
                            cudaStream_t s);

@@ -234,6 +234,34 @@ namespace gbint
     return cudaGetLastError();
   }
 
+  constexpr int kDirChunk = 24;
+  struct DirChunk {
+    int n;
+    int slot[kDirChunk];
+    TableDev v[kDirChunk];
+  };
+  static_assert(sizeof(DirChunk) <= 4096, "directory chunk exceeds the kernel parameter limit");
+  __global__ void k_dir_set_many(TableDev *dir, const DirChunk c)
+  {
+    if ((int)threadIdx.x < c.n) dir[c.slot[threadIdx.x]] = c.v[threadIdx.x];
+  }
+
+  cudaError_t launch_dir_set_many(TableDev *dir, const int *slot, const TableDev *v, int n, cudaStream_t s)
+  {
+    for (int i = 0; i < n; i += kDirChunk) {
+      DirChunk c{};
+      c.n = n - i < kDirChunk ? n - i : kDirChunk;
+      for (int j = 0; j < c.n; ++j) {
+        c.slot[j] = slot[i + j];
+        c.v[j] = v[i + j];
+      }
+      k_dir_set_many<<<1, kDirChunk, 0, s>>>(dir, c);
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+
 
   // ------------------------------------------------------------------------------------------
   // Throughput probes: 8 independent dependency chains per thread.

@@ -247,14 +247,19 @@ class Context:
         return Table(self, spec, data)
 
     def update_tables(self, pairs, stream=None):
-        """Update several tables as one group: served requests see all of them or none."""
-        L = capi.lib()
-        self.check(L.gb_table_group_begin(self.h))
-        try:
-            for t, data in pairs:
-                t.update(data, stream)
-        finally:
-            self.check(L.gb_table_group_end(self.h))
+        """Update several tables as one group (gb_table_update_many): served requests see all of
+        them or none."""
+        pairs = list(pairs)
+        arrs = []
+        for t, data in pairs:
+            d = np.ascontiguousarray(data, dtype=np.float32)
+            if d.size != int(np.prod(t.shape)):
+                raise ValueError("table data has %d values, expected %s" % (d.size, t.shape))
+            arrs.append(d)
+        n = len(pairs)
+        handles = (C.c_void_p * n)(*[t.h for t, _ in pairs])
+        ptrs = (C.POINTER(C.c_float) * n)(*[d.ctypes.data_as(C.POINTER(C.c_float)) for d in arrs])
+        self.check(capi.lib().gb_table_update_many(self.h, n, handles, ptrs, C.c_void_p(stream) if stream else None))
 
     def batch(self, integrals, tables=(), precision="fp32c") -> Batch:
         return Batch(self, integrals, tables, precision)

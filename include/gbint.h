@@ -168,6 +168,10 @@ int gb_table_update_device(gb_ctx *ctx, gb_table *t, const float *device_data, v
  * served request sees all updates of the group or none of them.  Blocks nest. */
 int gb_table_group_begin(gb_ctx *ctx);
 int gb_table_group_end(gb_ctx *ctx);
+/* n tables from host data in one call, as one group: one serving fence, the n copies on
+ * `stream`, one directory write for all of them (instead of one per table).  Each table at most
+ * once in the list. */
+int gb_table_update_many(gb_ctx *ctx, int n, gb_table *const *tables, const float *const *host_data, void *stream);
 int gb_table_epoch(gb_ctx *ctx, gb_table *t, uint64_t *epoch);
 int gb_table_destroy(gb_ctx *ctx, gb_table *t);
 

@@ -186,3 +186,38 @@ def test_c5_tables_with_linear_momentum_axis(ctx, oracle, W):
     ref = W.oracle_values(w, oracle)
     assert rel(run(ctx, W, w, "fp32c"), ref).max() <= TOL32
     assert rel(run(ctx, W, w, "fp32f"), ref).max() <= 2e-8  # the fast form (staged-table kernel)
+
+
+def test_update_many_equals_single_updates(ctx, oracle, W):
+    """gb_table_update_many: the same results as one gb_table_update per table, every epoch
+    advanced once, and a table listed twice is an argument error."""
+    from diffrg_gb300 import GbError
+    from test_gpu_parity import subset
+
+    w = subset(W, "C3")
+    items, tabs = W.engine_items(w)
+    T = [ctx.table(s, d) for s, d in tabs]
+    rng = np.random.default_rng(11)
+    new = [d * (1 + 0.1 * rng.random(d.shape)).astype(np.float32) for _, d in tabs]
+    e0 = [t.epoch for t in T]
+    ctx.update_tables(zip(T, new))
+    assert [t.epoch for t in T] == [e + 1 for e in e0]
+    b = ctx.batch(items, T, "fp32c")
+    many = b.get()
+    b.close()
+    for t, d in zip(T, [d for _, d in tabs]):
+        t.update(d)
+    for t, d in zip(T, new):
+        t.update(d)
+    b = ctx.batch(items, T, "fp32c")
+    single = b.get()
+    b.close()
+    assert np.array_equal(many, single)
+    w2 = dict(w)
+    w2["tables"] = [(s, d) for (s, _), d in zip(tabs, new)]
+    assert rel(many, W.oracle_values(w2, oracle)).max() <= TOL32
+    with pytest.raises(GbError) as e:
+        ctx.update_tables([(T[0], new[0]), (T[0], new[0])])
+    assert e.value.code == 1
+    for t in T:
+        t.close()
