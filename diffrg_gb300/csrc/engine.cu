@@ -1363,13 +1363,15 @@ static int table_update_impl(gb_ctx *ctx, gb_table *t, const float *src, cudaMem
     if (rc) return rc;
   }
   GB_CUDA(cudaMemcpyAsync(t->buf[back], src, (size_t)t->elems * 4, kind, s));
-  // publish the new buffer in the directory, ordered after the data on the same stream
-  TableDev &D = ctx->h_dir[t->slot];
+  // publish the new buffer in the directory, ordered after the data on the same stream (the
+  // host copy of the entry changes only once the device write is enqueued)
+  TableDev D = ctx->h_dir[t->slot];
   D.data = t->buf[back];
   GB_CUDA(launch_dir_set(ctx->d_dir + t->slot, D, s));
-  GB_CUDA(cudaEventRecord(ctx->tables_event, s));
+  ctx->h_dir[t->slot] = D;
   t->front = back;
   t->epoch++;
+  GB_CUDA(cudaEventRecord(ctx->tables_event, s));
   return GB_OK;
 }
 
@@ -1430,16 +1432,16 @@ int gb_table_update_many(gb_ctx *ctx, int n, gb_table *const *tables, const floa
     gb_table *t = tables[i];
     const int back = t->front ^ 1;
     GB_CUDA(cudaMemcpyAsync(t->buf[back], host_data[i], (size_t)t->elems * 4, cudaMemcpyHostToDevice, s));
-    TableDev &D = ctx->h_dir[t->slot];
-    D.data = t->buf[back];
-    dir[i] = D;
+    dir[i] = ctx->h_dir[t->slot];
+    dir[i].data = t->buf[back];
   }
   GB_CUDA(launch_dir_set_many(ctx->d_dir, slots.data(), dir.data(), n, s));
-  GB_CUDA(cudaEventRecord(ctx->tables_event, s));
   for (int i = 0; i < n; ++i) {
+    ctx->h_dir[slots[i]] = dir[i];
     tables[i]->front ^= 1;
     tables[i]->epoch++;
   }
+  GB_CUDA(cudaEventRecord(ctx->tables_event, s));
   return GB_OK;
 }
 
