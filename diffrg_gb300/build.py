@@ -34,7 +34,7 @@ def nvcc() -> str:
 
 
 def _flags():
-    return ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
+    return ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-pthread", "-I", INCLUDE, "-I", CSRC,
             "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"] + ARCH
 
 
@@ -75,7 +75,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    cmd = [nv, "-shared"] + ARCH + ["-o", LIB] + objs + ["-lcudart"]
+    cmd = [nv, "-shared"] + ARCH + ["-o", LIB] + objs + ["-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stderr[-4000:])

@@ -11,24 +11,6 @@ namespace gbint
   {
     const long double kPiL = 3.141592653589793238462643383279502884L;
 
-    // P_n(z) and P_{n-1}(z) by the Bonnet recurrence
-    inline void legendre_pair(int n, long double z, long double &pn, long double &pn1)
-    {
-      long double p0 = 1, p1 = z;
-      if (n == 0) {
-        pn = 1;
-        pn1 = 0;
-        return;
-      }
-      for (int j = 2; j <= n; ++j) {
-        const long double p2 = ((2 * j - 1) * z * p1 - (j - 1) * p0) / j;
-        p0 = p1;
-        p1 = p2;
-      }
-      pn = p1;
-      pn1 = p0;
-    }
-
     // Solve (J - shift I) y = rhs in place for the symmetric tridiagonal J (diagonal a, squared
     // off-diagonals b) by Gaussian elimination with partial (row) pivoting.  Row interchanges
     // create one extra super-diagonal (u2).  Exactly singular pivots are replaced by a tiny value,
@@ -90,34 +72,6 @@ namespace gbint
       return cnt;
     }
   } // namespace
-
-  void gl_rule01(int n, std::vector<double> &x, std::vector<double> &w)
-  {
-    if (n <= 0) throw std::invalid_argument("Gauss-Legendre order must be positive");
-    x.assign(n, 0.0);
-    w.assign(n, 0.0);
-    const int half = (n + 1) / 2;
-    for (int i = 0; i < half; ++i) {
-      // i-th largest root; initial guess from the asymptotic formula
-      long double z = std::cos(kPiL * (4 * i + 3) / (4 * n + 2));
-      long double pn = 0, pn1 = 0;
-      for (int it = 0; it < 64; ++it) {
-        legendre_pair(n, z, pn, pn1);
-        const long double dp = n * (pn1 - z * pn) / (1 - z * z);
-        const long double step = pn / dp;
-        z -= step;
-        if (std::fabs(step) <= 4 * std::numeric_limits<long double>::epsilon()) break;
-      }
-      legendre_pair(n, z, pn, pn1);
-      const long double dp = n * (pn1 - z * pn) / (1 - z * z);
-      const long double wt = 1 / ((1 - z * z) * dp * dp);  // weight on [0,1] = half of [-1,1]'s
-      x[n - 1 - i] = (double)((1 + z) / 2);
-      x[i] = (double)((1 - z) / 2);
-      w[n - 1 - i] = (double)wt;
-      w[i] = (double)wt;
-    }
-    if (n % 2 == 1) x[n / 2] = 0.5;
-  }
 
   void jacobi_gauss(const std::vector<long double> &a, const std::vector<long double> &b, long double mu0,
                     std::vector<long double> &x, std::vector<long double> &w)

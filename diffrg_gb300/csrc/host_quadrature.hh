@@ -1,8 +1,8 @@
 // host_quadrature.hh -- quadrature rules of the engine (host, long double).
 //
-//   * Gauss-Legendre on [0,1]: the rule the reference takes from GSL's fixed Legendre type
-//     (DiFfRG/src/DiFfRG/common/quadrature/quadrature.cu:12-60).  Computed by Newton's method
-//     on P_n with the three-term recurrence, nodes ascending.
+//   * Gauss-Legendre on [0,1]: gl_rule01 of gbint/gl_rule.hh (header-only, shared with the host
+//     loop integrals), the rule the reference takes from GSL's fixed Legendre type
+//     (DiFfRG/src/DiFfRG/common/quadrature/quadrature.cu:12-60).
 //   * Gauss rules from a Jacobi matrix (DiFfRG/include/DiFfRG/common/quadrature/quadrature.hh:28-45):
 //     eigenvalues by Sturm-sequence bisection, weights from the Christoffel function
 //     w_i = mu0 / sum_k p_k(x_i)^2 of the orthonormal recurrence polynomials.
@@ -12,10 +12,10 @@
 
 #include <vector>
 
+#include "gbint/gl_rule.hh"
+
 namespace gbint
 {
-  void gl_rule01(int n, std::vector<double> &x, std::vector<double> &w);
-
   // a: diagonal (n), b: squared off-diagonals (b[i] couples i and i+1; n entries, last unused)
   void jacobi_gauss(const std::vector<long double> &a, const std::vector<long double> &b, long double mu0,
                     std::vector<long double> &x, std::vector<long double> &w);
