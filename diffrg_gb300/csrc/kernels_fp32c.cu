@@ -223,13 +223,6 @@ namespace gbint
       const float f = axis_frac(a, x, i);
       return rcp32(__fmaf_rn(lerp32(T[i], T[i + 1], f), x, reg_R(x)));
     }
-    __device__ __forceinline__ df G1_df(const float *T, const AxisDev &a, df x)
-    {
-      int i;
-      const float f = axis_frac_df(a, x.hi, x.lo, i);
-      const df z = lerp_df(T[i], T[i + 1], f);
-      return df_rcp(df_add(df_mul(z, x), reg_R_df(x)));
-    }
     // 1 / (z x + R) for double-float z, x, R given as pairs whose low words may exceed half an ulp
     // of the high ones: the product's high part and R's are summed exactly and the rest collects in
     // the low word; the denominator is renormalised once before the reciprocal (one Newton step
@@ -301,13 +294,7 @@ namespace gbint
       const df z = lerp_df(T[i], T[i + 1], f);
       return df_rcp(df_add(df_mul(z, x), reg_R_df<true>(x)));
     }
-    __device__ __forceinline__ df V1_df(const float *T, const TableDev &D, df x)
-    {
-      int i;
-      const float f = frac1_df(T, D, x, i);
-      return lerp_df(T[i], T[i + 1], f);
-    }
-    // the same, unnormalised (for products)
+    // a 1D table lookup at a double-float argument, unnormalised (its consumers are products)
     __device__ __forceinline__ df V1_df_u(const float *T, const TableDev &D, df x)
     {
       int i;
@@ -326,12 +313,6 @@ namespace gbint
       int i;
       const float f = axis_frac(a, x, i);
       return lerp32(T[i], T[i + 1], f);
-    }
-    __device__ __forceinline__ df V1_df(const float *T, const AxisDev &a, df x)
-    {
-      int i;
-      const float f = axis_frac_df(a, x.hi, x.lo, i);
-      return lerp_df(T[i], T[i + 1], f);
     }
     // z + f dz for a double-float pair (z, dz) packed as {z hi, z lo, dz hi, dz lo}
     __device__ __forceinline__ df lerp_zd(float4 s, float f)
@@ -362,7 +343,7 @@ namespace gbint
       return lerp_dd(lerp_df(r0[0], r1[0], fx), lerp_df(r0[1], r1[1], fx), fy);
     }
 
-    // Double-float running sum of double-float terms (accurate form).  A Kahan sum of the high
+    // Double-float running sum of double-float products (accurate form).  A Kahan sum of the high
     // parts loses ~one FP32 rounding of every term (the compensated difference x - c is itself
     // rounded): ~6e-8 per term, ~1e-8 per row and ~3e-10 on a 2048-point integral, measured; the
     // double-float sum keeps ~2^-44 per term.
@@ -371,12 +352,6 @@ namespace gbint
     // sum, so its own rounding is ~2^-48 per term).
     struct AccDF {
       float hi = 0.f, lo = 0.f;
-      __device__ __forceinline__ void add(df t)
-      {
-        const df e = two_sum(hi, t.hi);
-        hi = e.hi;
-        lo = __fadd_rn(lo, __fadd_rn(e.lo, t.lo));
-      }
       // add a * b: the product's high part joins the exact sum, its rounding error and cross terms
       // go to the low word (the product is not renormalised first)
       __device__ __forceinline__ void add_prod(df a, df b)
