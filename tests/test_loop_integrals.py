@@ -325,3 +325,67 @@ def test_finite_T_extent_fits_match_the_restated_fits(driver, x0s, q0s):
 def test_marked_result_types_take_the_jacobian_rules(driver):
     a, b = (float(t) for t in run(driver, ["jac 16 8 2 1e-3 rational 0.8"])[0].split())
     assert a == b
+
+
+def test_dealii_rule_is_taken_when_dealii_is_included_first(tmp_path):
+    """With deal.II's quadrature_lib.h included first, DiFfRG::QGauss is deal.II's rule: a
+    stand-in with deal.II's interface (Point<1> points, include guard dealii_quadrature_lib_h)
+    goes through LoopIntegrals and FlowEquations unchanged."""
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    src = tmp_path / "dealii_rule.cc"
+    src.write_text(r'''
+#include <cmath>
+#include <cstdio>
+#include <map>
+#include <string>
+#include <vector>
+#include "gbint/gl_rule.hh"
+#define dealii_quadrature_lib_h
+namespace dealii {
+  template <int dim> struct Point { double c[dim]; double operator[](unsigned i) const { return c[i]; } };
+  template <int dim> class QGauss {
+  public:
+    explicit QGauss(unsigned n) : tag(7) {
+      std::vector<double> x; gbint::gl_rule01((int)n, x, w);
+      for (double v : x) p.push_back(Point<1>{{v}});
+    }
+    const std::vector<Point<1>> &get_points() const { return p; }
+    const std::vector<double> &get_weights() const { return w; }
+    unsigned size() const { return (unsigned)w.size(); }
+    int tag;
+  private:
+    std::vector<Point<1>> p; std::vector<double> w;
+  };
+}
+#include <DiFfRG/physics/flow_equations.hh>
+struct Json {
+  std::map<std::string, double> v;
+  unsigned get_uint(const std::string &k) const { return (unsigned)v.at(k); }
+  double get_double(const std::string &k) const { return v.at(k); }
+  int get_int(const std::string &k) const { return (int)v.at(k); }
+};
+struct Flow : DiFfRG::FlowEquations {
+  Flow(const Json &j) : FlowEquations(j, [](double q2) { return std::exp(-q2); }) {}
+  int tag() const { return x_quadrature.tag; }
+};
+int main() {
+  static_assert(std::is_same_v<DiFfRG::QGauss<1>, dealii::QGauss<1>>, "deal.II's rule");
+  Json j;
+  j.v = {{"/integration/x_quadrature_order", 16}, {"/integration/angle_quadrature_order", 8},
+         {"/integration/jacobian_quadrature_factor", 2}, {"/integration/x_extent_tolerance", 1e-3},
+         {"/output/verbosity", 0}};
+  Flow f(j);
+  const double v = f.angle_integrate<double, 4>([](double q2, double c) { return (1 + q2) * (1 + c * c); });
+  std::printf("%d %.17g\n", f.tag(), v);
+  return f.tag() == 7 && std::isfinite(v) ? 0 : 1;
+}
+''')
+    exe = str(tmp_path / "dealii_rule")
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-pthread", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        "-I", os.path.join(ROOT, "include", "gbint", "compat"), str(src), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
