@@ -24,7 +24,7 @@
 //
 // One deliberate difference: two_angle_integrate weights its phi nodes with the phi rule's
 // weights.  The reference multiplies the phi term by the weight of the current cos node
-// (loop_integrals.hh:182-183), which turns the phi quadrature into a plain sum of the nodes' values
+// (loop_integrals.hh:180-181), which turns the phi quadrature into a plain sum of the nodes' values
 // and does not compute the integral its documentation states (:129-142); that integral is
 // computed here.  Its phi nodes are, as in the reference, those of cos_quadrature on [0, 2 pi].
 #pragma once

@@ -15,7 +15,7 @@ Parity pins: the closed forms of the reference's own tests
 Matsubara sums) are checked against this restatement in tests/test_loop_integrals.py.
 
 two_angle_integrate: the reference weights its phi nodes with the weight of the current cos node
-(loop_integrals.hh:182-183); ``two_angle_integrate(..., reference_phi_weight=True)`` restates that
+(loop_integrals.hh:180-181); ``two_angle_integrate(..., reference_phi_weight=True)`` restates that
 literally, the default the integral the reference documents (phi weights of the phi rule).
 """
 from __future__ import annotations
