@@ -9,8 +9,6 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-import numpy as np
-
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libgbint.so")
 

@@ -10,7 +10,7 @@ throws std::runtime_error.
 from __future__ import annotations
 
 import ctypes as C
-from typing import Iterable, Sequence
+from typing import Sequence
 
 import numpy as np
 

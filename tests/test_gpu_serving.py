@@ -8,7 +8,6 @@
 * the node pool evicts unheld axes, so an RG flow with a new k per stage never runs out;
 * one Cash-Karp step of the C4 flow, FP32-compensated against FP64.
 """
-import math
 
 import numpy as np
 import pytest
