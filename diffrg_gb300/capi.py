@@ -26,7 +26,7 @@ GB_MAX_ARGS = 24
 # C ABI symbols declared in include/gbint.h (checked by the CPU test suite)
 EXPORTS = [
     "gb_version", "gb_status_string", "gb_ctx_create", "gb_ctx_destroy", "gb_last_error",
-    "gb_quad_gl", "gb_quad_matsubara", "gb_quad_config",
+    "gb_quad_gl", "gb_quad_rule", "gb_quad_rule_host", "gb_quad_matsubara", "gb_quad_config",
     "gb_table_create", "gb_table_update", "gb_table_update_device", "gb_table_update_many", "gb_table_epoch",
     "gb_table_destroy",
     "gb_batch_create", "gb_batch_run", "gb_batch_run_graph", "gb_batch_results", "gb_batch_get",
@@ -92,6 +92,9 @@ def load(path: str = LIB_PATH):
     L.gb_ctx_destroy.argtypes = [vp]
     L.gb_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
     L.gb_quad_gl.argtypes = [vp, C.c_int, C.c_int, C.POINTER(dp), C.POINTER(dp), C.POINTER(vp), C.POINTER(vp)]
+    L.gb_quad_rule.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(dp), C.POINTER(dp), C.POINTER(vp),
+                               C.POINTER(vp)]
+    L.gb_quad_rule_host.argtypes = [C.c_int, C.c_int, dp, dp]
     L.gb_quad_matsubara.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_int), C.POINTER(dp),
                                     C.POINTER(dp), C.POINTER(vp), C.POINTER(vp), dp]
     L.gb_quad_config.argtypes = [vp, C.c_int, C.c_int, C.c_int]

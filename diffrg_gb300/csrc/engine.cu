@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <cstdio>
 #include <set>
 
@@ -1095,6 +1096,12 @@ int gb_ctx_destroy(gb_ctx *ctx)
     cudaFree(kv.second.d32x);
     cudaFree(kv.second.d32w);
   }
+  for (auto &kv : ctx->rules) {
+    cudaFree(kv.second.d64x);
+    cudaFree(kv.second.d64w);
+    cudaFree(kv.second.d32x);
+    cudaFree(kv.second.d32w);
+  }
   for (auto &m : ctx->mats) {
     cudaFree(m->d64x);
     cudaFree(m->d64w);
@@ -1134,12 +1141,10 @@ int gb_last_error(gb_ctx *ctx, char *buf, size_t len)
 }
 
 // ------------------------------------------------------------------ provider
-int gb_quad_gl(gb_ctx *ctx, int order, int dtype, const double **hx, const double **hw, const void **dx,
-               const void **dw)
+// a cached rule's host arrays, and its device copies of dtype (made on first request)
+static int rule_out(gb_ctx *ctx, GLRule &r, int order, int dtype, const double **hx, const double **hw,
+                    const void **dx, const void **dw)
 {
-  if (!ctx || order <= 0 || order > 4096) return set_error(ctx, GB_EINVAL, "bad GL order");
-  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-  GLRule &r = const_cast<GLRule &>(gl_host(ctx, order));
   if (hx) *hx = r.x.data();
   if (hw) *hw = r.w.data();
   if (dx || dw) {
@@ -1164,6 +1169,45 @@ int gb_quad_gl(gb_ctx *ctx, int order, int dtype, const double **hx, const doubl
       if (dx) *dx = r.d32x;
       if (dw) *dw = r.d32w;
     }
+  }
+  return GB_OK;
+}
+
+int gb_quad_gl(gb_ctx *ctx, int order, int dtype, const double **hx, const double **hw, const void **dx,
+               const void **dw)
+{
+  if (!ctx || order <= 0 || order > 4096) return set_error(ctx, GB_EINVAL, "bad GL order");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  return rule_out(ctx, const_cast<GLRule &>(gl_host(ctx, order)), order, dtype, hx, hw, dx, dw);
+}
+
+int gb_quad_rule(gb_ctx *ctx, int type, int order, int dtype, const double **hx, const double **hw, const void **dx,
+                 const void **dw)
+{
+  if (type == GB_QUAD_LEGENDRE) return gb_quad_gl(ctx, order, dtype, hx, hw, dx, dw);
+  if (!ctx || order <= 0 || order > 4096) return set_error(ctx, GB_EINVAL, "bad quadrature order");
+  if (type < GB_QUAD_LEGENDRE || type > GB_QUAD_JACOBI) return set_error(ctx, GB_EINVAL, "Unknown quadrature type");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  auto it = ctx->rules.find({type, order});
+  if (it == ctx->rules.end()) {
+    GLRule r;
+    fixed_rule(type, order, r.x, r.w);
+    it = ctx->rules.emplace(std::make_pair(type, order), std::move(r)).first;
+  }
+  return rule_out(ctx, it->second, order, dtype, hx, hw, dx, dw);
+}
+
+int gb_quad_rule_host(int type, int order, double *nodes, double *weights)
+{
+  if (order <= 0 || order > 4096 || !nodes || !weights || type < GB_QUAD_LEGENDRE || type > GB_QUAD_JACOBI)
+    return GB_EINVAL;
+  try {
+    std::vector<double> x, w;
+    fixed_rule(type, order, x, w);
+    std::memcpy(nodes, x.data(), order * sizeof(double));
+    std::memcpy(weights, w.data(), order * sizeof(double));
+  } catch (...) {
+    return GB_EINVAL;
   }
   return GB_OK;
 }

@@ -133,6 +133,7 @@ struct gb_ctx {
   // provider
   int mats_min = 32, mats_vacuum = 48, mats_add = 0;
   std::map<int, gbint::GLRule> gl;
+  std::map<std::pair<int, int>, gbint::GLRule> rules;  // (QuadratureType, order), types other than Legendre
   std::vector<std::unique_ptr<gbint::MatsEntry>> mats;
   // nodes
   gbint::NodePool pool;

@@ -117,6 +117,64 @@ namespace gbint
     }
   }
 
+  void fixed_rule(int type, int n, std::vector<double> &x, std::vector<double> &w)
+  {
+    if (n <= 0) throw std::invalid_argument("quadrature order must be positive");
+    switch (type) {
+    case RULE_LEGENDRE:
+    case RULE_JACOBI:
+      gl_rule01(n, x, w);
+      return;
+    case RULE_CHEBYSHEV:
+      // x_i = (1 - cos t_i) / 2 = sin^2(t_i / 2), t_i = (2i+1) pi / (2n); every weight pi / n
+      x.resize(n);
+      w.assign(n, (double)(kPiL / n));
+      for (int i = 0; i < n; ++i) {
+        const long double s = std::sin(kPiL * (2 * i + 1) / (4 * n));
+        x[i] = (double)(s * s);
+      }
+      return;
+    case RULE_LAGUERRE:
+    case RULE_HERMITE: {
+      // nodes: eigenvalues of the Jacobi matrix of the monic recurrence (Laguerre a_j = 2j+1,
+      // b_j = j^2; Hermite a_j = 0, b_j = j/2), by Sturm bisection.  Weights: the Christoffel
+      // function 1 / sum_(k<n) p_k(x_i)^2 of the orthonormal polynomials (Laguerre: L_k itself;
+      // Hermite: H_k / sqrt(2^k k! sqrt(pi))), run forward at each node, where they are the
+      // growing solution; the tail weights (down to ~1e-170 at n = 100) keep full relative
+      // precision, which an eigenvector's first component from inverse iteration does not.
+      // Sums beyond the long double range give weight 0 (the true weight is below FP64's).
+      std::vector<long double> a(n), b(n, 0.0L), xs, ws;
+      for (int j = 0; j < n; ++j) {
+        const long double j1 = j + 1;
+        a[j] = type == RULE_LAGUERRE ? 2.0L * j + 1 : 0.0L;
+        b[j] = type == RULE_LAGUERRE ? j1 * j1 : j1 / 2;
+      }
+      jacobi_gauss(a, b, type == RULE_LAGUERRE ? 1.0L : std::sqrt(kPiL), xs, ws);
+      if (type == RULE_HERMITE && n % 2 == 1) xs[n / 2] = 0.0L;
+      x.resize(n);
+      w.resize(n);
+      const long double h0 = 1.0L / std::sqrt(std::sqrt(kPiL));
+      for (int i = 0; i < n; ++i) {
+        const long double z = xs[i];
+        long double pm = 0.0L, p = type == RULE_LAGUERRE ? 1.0L : h0, sum = p * p;
+        for (int k = 0; k + 1 < n; ++k) {
+          const long double pn = type == RULE_LAGUERRE
+                                     ? ((2 * k + 1 - z) * p - k * pm) / (k + 1)
+                                     : std::sqrt(2.0L / (k + 1)) * z * p - std::sqrt((long double)k / (k + 1)) * pm;
+          pm = p;
+          p = pn;
+          sum += p * p;
+        }
+        x[i] = (double)z;
+        w[i] = (double)(1.0L / sum);
+      }
+      return;
+    }
+    default:
+      throw std::invalid_argument("Unknown quadrature type");
+    }
+  }
+
   MatsRule matsubara_rule(double T, double E, int step, int min_size, int max_size, int vacuum_quad_size,
                           int precision_factor)
   {

@@ -16,6 +16,14 @@
 
 namespace gbint
 {
+  // The rules of the reference's QuadratureType (common/quadrature/quadrature.hh:47), as its
+  // Quadrature<NT>::reinit takes them from GSL's fixed types with a = 0, b = 1, alpha = beta = 0
+  // (quadrature.cu:12-60): Legendre on [0,1]; Chebyshev (first kind) on [0,1], weight
+  // 1/sqrt(x (1-x)); Laguerre on [0,inf), weight exp(-x); Hermite on the real line, weight
+  // exp(-x^2); Jacobi(0,0) on [0,1] (the Legendre rule).  Nodes ascending.
+  enum RuleType : int { RULE_LEGENDRE = 0, RULE_CHEBYSHEV = 1, RULE_LAGUERRE = 2, RULE_HERMITE = 3, RULE_JACOBI = 4 };
+  void fixed_rule(int type, int n, std::vector<double> &x, std::vector<double> &w);
+
   // a: diagonal (n), b: squared off-diagonals (b[i] couples i and i+1; n entries, last unused)
   void jacobi_gauss(const std::vector<long double> &a, const std::vector<long double> &b, long double mu0,
                     std::vector<long double> &x, std::vector<long double> &w);

@@ -197,6 +197,21 @@ class Ticket:
         return True
 
 
+# QuadratureType (DiFfRG/include/DiFfRG/common/quadrature/quadrature.hh:47)
+QUAD_LEGENDRE, QUAD_CHEBYSHEV, QUAD_LAGUERRE, QUAD_HERMITE, QUAD_JACOBI = 0, 1, 2, 3, 4
+
+
+def quad_rule_host(qtype: int, order: int):
+    """Nodes and weights of a QuadratureType without a context (host only, no GPU)."""
+    x = np.zeros(order)
+    w = np.zeros(order)
+    rc = capi.lib().gb_quad_rule_host(qtype, order, x.ctypes.data_as(C.POINTER(C.c_double)),
+                                      w.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc != 0:
+        raise GbError(rc, "gb_quad_rule_host(%d, %d)" % (qtype, order))
+    return x, w
+
+
 class Context:
     """One device context (gb_ctx): provider caches, node pool, table directory, streams."""
 
@@ -228,6 +243,19 @@ class Context:
         dx = C.c_void_p()
         dw = C.c_void_p()
         self.check(capi.lib().gb_quad_gl(self.h, order, dtype, None, None, C.byref(dx), C.byref(dw)))
+        return dx.value, dw.value
+
+    def rule(self, qtype: int, order: int):
+        """Host nodes and weights of a QuadratureType (QUAD_* below) from the context's cache."""
+        hx = C.POINTER(C.c_double)()
+        hw = C.POINTER(C.c_double)()
+        self.check(capi.lib().gb_quad_rule(self.h, qtype, order, 0, C.byref(hx), C.byref(hw), None, None))
+        return np.ctypeslib.as_array(hx, (order,)).copy(), np.ctypeslib.as_array(hw, (order,)).copy()
+
+    def rule_device(self, qtype: int, order: int, dtype=0):
+        dx = C.c_void_p()
+        dw = C.c_void_p()
+        self.check(capi.lib().gb_quad_rule(self.h, qtype, order, dtype, None, None, C.byref(dx), C.byref(dw)))
         return dx.value, dw.value
 
     def matsubara(self, T: float, E: float):

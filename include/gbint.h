@@ -148,6 +148,20 @@ int gb_last_error(gb_ctx *ctx, char *buf, size_t len);
  * process lifetime, as in the reference). */
 int gb_quad_gl(gb_ctx *ctx, int order, int dtype, const double **h_nodes, const double **h_weights,
                const void **d_nodes, const void **d_weights);
+/* The rule of a QuadratureType (common/quadrature/quadrature.hh:47, same order): Quadrature<NT>::reinit
+ * (quadrature.cu:12-60) takes GSL's fixed types with a = 0, b = 1, alpha = beta = 0:
+ *   GB_QUAD_LEGENDRE   [0,1], weight 1 (the rule of gb_quad_gl)
+ *   GB_QUAD_CHEBYSHEV  [0,1], weight 1/sqrt(x (1-x))
+ *   GB_QUAD_LAGUERRE   [0,inf), weight exp(-x)
+ *   GB_QUAD_HERMITE    (-inf,inf), weight exp(-x^2)
+ *   GB_QUAD_JACOBI     [0,1], weight (1-x)^0 x^0 (the Legendre rule)
+ * Nodes ascending.  Cached per (type, order) like gb_quad_gl; an unknown type is GB_EINVAL
+ * ("Unknown quadrature type", as the reference throws). */
+enum { GB_QUAD_LEGENDRE = 0, GB_QUAD_CHEBYSHEV = 1, GB_QUAD_LAGUERRE = 2, GB_QUAD_HERMITE = 3, GB_QUAD_JACOBI = 4 };
+int gb_quad_rule(gb_ctx *ctx, int type, int order, int dtype, const double **h_nodes, const double **h_weights,
+                 const void **d_nodes, const void **d_weights);
+/* The same rule into caller arrays of `order` doubles; host only, needs no context or GPU. */
+int gb_quad_rule_host(int type, int order, double *nodes, double *weights);
 /* Monien rule for (T, E): MatsubaraStorage::get_matsubara_quadrature (quadrature_provider.cu:12-58).
  * *size receives the rule size, *T_rule the rule's own T (0 for the vacuum form). */
 int gb_quad_matsubara(gb_ctx *ctx, double T, double E, int dtype, int *size, const double **h_nodes,

@@ -149,15 +149,17 @@ namespace DiFfRG
     gb_ctx *ctx() const { return ctx_.get(); }
     int num_sms() const { return num_sms_; }
 
+    // the rules of every QuadratureType (gb_quad_rule: GSL's fixed types with a = 0, b = 1,
+    // alpha = beta = 0, as quadrature.cu:12-60 takes them)
     template <typename NT = double>
-    const std::vector<NT> &get_points(const size_t order, const QuadratureType = QuadratureType::legendre)
+    const std::vector<NT> &get_points(const size_t order, const QuadratureType type = QuadratureType::legendre)
     {
-      return host_rule<NT>(order).first;
+      return host_rule<NT>(order, type).first;
     }
     template <typename NT = double>
-    const std::vector<NT> &get_weights(const size_t order, const QuadratureType = QuadratureType::legendre)
+    const std::vector<NT> &get_weights(const size_t order, const QuadratureType type = QuadratureType::legendre)
     {
-      return host_rule<NT>(order).second;
+      return host_rule<NT>(order, type).second;
     }
     template <typename NT = double> const std::vector<NT> &get_matsubara_points(const NT T, const NT E)
     {
@@ -168,17 +170,19 @@ namespace DiFfRG
       return host_mats<NT>(T, E).second;
     }
     template <typename NT = double>
-    const NT *get_device_points(const size_t order, const int = 0, const QuadratureType = QuadratureType::legendre)
+    const NT *get_device_points(const size_t order, const int = 0, const QuadratureType type = QuadratureType::legendre)
     {
       const void *dx = nullptr;
-      gbint_detail::check(ctx(), gb_quad_gl(ctx(), (int)order, dtype<NT>(), nullptr, nullptr, &dx, nullptr), "get_device_points");
+      gbint_detail::check(ctx(), gb_quad_rule(ctx(), (int)type, (int)order, dtype<NT>(), nullptr, nullptr, &dx, nullptr),
+                          "get_device_points");
       return static_cast<const NT *>(dx);
     }
     template <typename NT = double>
-    const NT *get_device_weights(const size_t order, const int = 0, const QuadratureType = QuadratureType::legendre)
+    const NT *get_device_weights(const size_t order, const int = 0, const QuadratureType type = QuadratureType::legendre)
     {
       const void *dw = nullptr;
-      gbint_detail::check(ctx(), gb_quad_gl(ctx(), (int)order, dtype<NT>(), nullptr, nullptr, nullptr, &dw), "get_device_weights");
+      gbint_detail::check(ctx(), gb_quad_rule(ctx(), (int)type, (int)order, dtype<NT>(), nullptr, nullptr, nullptr, &dw),
+                          "get_device_weights");
       return static_cast<const NT *>(dw);
     }
     template <typename NT = double> const NT *get_device_matsubara_points(const NT T, const NT E, const int = 0)
@@ -213,15 +217,18 @@ namespace DiFfRG
       static_assert(std::is_same_v<NT, double> || std::is_same_v<NT, float>, "double or float");
       return std::is_same_v<NT, double> ? GB_DTYPE_F64 : GB_DTYPE_F32;
     }
-    template <typename NT> const std::pair<std::vector<NT>, std::vector<NT>> &host_rule(size_t order)
+    template <typename NT>
+    const std::pair<std::vector<NT>, std::vector<NT>> &host_rule(size_t order, QuadratureType type)
     {
       std::lock_guard<std::mutex> lk(mu_);
-      auto &cache = std::get<std::map<size_t, std::pair<std::vector<NT>, std::vector<NT>>>>(gl_);
-      auto it = cache.find(order);
+      auto &cache = std::get<std::map<std::pair<int, size_t>, std::pair<std::vector<NT>, std::vector<NT>>>>(gl_);
+      const std::pair<int, size_t> key{(int)type, order};
+      auto it = cache.find(key);
       if (it != cache.end()) return it->second;
       const double *hx = nullptr, *hw = nullptr;
-      gbint_detail::check(ctx(), gb_quad_gl(ctx(), (int)order, GB_DTYPE_F64, &hx, &hw, nullptr, nullptr), "get_points");
-      auto &e = cache[order];
+      gbint_detail::check(ctx(), gb_quad_rule(ctx(), (int)type, (int)order, GB_DTYPE_F64, &hx, &hw, nullptr, nullptr),
+                          "get_points");
+      auto &e = cache[key];
       e.first.assign(hx, hx + order);
       e.second.assign(hw, hw + order);
       return e;
@@ -243,8 +250,8 @@ namespace DiFfRG
     std::shared_ptr<gb_ctx> ctx_;
     int num_sms_ = 1;
     std::mutex mu_;
-    std::tuple<std::map<size_t, std::pair<std::vector<double>, std::vector<double>>>,
-               std::map<size_t, std::pair<std::vector<float>, std::vector<float>>>>
+    std::tuple<std::map<std::pair<int, size_t>, std::pair<std::vector<double>, std::vector<double>>>,
+               std::map<std::pair<int, size_t>, std::pair<std::vector<float>, std::vector<float>>>>
         gl_;
     std::tuple<std::map<std::pair<double, double>, std::pair<std::vector<double>, std::vector<double>>>,
                std::map<std::pair<double, double>, std::pair<std::vector<float>, std::vector<float>>>>

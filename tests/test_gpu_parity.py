@@ -45,6 +45,35 @@ def test_gl_provider_matches_oracle(ctx, oracle, n):
     assert np.max(np.abs(w - wo)) <= 4e-16 * max(1, n / 64)
 
 
+def _device_array(ptr, n, typestr):
+    import torch
+
+    class _View:
+        pass
+
+    v = _View()
+    # torch takes no read-only flag (it must be False); the view is only copied to the host
+    v.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False), "strides": None,
+                                  "version": 3}
+    return torch.as_tensor(v, device="cuda").cpu().numpy()
+
+
+@pytest.mark.parametrize("qtype", [0, 1, 2, 3, 4])
+def test_rule_types_host_and_device(ctx, qtype):
+    """QuadratureProvider::get_points/get_device_points with a QuadratureType: the context's
+    cached rule equals the host-only rule, and its FP64 / FP32 device copies hold the same values."""
+    from diffrg_gb300 import engine as E
+
+    n = 24
+    x, w = ctx.rule(qtype, n)
+    xh, wh = E.quad_rule_host(qtype, n)
+    assert np.array_equal(x, xh) and np.array_equal(w, wh)
+    for dtype, typestr, npt in ((0, "<f8", np.float64), (1, "<f4", np.float32)):
+        dx, dw = ctx.rule_device(qtype, n, dtype)
+        assert np.array_equal(_device_array(dx, n, typestr), x.astype(npt))
+        assert np.array_equal(_device_array(dw, n, typestr), w.astype(npt))
+
+
 @pytest.mark.parametrize("T,E", [(0.05, 1.0), (0.2, 1.0), (1.0, 1.0), (0.1, 0.3), (0.001, 1.0), (0.0, 2.0)])
 def test_matsubara_provider_matches_oracle(ctx, oracle, T, E):
     x, w, tr = ctx.matsubara(T, E)
