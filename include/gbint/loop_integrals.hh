@@ -27,6 +27,8 @@
 // (loop_integrals.hh:180-181), which turns the phi quadrature into a plain sum of the nodes' values
 // and does not compute the integral its documentation states (:129-142); that integral is
 // computed here.  Its phi nodes are, as in the reference, those of cos_quadrature on [0, 2 pi].
+// Defining GBINT_LOOP_REFERENCE_PHI_WEIGHT before this header restores the reference's weighting,
+// for comparisons with results obtained from it.
 #pragma once
 
 #include <algorithm>
@@ -223,7 +225,11 @@ namespace DiFfRG
           const double cos_weight = cos_q_w[cos_it] * 2.;
           for (int phi_it = 0; phi_it < cos_size; ++phi_it) {
             const double phi = cos_q_p[phi_it][0] * two_pi;
+#ifdef GBINT_LOOP_REFERENCE_PHI_WEIGHT
+            const double phi_weight = cos_q_w[cos_it] * two_pi;  // the reference's weighting, opt-in
+#else
             const double phi_weight = cos_q_w[phi_it] * two_pi;
+#endif
             acc += x_weight * prefactor * (0.5 * ipow<d>(k) * std::pow(x, (d - 2) / 2.)) * 0.5 * cos_weight *
                    phi_weight / two_pi * fun(q2, cos, phi);
           }

@@ -389,3 +389,20 @@ int main() {
     assert r.returncode == 0, r.stderr[-4000:]
     r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_reference_phi_weighting_on_request(tmp_path):
+    """-DGBINT_LOOP_REFERENCE_PHI_WEIGHT gives the reference's two_angle_integrate
+    (loop_integrals.hh:180-181), as the oracle restates it literally."""
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    exe = str(tmp_path / "ref_phi")
+    r = subprocess.run([gxx, "-std=c++17", "-O2", "-pthread", "-DGBINT_LOOP_REFERENCE_PHI_WEIGHT", "-I",
+                        os.path.join(ROOT, "include"), SRC, "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+    f = lambda q2, c, ph: (1 + q2) * (0.5 + c * c) * (1 + 0.1 * ph)
+    theirs = L.two_angle_integrate(f, 4, 16, 1.3, 0.9, 5, reference_phi_weight=True)
+    got = parse_c(run(exe, [li_line("two_angle", d=4, nx=16, ncos=5, x_extent=1.3, k=0.9, a=(1, 1), c=(0.5, 0, 1),
+                                    e=(1, 0.1))])[0]).real
+    assert abs(got - theirs) <= 1e-13 * abs(theirs)
