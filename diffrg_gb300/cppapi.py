@@ -2,7 +2,10 @@
 
 A user translation unit that includes the header is compiled by nvcc for sm_103a and linked
 against the in-tree libgbint.so; `compile_program` does exactly that (with an rpath to the
-library), `build_tests` compiles the test driver tests/cpp/test_integrators.cu.
+library), `build_tests` compiles the test driver tests/cpp/test_integrators.cu, and
+`compile_flow` compiles a flow in the layout of DiFfRG's generated code (an example directory
+holding flows/def.hh and flows/<dir>/<X>.{hh,cu,kernel}) into tests/cpp/flow_driver.cu with the
+drop-in headers at the reference's include paths (include/gbint/compat).
 """
 from __future__ import annotations
 
@@ -15,6 +18,50 @@ from . import build as B
 ROOT = B.ROOT
 TEST_SRC = os.path.join(ROOT, "tests", "cpp", "test_integrators.cu")
 TEST_BIN = os.path.join(ROOT, "tests", "cpp", "bin", "test_integrators")
+
+
+COMPAT = os.path.join(B.INCLUDE, "gbint", "compat")
+FLOW_DRIVER = os.path.join(ROOT, "tests", "cpp", "flow_driver.cu")
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+
+
+def _headers_digest(h) -> None:
+    for d, _, fs in sorted(os.walk(B.INCLUDE)):
+        for f in sorted(fs):
+            if f.endswith((".h", ".hh", ".cuh")):
+                h.update(f.encode())
+                h.update(open(os.path.join(d, f), "rb").read())
+
+
+def compile_flow(example_dir: str, source: str, name: str, kind: int, family: int, out: str) -> str:
+    """Compile tests/cpp/flow_driver.cu around the flow file `source` (relative to example_dir,
+    e.g. "flows/AA/ZA.cu"); the flow's own files are compiled as they are."""
+    lib = B.build()
+    libdir = os.path.dirname(lib)
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    h = hashlib.sha256()
+    _headers_digest(h)
+    for p in (FLOW_DRIVER, os.path.join(ORACLE_DIR, "families.hh"), os.path.join(ORACLE_DIR, "oracle.hh")):
+        h.update(open(p, "rb").read())
+    flows = os.path.join(example_dir, "flows")
+    for d, _, fs in sorted(os.walk(flows)):
+        for f in sorted(fs):
+            h.update(open(os.path.join(d, f), "rb").read())
+    h.update(("%s|%s|%d|%d" % (source, name, kind, family)).encode())
+    h.update(open(lib, "rb").read()[:4096])
+    stamp = out + ".stamp"
+    if os.path.exists(out) and os.path.exists(stamp) and open(stamp).read() == h.hexdigest():
+        return out
+    cmd = [B.nvcc(), "-std=c++20", "-O2", "--expt-relaxed-constexpr", "-I", COMPAT, "-I", B.INCLUDE, "-I", ORACLE_DIR,
+           "-I", example_dir, '-DGBINT_FLOW_SOURCE="%s"' % source, "-DGBINT_FLOW_NAME=%s" % name,
+           "-DGBINT_FLOW_KIND=%d" % kind, "-DGBINT_FLOW_FAMILY=%d" % family] + B.ARCH + \
+        [FLOW_DRIVER, "-o", out, "-L", libdir, "-lgbint", "-Xlinker", "-rpath," + libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stderr[-6000:])
+    with open(stamp, "w") as f:
+        f.write(h.hexdigest())
+    return out
 
 
 def compile_program(src: str, out: str, extra=()) -> str:

@@ -8,7 +8,9 @@
 #include <cmath>
 #include <cstring>
 #include <cstdio>
+#include <new>
 #include <set>
+#include <stdexcept>
 
 #include <cub/device/device_reduce.cuh>
 
@@ -168,10 +170,15 @@ namespace
                     aw = dev::df_from(h.w[i] * h.a[i]);
       rec[i] = NodeRec{v.hi, v.lo, w.hi, w.lo, a.hi, a.lo, aw.hi, aw.lo};
     }
-    GB_CUDA(cudaMemcpy(ctx->pool.d_v + off, h.v.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-    GB_CUDA(cudaMemcpy(ctx->pool.d_w + off, h.w.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-    GB_CUDA(cudaMemcpy(ctx->pool.d_a + off, h.a.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-    GB_CUDA(cudaMemcpy(ctx->pool.d_rec + off, rec.data(), n * sizeof(NodeRec), cudaMemcpyHostToDevice));
+    // stream-ordered copies on the context's own (non-blocking) stream, then a wait on that
+    // stream only: the nodes are in place before any later launch on any stream reads them,
+    // and the legacy default stream is never touched
+    cudaStream_t s = ctx->stream;
+    GB_CUDA(cudaMemcpyAsync(ctx->pool.d_v + off, h.v.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+    GB_CUDA(cudaMemcpyAsync(ctx->pool.d_w + off, h.w.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+    GB_CUDA(cudaMemcpyAsync(ctx->pool.d_a + off, h.a.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+    GB_CUDA(cudaMemcpyAsync(ctx->pool.d_rec + off, rec.data(), n * sizeof(NodeRec), cudaMemcpyHostToDevice, s));
+    GB_CUDA(cudaStreamSynchronize(s));
     ref.off = off;
     ref.n = n;
     ref.pm_from = std::min(h.pm_from, n);
@@ -1187,12 +1194,30 @@ int gb_quad_rule(gb_ctx *ctx, int type, int order, int dtype, const double **hx,
   if (type == GB_QUAD_LEGENDRE) return gb_quad_gl(ctx, order, dtype, hx, hw, dx, dw);
   if (!ctx || order <= 0 || order > 4096) return set_error(ctx, GB_EINVAL, "bad quadrature order");
   if (type < GB_QUAD_LEGENDRE || type > GB_QUAD_JACOBI) return set_error(ctx, GB_EINVAL, "Unknown quadrature type");
+  {
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    auto it = ctx->rules.find({type, order});
+    if (it != ctx->rules.end()) return rule_out(ctx, it->second, order, dtype, hx, hw, dx, dw);
+  }
+  // A cold rule is built without the context lock (Laguerre and Hermite bisect every node on the
+  // Jacobi matrix: up to ~1 s at order 4096), so serving and other callers are not held up; a
+  // rule built twice by racing callers is the same rule, and the first one inserted is kept.
+  GLRule r;
+  try {
+    fixed_rule(type, order, r.x, r.w);
+  } catch (const std::bad_alloc &) {
+    return set_error(ctx, GB_ENOMEM, "quadrature rule: host memory");
+  } catch (const std::exception &ex) {
+    return set_error(ctx, GB_EINVAL, std::string("quadrature rule: ") + ex.what());
+  }
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   auto it = ctx->rules.find({type, order});
   if (it == ctx->rules.end()) {
-    GLRule r;
-    fixed_rule(type, order, r.x, r.w);
-    it = ctx->rules.emplace(std::make_pair(type, order), std::move(r)).first;
+    try {
+      it = ctx->rules.emplace(std::make_pair(type, order), std::move(r)).first;
+    } catch (const std::bad_alloc &) {
+      return set_error(ctx, GB_ENOMEM, "quadrature rule: host memory");
+    }
   }
   return rule_out(ctx, it->second, order, dtype, hx, hw, dx, dw);
 }

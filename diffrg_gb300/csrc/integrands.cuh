@@ -177,5 +177,34 @@ namespace gbint
       default: break;
       }
     }
+
+    // One grid point of an FP64 item: the flattened index `pt` is split into one node per axis
+    // (last axis fastest), the node values set the integrand's coordinates and the node weights
+    // multiply; axes with +-q0 pairs add the integrand at -q0 from node pm_from on.  The one
+    // definition behind every FP64 kernel that walks an item's grid (k_generic, k_generic_noalloc),
+    // so their results agree bit for bit.
+    __device__ __forceinline__ double eval_point_fp64(const ItemDev &it, long long pt, const double *pv,
+                                                      const double *pw, const TableDev *T)
+    {
+      Pt P{0, 0, 0, 0, 0, 0, 0, 0, it.k};
+      double w = 1.0;
+      bool pm = false;
+      long long rem = pt;
+      for (int a = it.n_axes - 1; a >= 0; --a) {
+        const AxisRef ax = it.ax[a];
+        const int idx = (int)(rem % ax.n);
+        rem /= ax.n;
+        const int node = ax.off + idx;
+        set_role(P, ax.role, pv[node]);
+        w *= pw[node];
+        if (idx >= ax.pm_from) pm = true;
+      }
+      double f = ig_eval64(it.integrand, it.family, P, it.args, T);
+      if (pm) {
+        P.q0 = -P.q0;
+        f += ig_eval64(it.integrand, it.family, P, it.args, T);
+      }
+      return w * f;
+    }
   } // namespace dev
 } // namespace gbint

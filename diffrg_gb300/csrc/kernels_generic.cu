@@ -16,30 +16,6 @@ namespace gbint
   // Replaces gridreduce_* + thrust::reduce (e.g. integrator_4D_gpu.hh:21-49,141-158) with one
   // launch for a whole batch and no per-point global buffer.
   // ------------------------------------------------------------------------------------------
-  __device__ __forceinline__ double eval_point(const ItemDev &it, long long pt, const double *pv, const double *pw,
-                                               const TableDev *T)
-  {
-    Pt P{0, 0, 0, 0, 0, 0, 0, 0, it.k};
-    double w = 1.0;
-    bool pm = false;
-    long long rem = pt;
-    for (int a = it.n_axes - 1; a >= 0; --a) {
-      const AxisRef ax = it.ax[a];
-      const int idx = (int)(rem % ax.n);
-      rem /= ax.n;
-      const int node = ax.off + idx;
-      set_role(P, ax.role, pv[node]);
-      w *= pw[node];
-      if (idx >= ax.pm_from) pm = true;
-    }
-    double f = ig_eval64(it.integrand, it.family, P, it.args, T);
-    if (pm) {
-      P.q0 = -P.q0;
-      f += ig_eval64(it.integrand, it.family, P, it.args, T);
-    }
-    return w * f;
-  }
-
   __global__ void __launch_bounds__(kGenericThreads) k_generic(const RunParams P)
   {
     __shared__ double red[32];
@@ -61,7 +37,7 @@ namespace gbint
 #pragma unroll 1
       for (int k = 0; k < kGenericPPT; ++k) {
         const int local = threadIdx.x + k * blockDim.x;
-        if (local < U.row_count) acc += eval_point(it, (long long)U.row_begin + local, P.pv, P.pw, sT);
+        if (local < U.row_count) acc += eval_point_fp64(it, (long long)U.row_begin + local, P.pv, P.pw, sT);
       }
       const double tot = block_sum(acc, red);
       unit_finish(P, u, U.item, tot, red, &s_flag);

@@ -1,27 +1,38 @@
 // noalloc.cu -- gb_get_noalloc: one FP64 integral evaluated without allocating device memory.
 //
-// Who needs it: hosts that must not call cudaMalloc/cudaFree (or any allocating library
-// routine) while they integrate -- e.g. a time stepper that records a whole right-hand-side
-// evaluation under CUDA stream capture in global mode, where cudaMalloc is an illegal call, or
-// a code that runs under a fixed device-memory budget handed out once at start-up by another
-// allocator.  gb_get builds a small batch per call and allocates its scratch; this entry point
-// keeps its scratch in a fixed file-scope device array instead.
+// Who needs it: callers that cannot let this library call cudaMalloc or cudaFree while they
+// integrate.  Two kinds are common.  (1) A host program whose device memory belongs to another
+// allocator: a caching or pool allocator (a PyTorch process, an RMM pool) that reserved nearly
+// all of HBM at start-up, or a code that grants each library a fixed budget once -- a cudaMalloc
+// from here would fail, or would take memory the owner has already promised elsewhere.
+// (2) A caller on a latency-critical path with work in flight on other streams: cudaFree waits
+// for the whole device, and cudaMalloc may, so one allocating call stalls everyone's kernels.
+// gb_get builds a small batch per call and allocates its scratch; this entry point keeps its
+// scratch in a fixed file-scope device array instead, and otherwise computes the same integral
+// with the same kernel body (dev::eval_point_fp64 and the same reduction order).
 //
 // Scratch: g_noalloc_scratch below, GB_NOALLOC_SCRATCH_BYTES (36 KiB) per device, resident from
-// module load until process exit.  It holds the integral's descriptor, two counters, the result
-// and one FP64 partial per work unit of 1024 grid points, so one call accepts at most
-// GB_NOALLOC_MAX_POINTS = 4096 * 1024 = 4,194,304 grid points (nodes per axis multiplied; the
-// +-q0 pairs of finite-T axes count once).  Larger integrals are rejected with GB_EINVAL.
+// module load until process exit on every GPU that loads the library.  It holds the integral's
+// descriptor, two counters, the result and one FP64 partial per work unit of 1024 grid points,
+// so one call accepts at most GB_NOALLOC_MAX_POINTS = 4096 * 1024 = 4,194,304 grid points (nodes
+// per axis multiplied; the +-q0 pairs of finite-T axes count once).  Larger integrals are
+// rejected with GB_EINVAL and a message naming the limit; nothing is launched for them.
 //
-// Every call on a device shares the one array; the counters are cleared on the stream before
-// each launch.  Calls serialise on the context mutex and complete (stream synchronised) before
-// they return; two contexts on the same device whose calls overlap on the GPU race on the array.
+// Every call on a device shares the one array and finds the previous call's contents in it: the
+// descriptor is rewritten and the two counters are cleared on the stream before each launch, and
+// the result slot is written by the kernel before it is read.  Calls through one context
+// serialise on the context mutex and complete (the context's stream is synchronised) before they
+// return; calls through two contexts on the same device whose work overlaps on the GPU race on
+// the array and must not be made.
 //
-// The host cannot use the array's name as a device address (in host code it names a host-side
-// stand-in).  The first call on each device resolves the address with cudaGetSymbolAddress with
-// that device current and caches it; make that first call before any stream capture begins.
-// New quadrature orders fill host-side caches and are copied into the context's pre-allocated
-// node pool; no device or pinned memory is allocated by this entry point.
+// The host cannot use the array's name as a device address: in host code it names a host-side
+// stand-in, and a kernel given that pointer would fault or silently use the wrong memory.  The
+// first call on each device therefore resolves the address with cudaGetSymbolAddress, with that
+// device current, checks the return code and caches the address per device ordinal.  That lookup
+// is part of the first call's set-up: make the first call on each device before any CUDA stream
+// capture begins.  New quadrature orders and axes fill host-side caches and
+// are copied into the context's node pool, which was allocated once at gb_ctx_create; no device
+// or pinned memory is allocated by this entry point.
 #include <cstddef>
 #include <mutex>
 
@@ -56,31 +67,6 @@ namespace gbint
     std::mutex g_addr_mu;
     void *g_addr[64] = {};  // device address of g_noalloc_scratch per device ordinal
 
-    // same per-point evaluation as the generic kernel (kernels_generic.cu)
-    __device__ __forceinline__ double eval_point_na(const ItemDev &it, long long pt, const double *pv, const double *pw,
-                                                    const TableDev *T)
-    {
-      dev::Pt P{0, 0, 0, 0, 0, 0, 0, 0, it.k};
-      double w = 1.0;
-      bool pm = false;
-      long long rem = pt;
-      for (int a = it.n_axes - 1; a >= 0; --a) {
-        const AxisRef ax = it.ax[a];
-        const int idx = (int)(rem % ax.n);
-        rem /= ax.n;
-        const int node = ax.off + idx;
-        dev::set_role(P, ax.role, pv[node]);
-        w *= pw[node];
-        if (idx >= ax.pm_from) pm = true;
-      }
-      double f = dev::ig_eval64(it.integrand, it.family, P, it.args, T);
-      if (pm) {
-        P.q0 = -P.q0;
-        f += dev::ig_eval64(it.integrand, it.family, P, it.args, T);
-      }
-      return w * f;
-    }
-
     // The generic FP64 kernel with its work units implied (unit u = grid points
     // [u*1024, (u+1)*1024)) and all scratch -- descriptor, counters, partials, result -- in the
     // static array.  Reduction order equals the generic kernel's, so results agree bitwise.
@@ -112,7 +98,7 @@ namespace gbint
 #pragma unroll 1
         for (int k = 0; k < kGenericPPT; ++k) {
           const int local = threadIdx.x + k * blockDim.x;
-          if (local < count) acc += eval_point_na(it, begin + local, pv, pw, sT);
+          if (local < count) acc += dev::eval_point_fp64(it, begin + local, pv, pw, sT);
         }
         const double tot = dev::block_sum(acc, red);
         dev::unit_finish(P, u, 0, tot, red, &s_flag);

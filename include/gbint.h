@@ -217,16 +217,20 @@ int gb_batch_destroy(gb_ctx *ctx, gb_batch *b);
 int gb_get(gb_ctx *ctx, const gb_integral *item, gb_table *const *tables, int n_tables, int precision,
            double *out);
 
-/* Allocation-free get() in FP64 -- no counterpart in the reference.  For hosts that must not
- * allocate device memory while they integrate: code running under CUDA stream capture in
- * global mode (where cudaMalloc is an illegal call) or under a fixed memory budget handed out by
- * another allocator at start-up.  It calls no cudaMalloc/cudaFree nor any allocating library
+/* Allocation-free get() in FP64 -- no counterpart in the reference.  For callers that cannot let
+ * the library allocate device memory while they integrate: a host program whose HBM belongs to
+ * another allocator (a caching or pool allocator that reserved it at start-up, or a fixed budget
+ * granted once), and callers on a latency-critical path, where cudaFree (and possibly cudaMalloc)
+ * would wait for the whole device.  It calls no cudaMalloc/cudaFree nor any allocating library
  * routine; its scratch is one fixed file-scope device array of GB_NOALLOC_SCRATCH_BYTES per
- * device, held until process exit.  Limit: GB_NOALLOC_MAX_POINTS grid points per integral
- * (larger ones return GB_EINVAL).  The first call on a device looks up the array's address
- * (cudaGetSymbolAddress) -- make it before any stream capture.  All calls on a device share the
- * array: calls through one context serialise, calls from two contexts that overlap on the GPU
- * race.  Results equal gb_get(..., GB_PREC_FP64, ...). */
+ * device, held by every GPU that loads the library until process exit.  Limit:
+ * GB_NOALLOC_MAX_POINTS grid points per integral (larger ones return GB_EINVAL, nothing runs).
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress with
+ * that device current) -- make it before any CUDA stream capture begins.  All calls on a device
+ * share the array, which keeps the last call's contents (the counters are cleared before each
+ * launch): calls through one context serialise, calls from two contexts whose work overlaps on
+ * the GPU race.  The call runs on the context's stream and returns with the result in *out;
+ * results equal gb_get(..., GB_PREC_FP64, ...). */
 #define GB_NOALLOC_MAX_POINTS 4194304
 #define GB_NOALLOC_SCRATCH_BYTES 36864
 int gb_get_noalloc(gb_ctx *ctx, const gb_integral *item, gb_table *const *tables, int n_tables, double *out);

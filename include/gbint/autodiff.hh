@@ -21,12 +21,32 @@
 #include <cmath>
 #include <type_traits>
 
+#include <cuda/std/complex>
+
 #include "gbint/integrators.hh"
 
 namespace gbint
 {
+  template <typename T> struct dual;
   namespace ad_detail
   {
+    template <typename T> struct is_cplx : std::false_type {
+    };
+    template <typename T> struct is_cplx<::cuda::std::complex<T>> : std::true_type {
+    };
+    // complex components: the elementary functions of cuda::std
+    template <typename T> __host__ __device__ ::cuda::std::complex<T> exp_(const ::cuda::std::complex<T> &x)
+    {
+      return ::cuda::std::exp(x);
+    }
+    template <typename T> __host__ __device__ ::cuda::std::complex<T> log_(const ::cuda::std::complex<T> &x)
+    {
+      return ::cuda::std::log(x);
+    }
+    template <typename T> __host__ __device__ ::cuda::std::complex<T> sqrt_(const ::cuda::std::complex<T> &x)
+    {
+      return ::cuda::std::sqrt(x);
+    }
     __host__ __device__ inline double exp_(double x) { return ::exp(x); }
     __host__ __device__ inline float exp_(float x) { return ::expf(x); }
     __host__ __device__ inline double expm1_(double x) { return ::expm1(x); }
@@ -47,21 +67,41 @@ namespace gbint
     __host__ __device__ inline float pow_(float x, float y) { return ::powf(x, y); }
     __host__ __device__ inline double abs_(double x) { return ::fabs(x); }
     __host__ __device__ inline float abs_(float x) { return ::fabsf(x); }
+    __host__ __device__ inline double sinh_(double x) { return ::sinh(x); }
+    __host__ __device__ inline float sinh_(float x) { return ::sinhf(x); }
+    __host__ __device__ inline double cosh_(double x) { return ::cosh(x); }
+    __host__ __device__ inline float cosh_(float x) { return ::coshf(x); }
+    __host__ __device__ inline double tan_(double x) { return ::tan(x); }
+    __host__ __device__ inline float tan_(float x) { return ::tanf(x); }
+    __host__ __device__ inline double atan_(double x) { return ::atan(x); }
+    __host__ __device__ inline float atan_(float x) { return ::atanf(x); }
+    __host__ __device__ inline double atan2_(double y, double x) { return ::atan2(y, x); }
+    __host__ __device__ inline float atan2_(float y, float x) { return ::atan2f(y, x); }
+    __host__ __device__ inline double asin_(double x) { return ::asin(x); }
+    __host__ __device__ inline float asin_(float x) { return ::asinf(x); }
+    __host__ __device__ inline double acos_(double x) { return ::acos(x); }
+    __host__ __device__ inline float acos_(float x) { return ::acosf(x); }
   } // namespace ad_detail
 
   // value v and derivative d of a quantity along one seeded direction
   template <typename T> struct dual {
-    static_assert(std::is_floating_point_v<T>, "gbint::dual<T> needs a floating-point T");
+    static_assert(std::is_floating_point_v<T> || ad_detail::is_cplx<T>::value,
+                  "gbint::dual<T> needs a floating-point or complex T");
     T v = 0, d = 0;
 
-    __host__ __device__ constexpr dual() = default;
+    constexpr dual() = default;
     __host__ __device__ constexpr dual(T value, T deriv) : v(value), d(deriv) {}
     // a constant (zero derivative): implicit, as for autodiff::real
-    template <typename S, std::enable_if_t<std::is_arithmetic_v<S>, int> = 0>
+    template <typename S, std::enable_if_t<std::is_arithmetic_v<S> || std::is_same_v<S, T>, int> = 0>
     __host__ __device__ constexpr dual(S value) : v(T(value)), d(0)
     {
     }
     template <typename U> __host__ __device__ constexpr explicit dual(const dual<U> &o) : v(T(o.v)), d(T(o.d)) {}
+    // the value, by explicit conversion (as autodiff::real converts with a cast)
+    __host__ __device__ constexpr explicit operator T() const { return v; }
+    // component access in autodiff::real's layout: [0] the value, [1] the derivative
+    __host__ __device__ T &operator[](int i) { return i ? d : v; }
+    __host__ __device__ const T &operator[](int i) const { return i ? d : v; }
 
     __host__ __device__ dual &operator+=(const dual &b)
     {
@@ -90,7 +130,9 @@ namespace gbint
     }
   };
 
-  using real = dual<double>;
+  // the value-and-derivative type of double results; under the reference's name it is
+  // autodiff::real (bottom of this file)
+  using dreal = dual<double>;
 
   template <typename T> __host__ __device__ constexpr T val(const dual<T> &a) { return a.v; }
   template <typename T> __host__ __device__ constexpr T derivative(const dual<T> &a) { return a.d; }
@@ -121,6 +163,69 @@ namespace gbint
   GBINT_DUAL_SCALAR_OPS(*)
   GBINT_DUAL_SCALAR_OPS(/)
 #undef GBINT_DUAL_SCALAR_OPS
+
+  // complex-valued forward numbers (the reference's cxReal, autodiff::Real<1, complex<double>>):
+  // a real dual meeting a complex number or a complex dual becomes a complex dual
+#define GBINT_DUAL_COMPLEX_OPS(OP)                                                                        \
+  template <typename T>                                                                                   \
+  __host__ __device__ dual<::cuda::std::complex<T>> operator OP(const dual<::cuda::std::complex<T>> &a,   \
+                                                             const ::cuda::std::complex<T> &s)            \
+  {                                                                                                       \
+    return a OP dual<::cuda::std::complex<T>>(s);                                                        \
+  }                                                                                                       \
+  template <typename T>                                                                                   \
+  __host__ __device__ dual<::cuda::std::complex<T>> operator OP(const ::cuda::std::complex<T> &s,         \
+                                                             const dual<::cuda::std::complex<T>> &a)      \
+  {                                                                                                       \
+    return dual<::cuda::std::complex<T>>(s) OP a;                                                        \
+  }                                                                                                       \
+  template <typename T, std::enable_if_t<std::is_floating_point_v<T>, int> = 0>                           \
+  __host__ __device__ dual<::cuda::std::complex<T>> operator OP(const dual<T> &a, const ::cuda::std::complex<T> &s) \
+  {                                                                                                       \
+    return dual<::cuda::std::complex<T>>(a) OP dual<::cuda::std::complex<T>>(s);                         \
+  }                                                                                                       \
+  template <typename T, std::enable_if_t<std::is_floating_point_v<T>, int> = 0>                           \
+  __host__ __device__ dual<::cuda::std::complex<T>> operator OP(const ::cuda::std::complex<T> &s, const dual<T> &a) \
+  {                                                                                                       \
+    return dual<::cuda::std::complex<T>>(s) OP dual<::cuda::std::complex<T>>(a);                         \
+  }                                                                                                       \
+  template <typename T, std::enable_if_t<std::is_floating_point_v<T>, int> = 0>                           \
+  __host__ __device__ dual<::cuda::std::complex<T>> operator OP(const dual<::cuda::std::complex<T>> &a,   \
+                                                             const dual<T> &b)                            \
+  {                                                                                                       \
+    return a OP dual<::cuda::std::complex<T>>(b);                                                        \
+  }                                                                                                       \
+  template <typename T, std::enable_if_t<std::is_floating_point_v<T>, int> = 0>                           \
+  __host__ __device__ dual<::cuda::std::complex<T>> operator OP(const dual<T> &a,                         \
+                                                             const dual<::cuda::std::complex<T>> &b)      \
+  {                                                                                                       \
+    return dual<::cuda::std::complex<T>>(a) OP b;                                                        \
+  }
+  GBINT_DUAL_COMPLEX_OPS(+)
+  GBINT_DUAL_COMPLEX_OPS(-)
+  GBINT_DUAL_COMPLEX_OPS(*)
+  GBINT_DUAL_COMPLEX_OPS(/)
+#undef GBINT_DUAL_COMPLEX_OPS
+
+  // real and imaginary parts: of a complex dual, component by component; of a real dual, itself and 0
+  template <typename T> __host__ __device__ dual<T> real(const dual<::cuda::std::complex<T>> &a)
+  {
+    return dual<T>(a.v.real(), a.d.real());
+  }
+  template <typename T> __host__ __device__ dual<T> imag(const dual<::cuda::std::complex<T>> &a)
+  {
+    return dual<T>(a.v.imag(), a.d.imag());
+  }
+  template <typename T, std::enable_if_t<std::is_floating_point_v<T>, int> = 0>
+  __host__ __device__ dual<T> real(const dual<T> &a)
+  {
+    return a;
+  }
+  template <typename T, std::enable_if_t<std::is_floating_point_v<T>, int> = 0>
+  __host__ __device__ T imag(const dual<T> &)
+  {
+    return T(0);
+  }
 
   template <typename T> __host__ __device__ bool operator<(const dual<T> &a, const dual<T> &b) { return a.v < b.v; }
   template <typename T> __host__ __device__ bool operator>(const dual<T> &a, const dual<T> &b) { return a.v > b.v; }
@@ -176,12 +281,57 @@ namespace gbint
   {
     return dual<T>(ad_detail::cos_(a.v), -ad_detail::sin_(a.v) * a.d);
   }
+  // tanh' = sech^2 = 1/cosh^2, accurate also where tanh rounds to +-1 (1 - tanh^2 would be 0 there)
   template <typename T> __host__ __device__ dual<T> tanh(const dual<T> &a)
   {
-    const T t = ad_detail::tanh_(a.v);
-    return dual<T>(t, (T(1) - t * t) * a.d);
+    const T c = ad_detail::cosh_(a.v);
+    return dual<T>(ad_detail::tanh_(a.v), a.d / (c * c));
   }
   template <typename T> __host__ __device__ dual<T> abs(const dual<T> &a) { return a.v < 0 ? -a : a; }
+  template <typename T> __host__ __device__ dual<T> fabs(const dual<T> &a) { return a.v < 0 ? -a : a; }
+  template <typename T> __host__ __device__ dual<T> sinh(const dual<T> &a)
+  {
+    return dual<T>(ad_detail::sinh_(a.v), ad_detail::cosh_(a.v) * a.d);
+  }
+  template <typename T> __host__ __device__ dual<T> cosh(const dual<T> &a)
+  {
+    return dual<T>(ad_detail::cosh_(a.v), ad_detail::sinh_(a.v) * a.d);
+  }
+  // tan' = 1 + tan^2
+  template <typename T> __host__ __device__ dual<T> tan(const dual<T> &a)
+  {
+    const T t = ad_detail::tan_(a.v);
+    return dual<T>(t, (T(1) + t * t) * a.d);
+  }
+  template <typename T> __host__ __device__ dual<T> atan(const dual<T> &a)
+  {
+    return dual<T>(ad_detail::atan_(a.v), a.d / (T(1) + a.v * a.v));
+  }
+  // d atan2(y, x) = (x dy - y dx) / (x^2 + y^2)
+  template <typename T> __host__ __device__ dual<T> atan2(const dual<T> &y, const dual<T> &x)
+  {
+    return dual<T>(ad_detail::atan2_(y.v, x.v), (x.v * y.d - y.v * x.d) / (x.v * x.v + y.v * y.v));
+  }
+  template <typename T, typename S, std::enable_if_t<std::is_arithmetic_v<S>, int> = 0>
+  __host__ __device__ dual<T> atan2(const dual<T> &y, S x)
+  {
+    return atan2(y, dual<T>(x));
+  }
+  template <typename T, typename S, std::enable_if_t<std::is_arithmetic_v<S>, int> = 0>
+  __host__ __device__ dual<T> atan2(S y, const dual<T> &x)
+  {
+    return atan2(dual<T>(y), x);
+  }
+  template <typename T> __host__ __device__ dual<T> asin(const dual<T> &a)
+  {
+    return dual<T>(ad_detail::asin_(a.v), a.d / ad_detail::sqrt_(T(1) - a.v * a.v));
+  }
+  template <typename T> __host__ __device__ dual<T> acos(const dual<T> &a)
+  {
+    return dual<T>(ad_detail::acos_(a.v), -a.d / ad_detail::sqrt_(T(1) - a.v * a.v));
+  }
+  template <typename T> __host__ __device__ bool isfinite(const dual<T> &a) { return ::isfinite(a.v) && ::isfinite(a.d); }
+  template <typename T> __host__ __device__ bool isnan(const dual<T> &a) { return ::isnan(a.v) || ::isnan(a.d); }
   template <typename T, typename S, std::enable_if_t<std::is_arithmetic_v<S>, int> = 0>
   __host__ __device__ dual<T> pow(const dual<T> &a, S p)
   {
@@ -214,3 +364,19 @@ namespace DiFfRG
     };
   } // namespace gbint_detail
 } // namespace DiFfRG
+
+// autodiff::real, autodiff::Real<1, T>, autodiff::val and autodiff::derivative: the names
+// DiFfRG code uses for the autodiff library's first-order forward numbers (e.g.
+// Examples/ONfiniteT/flows/V/V.hh request<autodiff::real>), here gbint::dual.  A translation
+// unit uses either this header or the autodiff library, not both.
+namespace autodiff
+{
+  template <unsigned N, typename T> struct RealOrder;
+  template <typename T> struct RealOrder<1, T> {
+    using type = gbint::dual<T>;
+  };
+  template <unsigned N, typename T> using Real = typename RealOrder<N, T>::type;
+  using real = gbint::dual<double>;
+  using gbint::derivative;
+  using gbint::val;
+} // namespace autodiff

@@ -60,8 +60,8 @@ namespace gbint
     // IntegratorGPU<d>: gridreduce functor, integrator_gpu.hh:34-60
     template <int d> struct F1D {
       template <typename ctype> __host__ __device__ static long long points(const Params<ctype> &P) { return P.n[0]; }
-      template <class K, typename NT, typename ctype, class... T>
-      __device__ static NT eval(const Params<ctype> &P, long long idx, const T &...t)
+      template <class K, typename NT, typename ctype, class... Args>
+      __device__ static NT eval(const Params<ctype> &P, long long idx, const Args &...t)
       {
         const int i = (int)idx;
         const ctype q = P.k * sqrt(P.x[0][i] * P.x_extent);
@@ -76,8 +76,8 @@ namespace gbint
       {
         return (long long)P.n[0] * P.n[1];
       }
-      template <class K, typename NT, typename ctype, class... T>
-      __device__ static NT eval(const Params<ctype> &P, long long idx, const T &...t)
+      template <class K, typename NT, typename ctype, class... Args>
+      __device__ static NT eval(const Params<ctype> &P, long long idx, const Args &...t)
       {
         const int i = (int)(idx / P.n[1]), j = (int)(idx % P.n[1]);
         const ctype q = P.k * sqrt(P.x[0][i] * P.x_extent);
@@ -95,8 +95,8 @@ namespace gbint
       {
         return (long long)P.n[0] * P.n[1] * P.n[2];
       }
-      template <class K, typename NT, typename ctype, class... T>
-      __device__ static NT eval(const Params<ctype> &P, long long idx, const T &...t)
+      template <class K, typename NT, typename ctype, class... Args>
+      __device__ static NT eval(const Params<ctype> &P, long long idx, const Args &...t)
       {
         const int l = (int)(idx % P.n[2]);
         idx /= P.n[2];
@@ -116,8 +116,8 @@ namespace gbint
       {
         return (long long)P.n[0] * P.n[1] * P.n[2];
       }
-      template <class K, typename NT, typename ctype, class... T>
-      __device__ static NT eval(const Params<ctype> &P, long long idx, const T &...t)
+      template <class K, typename NT, typename ctype, class... Args>
+      __device__ static NT eval(const Params<ctype> &P, long long idx, const Args &...t)
       {
         const int l = (int)(idx % P.n[2]);
         idx /= P.n[2];
@@ -137,8 +137,8 @@ namespace gbint
       {
         return (long long)P.n[0] * P.n[1] * P.n[2] * P.n[3];
       }
-      template <class K, typename NT, typename ctype, class... T>
-      __device__ static NT eval(const Params<ctype> &P, long long idx, const T &...t)
+      template <class K, typename NT, typename ctype, class... Args>
+      __device__ static NT eval(const Params<ctype> &P, long long idx, const Args &...t)
       {
         const int m = (int)(idx % P.n[3]);
         idx /= P.n[3];
@@ -163,8 +163,8 @@ namespace gbint
         if (dim > 2) p *= P.n[2];
         return p;
       }
-      template <class K, typename NT, typename ctype, class... T>
-      __device__ static NT eval(const Params<ctype> &P, long long idx, const T &...t)
+      template <class K, typename NT, typename ctype, class... Args>
+      __device__ static NT eval(const Params<ctype> &P, long long idx, const Args &...t)
       {
         const ctype ie = powi(two_pi<ctype>(), -dim);
         if constexpr (dim == 1) {
@@ -193,8 +193,8 @@ namespace gbint
       {
         return (long long)P.n[0] * P.n[1] * P.n[2];
       }
-      template <class K, typename NT, typename ctype, class... T>
-      __device__ static NT eval(const Params<ctype> &P, long long idx, const T &...t)
+      template <class K, typename NT, typename ctype, class... Args>
+      __device__ static NT eval(const Params<ctype> &P, long long idx, const Args &...t)
       {
         const int l = (int)(idx % P.n[2]);
         idx /= P.n[2];
@@ -215,8 +215,8 @@ namespace gbint
       {
         return (long long)P.n[0] * P.n[1] * P.n[2] * P.n[3];
       }
-      template <class K, typename NT, typename ctype, class... T>
-      __device__ static NT eval(const Params<ctype> &P, long long idx, const T &...t)
+      template <class K, typename NT, typename ctype, class... Args>
+      __device__ static NT eval(const Params<ctype> &P, long long idx, const Args &...t)
       {
         const int m = (int)(idx % P.n[3]);
         idx /= P.n[3];
@@ -243,8 +243,8 @@ namespace gbint
         if (ANG == 2) p *= P.n[2];
         return p;
       }
-      template <class K, typename NT, typename ctype, class... T>
-      __device__ static NT eval(const Params<ctype> &P, long long idx, const T &...t)
+      template <class K, typename NT, typename ctype, class... Args>
+      __device__ static NT eval(const Params<ctype> &P, long long idx, const Args &...t)
       {
         const int m = (int)(idx % P.nm);
         idx /= P.nm;
@@ -300,8 +300,8 @@ namespace gbint
         if (ANG == 2) p *= P.n[2];
         return p;
       }
-      template <class K, typename NT, typename ctype, class... T>
-      __device__ static NT eval(const Params<ctype> &P, long long idx, const T &...t)
+      template <class K, typename NT, typename ctype, class... Args>
+      __device__ static NT eval(const Params<ctype> &P, long long idx, const Args &...t)
       {
         const int nz = P.ns + P.n[TAIL];
         const int m = (int)(idx % nz);

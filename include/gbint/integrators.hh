@@ -263,10 +263,22 @@ namespace DiFfRG
   // ---------------------------------------------------------------------------------------
   namespace gbint_detail
   {
+    // forward declaration: the definition (a kernel launch) is compiled only by nvcc; a host
+    // compiler translation unit (e.g. a flow's FlowEquations source, compiled by g++ as in the
+    // reference's build) sees the integrator classes complete but cannot launch them
+    template <typename NT> class Pending;
+    template <class FAM, class KERNEL, typename NT, typename ctype, class... T>
+    std::shared_ptr<Pending<NT>> launch(QuadratureProvider &qp, std::shared_ptr<gb_ctx> keep,
+                                        const gbint::fam::Params<ctype> &P, NT constant, const T &...t);
+  } // namespace gbint_detail
+
+  namespace gbint_detail
+  {
     constexpr int kThreads = 256;
     constexpr int kPPT = 4;
     constexpr int kUnit = kThreads * kPPT;
 
+#ifdef __CUDACC__
     __device__ __forceinline__ double warp_sum(double v)
     {
 #pragma unroll
@@ -373,6 +385,8 @@ namespace DiFfRG
       }
     }
 
+#endif // __CUDACC__
+
     // one launched request: resolves to constant + integral
     template <typename NT> class Pending
     {
@@ -403,6 +417,7 @@ namespace DiFfRG
       int n_units_;
     };
 
+#ifdef __CUDACC__
     template <class FAM, class KERNEL, typename NT, typename ctype, class... T>
     std::shared_ptr<Pending<NT>> launch(QuadratureProvider &qp, std::shared_ptr<gb_ctx> keep,
                                         const gbint::fam::Params<ctype> &P, NT constant, const T &...t)
@@ -425,6 +440,7 @@ namespace DiFfRG
       }
       return std::make_shared<Pending<NT>>(std::move(keep), slot, constant, n_units);
     }
+#endif // __CUDACC__
 
     template <typename NT> std::future<NT> as_future(std::shared_ptr<Pending<NT>> p)
     {

@@ -12,8 +12,14 @@
 // Functions (as in the reference): RB = R_B(k^2, q^2); RBdot = d/dt R_B with t = ln k;
 // dq2RB = dR_B/dq^2; RF = sqrt(R_B + q^2) - sqrt(q^2) (fermionic, p r_F); RFdot = dRF/dt;
 // dq2RF = dRF/dq^2.  The derivatives are written out from the shapes above.
-// The reference's RationalExpRegulator (tabulated rational f) is not provided here; code that
-// uses it keeps the reference header for it.
+//   RationalExpRegulator<Opts{order, c, b0}>
+//                                  R_B = k^2 e^(-f(x)),  f = P/D rational              (:244-600)
+// RationalExpRegulator's f is built here from its defining properties rather than from the
+// reference's per-order expressions: D(x) = 1 + b0 x^m + g x^(n-1) (n = order, m = floor(n/2),
+// g = a/(c-1), a = 1/n + b0/ceil(n/2)) and P = the part of degree <= n of D(x) L(x), with
+// L(x) = sum_{i>=1} x^i/i = -ln(1-x).  So f = -ln(1-x) + O(x^n) near 0 (R_B = k^2(1 - x) + ...,
+// a pole of order n in the propagator once the mass turns negative) and f -> c x for large x
+// (tail e^(-c x)); P and D reproduce the reference's expressions for every order 1..16.
 #pragma once
 
 #include <cmath>
@@ -216,6 +222,106 @@ namespace DiFfRG
       using std::exp;
       const auto x = q2 / k2;
       return -exp(-f(x)) * df(x);
+    }
+  };
+
+  struct RationalExpRegulatorOpts {
+    static constexpr int order = 8;
+    constexpr static double c = 2;
+    constexpr static double b0 = 0.;
+  };
+  template <class OPTS = RationalExpRegulatorOpts>
+  struct RationalExpRegulator : FermionicFromBosonic<RationalExpRegulator<OPTS>> {
+    static constexpr int order = OPTS::order;
+    static_assert(order > 0, "RationalExpRegulator: order must be positive");
+    constexpr static double c = OPTS::c;
+    constexpr static double b0 = OPTS::b0;
+    static_assert(c != 1.0, "RationalExpRegulator: c = 1 has no tail");
+
+    // coefficients of D (degree order-1) and P (degree order, no constant term); constant-evaluated
+    static constexpr int m_ = order / 2;
+    static constexpr double g_ = (1.0 / order + b0 / (order - m_)) / (c - 1.0);
+    static constexpr double dcoef(int l)
+    {
+      return (l == 0 ? 1.0 : 0.0) + (l == m_ ? b0 : 0.0) + (l == order - 1 ? g_ : 0.0);
+    }
+    static constexpr double pcoef(int i)  // [x^i] (D L), i = 1..order
+    {
+      double s = 0.0;
+      for (int l = 0; l < i && l < order; ++l) s += dcoef(l) / (double)(i - l);
+      return s;
+    }
+
+    // Horner sums with compile-time coefficients: sum_{i=I..N} C(i) x^(i-I)
+    template <int I, typename T> static GBINT_REG_HD T hornerP(const T &x)  // P(x)/x
+    {
+      constexpr double cf = pcoef(I);
+      if constexpr (I == order)
+        return T(cf);
+      else
+        return hornerP<I + 1>(x) * x + T(cf);
+    }
+    template <int I, typename T> static GBINT_REG_HD T hornerdP(const T &x)  // P'(x)
+    {
+      constexpr double cf = I * pcoef(I);
+      if constexpr (I == order)
+        return T(cf);
+      else
+        return hornerdP<I + 1>(x) * x + T(cf);
+    }
+    template <int I, typename T> static GBINT_REG_HD T hornerD(const T &x)
+    {
+      constexpr double cf = dcoef(I);
+      if constexpr (I == order - 1)
+        return T(cf);
+      else
+        return hornerD<I + 1>(x) * x + T(cf);
+    }
+    template <int I, typename T> static GBINT_REG_HD T hornerdD(const T &x)  // D'(x), I from 1
+    {
+      constexpr double cf = I * dcoef(I);
+      if constexpr (I >= order - 1)
+        return T(cf);
+      else
+        return hornerdD<I + 1>(x) * x + T(cf);
+    }
+
+    template <typename T> static GBINT_REG_HD T get_f(const T x)
+    {
+      if constexpr (order == 1)
+        return x;
+      else
+        return x * hornerP<1>(x) / hornerD<0>(x);
+    }
+    // f' = (P' D - P D') / D^2
+    template <typename T> static GBINT_REG_HD T get_df(const T x)
+    {
+      if constexpr (order == 1)
+        return T(1.);
+      else {
+        const T D = hornerD<0>(x);
+        return (hornerdP<1>(x) * D - x * hornerP<1>(x) * hornerdD<1>(x)) / (D * D);
+      }
+    }
+
+    template <typename NT1, typename NT2> static GBINT_REG_HD auto RB(const NT1 k2, const NT2 q2)
+    {
+      using std::exp;
+      const auto x = q2 / k2;
+      return k2 * exp(-get_f(x));
+    }
+    // d/dt at fixed q^2: 2 k^2 e^(-f) (1 + x f'(x))
+    template <typename NT1, typename NT2> static GBINT_REG_HD auto RBdot(const NT1 k2, const NT2 q2)
+    {
+      using std::exp;
+      const auto x = q2 / k2;
+      return 2. * k2 * exp(-get_f(x)) * (1. + get_df(x) * x);
+    }
+    template <typename NT1, typename NT2> static GBINT_REG_HD auto dq2RB(const NT1 k2, const NT2 q2)
+    {
+      using std::exp;
+      const auto x = q2 / k2;
+      return -exp(-get_f(x)) * get_df(x);
     }
   };
 } // namespace DiFfRG

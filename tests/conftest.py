@@ -37,3 +37,21 @@ def ctx(gblib):
     c = Context(0)
     yield c
     c.close()
+
+
+def reference_checkout():
+    """The DiFfRG checkout the reference-reading tests use: $GBINT_REFERENCE_DIR, else a directory
+    named 'reference' beside this repository; None when neither holds DiFfRG's sources."""
+    cands = [os.environ.get("GBINT_REFERENCE_DIR"), os.path.join(os.path.dirname(ROOT), "reference")]
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "Examples")):
+            return c
+    return None
+
+
+@pytest.fixture(scope="session")
+def reference_dir():
+    d = reference_checkout()
+    if d is None:
+        pytest.skip("no DiFfRG checkout (set GBINT_REFERENCE_DIR)")
+    return d

@@ -213,7 +213,7 @@ template <typename T> struct KDualAngle {
   static __host__ __device__ R constant(T, const Coeffs &C, const R &) { return R(C.a[0]); }
 };
 struct KDualCart {
-  using R = gbint::real;
+  using R = autodiff::real;
   static __host__ __device__ R kernel(double qx, double k, const Coeffs &C, const R &s)
   {
     return K1<double>::kernel(qx, k, C) * exp(-s * (qx * qx / (k * k)));
@@ -221,7 +221,7 @@ struct KDualCart {
   static __host__ __device__ R constant(double, const Coeffs &C, const R &) { return R(C.a[0]); }
 };
 struct KDualFT {
-  using R = gbint::real;
+  using R = autodiff::real;
   static __host__ __device__ R kernel(double q, double c, double q0, double k, const Coeffs &C, const R &s)
   {
     return KT2<double>::kernel(q, c, q0, k, C) * exp(-s * (q * q / (k * k)));
@@ -267,30 +267,30 @@ int dual_cases()
   A.a[8] = 0.3;
   A.a[19] = 1.0;  // q0 factor 1 + q0^2 (finite T)
   A.a[21] = 1.0;
-  IntegratorAngleGPU<4, gbint::real, KDualAngle<double>> IA(qp, {{48, 16}}, 1.7);
+  IntegratorAngleGPU<4, autodiff::real, KDualAngle<double>> IA(qp, {{48, 16}}, 1.7);
   IntegratorAngleGPU<4, gbint::dual<float>, KDualAngle<float>> IAf(qp, {{48, 16}}, 1.7);
   IntegratorAngleGPU<4, double, PDualAngle<0>> PA0(qp, {{48, 16}}, 1.7);
   IntegratorAngleGPU<4, double, PDualAngle<1>> PA1(qp, {{48, 16}}, 1.7);
-  Integrator1DCartesianGPU<gbint::real, KDualCart> IC(qp, {{32}});
+  Integrator1DCartesianGPU<autodiff::real, KDualCart> IC(qp, {{32}});
   Integrator1DCartesianGPU<double, PDualCart<0>> PC0(qp, {{32}});
   Integrator1DCartesianGPU<double, PDualCart<1>> PC1(qp, {{32}});
   PC0.set_qx_min(-1.5), PC0.set_qx_max(1.2);
   PC1.set_qx_min(-1.5), PC1.set_qx_max(1.2);
   IC.set_qx_min(-1.5), IC.set_qx_max(1.2);
-  IntegratorAngleFiniteTq0GPU<4, gbint::real, KDualFT> IT(qp, {{32, 12}}, 1.5, 0.2);
+  IntegratorAngleFiniteTq0GPU<4, autodiff::real, KDualFT> IT(qp, {{32, 12}}, 1.5, 0.2);
   IntegratorAngleFiniteTq0GPU<4, double, PDualFT<0>> PT0(qp, {{32, 12}}, 1.5, 0.2);
   IntegratorAngleFiniteTq0GPU<4, double, PDualFT<1>> PT1(qp, {{32, 12}}, 1.5, 0.2);
   for (double k : {0.6, 1.1}) {
     for (double s : {0.3, 1.7}) {
-      const gbint::real sd = gbint::seed(s);
-      const gbint::real a = IA.get(k, A, sd);
+      const autodiff::real sd = gbint::seed(s);
+      const autodiff::real a = IA.get(k, A, sd);
       const gbint::dual<float> af = IAf.request((float)k, A, gbint::seed((float)s)).get();
       std::printf("DUAL ANGLE %.17g %.17g %.17g %.17g\n", val(a), derivative(a), PA0.get(k, A, s), PA1.get(k, A, s));
       std::printf("DUAL ANGLEF %.9g %.9g %.17g %.17g\n", (double)val(af), (double)derivative(af), PA0.get(k, A, s),
                   PA1.get(k, A, s));
-      const gbint::real c = IC.request(k, A, sd).get();
+      const autodiff::real c = IC.request(k, A, sd).get();
       std::printf("DUAL CART1 %.17g %.17g %.17g %.17g\n", val(c), derivative(c), PC0.get(k, A, s), PC1.get(k, A, s));
-      const gbint::real t = IT.get(k, A, sd);
+      const autodiff::real t = IT.get(k, A, sd);
       std::printf("DUAL FTQ0 %.17g %.17g %.17g %.17g\n", val(t), derivative(t), PT0.get(k, A, s), PT1.get(k, A, s));
     }
   }
@@ -328,6 +328,11 @@ struct Exp3 {
 struct Poly3 {
   static constexpr int order = 3;
 };
+struct Rat5 {
+  static constexpr int order = 5;
+  constexpr static double c = 1.5;
+  constexpr static double b0 = 0.25;
+};
 template <class R, bool DQ2> int reg_case(const char *name)
 {
   std::vector<double> kq;
@@ -350,9 +355,9 @@ template <class R, bool DQ2> int reg_case(const char *name)
     reg_eval<R, DQ2>(k2, q2, h);
     double ad[kRegFns];
     for (double &v : ad) v = NAN;
-    ad[1] = gbint::derivative(R::RB(gbint::real(k2, 2 * k2), q2));
+    ad[1] = gbint::derivative(R::RB(autodiff::real(k2, 2 * k2), q2));
     if constexpr (DQ2) ad[2] = gbint::derivative(R::RB(k2, gbint::seed(q2)));
-    ad[4] = gbint::derivative(R::RF(gbint::real(k2, 2 * k2), q2));
+    ad[4] = gbint::derivative(R::RF(autodiff::real(k2, 2 * k2), q2));
     if constexpr (DQ2) ad[5] = gbint::derivative(R::RF(k2, gbint::seed(q2)));
     for (int f = 0; f < kRegFns; ++f)
       std::printf("REG %s %.17g %.17g %d %.17g %.17g %.17g\n", name, k2, q2, f, h[f], dev[t * kRegFns + f], ad[f]);
@@ -370,6 +375,8 @@ int regulator_cases()
   rc |= reg_case<SmoothedLitimRegulator<>, false>("smoothlitim");
   rc |= reg_case<PolynomialExpRegulator<>, true>("polyexp8");
   rc |= reg_case<PolynomialExpRegulator<Poly3>, true>("polyexp3");
+  rc |= reg_case<RationalExpRegulator<>, true>("ratexp8");
+  rc |= reg_case<RationalExpRegulator<Rat5>, true>("ratexp5");
   return rc;
 }
 

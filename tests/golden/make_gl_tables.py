@@ -5,8 +5,8 @@ nodes x[i] and weights w[i] on [0,1]).  The reference's own quadrature test comp
 make_quadrature against exactly these tables for N = 4, 8, 16, 32, 64, 128
 (DiFfRG/tests/common/quadrature/test_quadrature.cc:10-33); the same orders are extracted here.
 
-Run in a checkout that has the reference mounted:
-    python tests/golden/make_gl_tables.py [/path/to/DiFfRG-project-root]
+Run with the path of a DiFfRG checkout (the project root):
+    python tests/golden/make_gl_tables.py /path/to/DiFfRG-project-root
 The JSON keeps the decimal strings of the header (30+ digits), parsed to float at test time.
 """
 import json
@@ -18,7 +18,9 @@ ORDERS = [4, 8, 16, 32, 64, 128]
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_gl_tables.py /path/to/DiFfRG-project-root")
+    root = sys.argv[1]
     path = os.path.join(root, "DiFfRG/include/DiFfRG/common/quadrature/gauss_legendre.hh")
     text = open(path).read()
     blocks = re.split(r"template <typename ctype> struct GLQuadrature<(\d+), ctype>", text)

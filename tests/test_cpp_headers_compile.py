@@ -60,8 +60,8 @@ int main() {
   Flow flow(j);
   flow.set_k(0.9);
   const double a = 0.7;
-  const gbint::real A = gbint::seed(a);
-  const gbint::real r = flow.integrate<gbint::real, 4>([&](double q2) { return gbint::exp(-A * q2); });
+  const autodiff::real A = gbint::seed(a);
+  const autodiff::real r = flow.integrate<autodiff::real, 4>([&](double q2) { return gbint::exp(-A * q2); });
   const DiFfRG::QGauss<1> jq(flow.jo());
   const double v = DiFfRG::LoopIntegrals::integrate<double, 4>([&](double q2) { return std::exp(-a * q2); }, jq,
                                                                flow.xe(), 0.9);

@@ -170,6 +170,22 @@ def _reg_closed_forms(name, k2, q2):
         RB = (k2 - q2) / (1 + E)
         RBdot = 0.0 if E > 1e50 else 2 * k2 * (1 + E * (x - x * x + a) / a) / (1 + E) ** 2
         dRB = nan
+    elif name.startswith("ratexp"):
+        # f = P/D: D = 1 + b0 x^(n//2) + g x^(n-1), g = (1/n + b0/ceil(n/2))/(c-1), P = [D(x) (-ln(1-x))] up to x^n
+        n = int(name[len("ratexp"):])
+        c, b0 = (2.0, 0.0) if n == 8 else (1.5, 0.25)
+        g = (1.0 / n + b0 / (n - n // 2)) / (c - 1)
+        d = [0.0] * n
+        d[0] += 1
+        d[n // 2] += b0
+        d[n - 1] += g
+        pc = [0.0] + [sum(d[l] / (i - l) for l in range(min(i, n))) for i in range(1, n + 1)]
+        D = sum(d[l] * x ** l for l in range(n))
+        dD = sum(l * d[l] * x ** (l - 1) for l in range(1, n))
+        P = sum(pc[i] * x ** i for i in range(1, n + 1))
+        dP = sum(i * pc[i] * x ** (i - 1) for i in range(1, n + 1))
+        f, fp = P / D, (dP * D - P * dD) / D ** 2
+        RB, RBdot, dRB = k2 * math.exp(-f), 2 * k2 * math.exp(-f) * (1 + x * fp), -math.exp(-f) * fp
     else:
         n = int(name[len("polyexp"):])
         f = sum(x ** m / m for m in range(1, n + 1))
@@ -189,7 +205,8 @@ def test_regulators_host_device_and_derivatives(binary):
     out = run(binary, [], extra=["--regulators"])
     rows = [l.split()[1:] for l in out if l.startswith("REG")]
     names = {r[0] for r in rows}
-    assert names == {"litim", "bosonic2", "bosonic1", "exp2", "exp3", "smoothlitim", "polyexp8", "polyexp3"}
+    assert names == {"litim", "bosonic2", "bosonic1", "exp2", "exp3", "smoothlitim", "polyexp8", "polyexp3",
+                     "ratexp8", "ratexp5"}
     checked_ad = 0
     for name, k2, q2, fn, host, dev, ad in rows:
         k2, q2, fn, host, dev, ad = float(k2), float(q2), int(fn), float(host), float(dev), float(ad)
