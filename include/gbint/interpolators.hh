@@ -16,7 +16,9 @@
 // (bi-/trilinearly in 2D/3D), on the host and on the device alike.  The Tex* variants keep the
 // reference's FP32 data but interpolate exactly (the reference's texture filter has an 8-bit
 // fraction, ~1e-3 relative, DiFfRG/tests/physics/interpolation/tex_linear_interpolation_1D_gpu.cu:55-57)
-// and return NT instead of float.  Device data lives in buffers of the process-wide
+// and return NT instead of float; for double-based NT the coordinate map and the interpolation
+// run in double (the reference maps in the coordinates' float type), so that the host and the
+// device interpolate alike to FP64 rounding.  Device data lives in buffers of the process-wide
 // interpolator context until process exit; update() copies the host data in place after the
 // device drained, as the reference's update() synchronises.
 #pragma once
@@ -31,8 +33,14 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <cuda/std/complex>
 
 #include "gbint.h"
+
+namespace gbint
+{
+  template <typename T> struct dual;
+}
 
 // Coordinates return std::array / std::tuple from __host__ __device__ members, as the
 // reference's do; nvcc needs --expt-relaxed-constexpr for that (DiFfRG's own build passes it,
@@ -71,35 +79,36 @@ namespace DiFfRG
     NT a;
   };
 
+  // y(i) = start + span (e^(i bias/(n-1)) - 1): n points from start to stop, denser near start
+  // for bias > 0; backward(y) = (n-1)/bias * ln(1 + (y - start)/span) is the (fractional) index.
+  // backward_derivative keeps the reference's expression (n-1)/(bias (y - start)).
   template <typename NT> class LogarithmicCoordinates1D
   {
   public:
     using ctype = NT;
     static constexpr uint dim = 1;
     LogarithmicCoordinates1D(uint grid_extent, NT start_, NT stop_, NT bias_)
-        : start(start_), stop(stop_), bias(bias_), grid_extent(grid_extent), gem1((NT)(grid_extent - 1.)),
-          gem1inv((NT)(1. / (grid_extent - 1.)))
+        : start(start_), stop(stop_), bias(bias_), n_(grid_extent)
     {
-      if (grid_extent == 0) throw std::runtime_error("LogarithmicCoordinates1D: grid_extent must be > 0");
-      a = bias;
-      b = (stop - start) / std::expm1(a);
-      c = start;
+      if (grid_extent == 0) throw std::runtime_error("LogarithmicCoordinates1D: a grid needs at least one point");
+      idx_per_log_ = (NT)((grid_extent - 1.) / bias);
+      log_per_idx_ = (NT)(bias / (grid_extent - 1.));
+      span_ = (stop - start) / std::expm1(bias);
     }
     template <typename NT2>
     LogarithmicCoordinates1D(const LogarithmicCoordinates1D<NT2> &other)
         : LogarithmicCoordinates1D(other.size(), (NT)other.start, (NT)other.stop, (NT)other.bias)
     {
     }
-    __host__ __device__ NT forward(const uint &x) const { return b * expm1(a * x * gem1inv) + c; }
-    __host__ __device__ NT backward(const NT &y) const { return log1p((y - c) / b) * gem1 / a; }
-    __host__ __device__ NT backward_derivative(const NT &y) const { return (NT)1 / (y - c) * gem1 / a; }
-    __host__ __device__ uint size() const { return grid_extent; }
+    __host__ __device__ NT forward(const uint &x) const { return span_ * expm1(log_per_idx_ * x) + start; }
+    __host__ __device__ NT backward(const NT &y) const { return log1p((y - start) / span_) * idx_per_log_; }
+    __host__ __device__ NT backward_derivative(const NT &y) const { return idx_per_log_ / (y - start); }
+    __host__ __device__ uint size() const { return n_; }
     NT start, stop, bias;
 
   private:
-    uint grid_extent;
-    NT gem1, gem1inv;
-    NT a, b, c;
+    uint n_;
+    NT idx_per_log_, log_per_idx_, span_;
   };
 
   // integer stack index and Matsubara frequencies (stack axes of the finite-T coordinates)
@@ -242,6 +251,13 @@ namespace DiFfRG
         : Coordinates1DFiniteT(m_start, m_stop, m_T, lc.size(), (NT)lc.start, (NT)lc.stop, (NT)lc.bias)
     {
     }
+    // the same axes in another precision
+    template <typename NT2>
+    explicit Coordinates1DFiniteT(const Coordinates1DFiniteT<Idx, NT2, FERMIONIC> &o)
+        : Coordinates1DFiniteT((Idx)o.m_start, (Idx)o.m_stop, (NT)o.m_T, o.sizes()[1], (NT)o.p_start, (NT)o.p_stop,
+                               (NT)o.p_bias)
+    {
+    }
     __host__ __device__ std::array<NT, 2> forward(const uint m, const uint p) const
     {
       return {{matsubara_values.forward((Idx)m), logarithmic_coordinates.forward(p)}};
@@ -269,6 +285,64 @@ namespace DiFfRG
   };
   template <typename Idx, typename NT> using BosonicCoordinates1DFiniteT = Coordinates1DFiniteT<Idx, NT, false>;
   template <typename Idx, typename NT> using FermionicCoordinates1DFiniteT = Coordinates1DFiniteT<Idx, NT, true>;
+
+  namespace gbint_detail
+  {
+    // The precision an interpolator maps coordinates and interpolates in: double whenever the
+    // result type is double-based (double, complex<double>, dual<double>), else the coordinates'
+    // own type.  The reference maps in the coordinates' type (float for the usual
+    // LogarithmicCoordinates1D<float>) and filters with 8-bit texture fractions; mapping in double
+    // makes host and device results agree to FP64 rounding.
+    template <typename NT> struct scalar_of {
+      using type = NT;
+    };
+    template <typename T> struct scalar_of<::cuda::std::complex<T>> {
+      using type = typename scalar_of<T>::type;
+    };
+    template <typename T> struct scalar_of<gbint::dual<T>> {
+      using type = typename scalar_of<T>::type;
+    };
+    template <typename NT, typename ctype>
+    using map_precision = std::conditional_t<std::is_same_v<typename scalar_of<NT>::type, double>, double, ctype>;
+
+    // coordinates C with their floating-point type replaced by W (others unchanged)
+    template <class C, typename W> struct at_precision {
+      using type = C;
+      static const C &make(const C &c) { return c; }
+    };
+    template <typename T, typename W> struct at_precision<LinearCoordinates1D<T>, W> {
+      using type = LinearCoordinates1D<W>;
+      static type make(const LinearCoordinates1D<T> &c) { return type(c); }
+    };
+    template <typename T, typename W> struct at_precision<LogarithmicCoordinates1D<T>, W> {
+      using type = LogarithmicCoordinates1D<W>;
+      static type make(const LogarithmicCoordinates1D<T> &c) { return type(c); }
+    };
+    template <typename Idx, typename T, bool F, typename W> struct at_precision<Coordinates1DFiniteT<Idx, T, F>, W> {
+      using type = Coordinates1DFiniteT<Idx, W, F>;
+      static type make(const Coordinates1DFiniteT<Idx, T, F> &c) { return type(c); }
+    };
+    template <class C0, typename W> struct at_precision<CoordinatePackND<C0>, W> {
+      using type = CoordinatePackND<typename at_precision<C0, W>::type>;
+      static type make(const CoordinatePackND<C0> &c) { return type(at_precision<C0, W>::make(c.c0)); }
+    };
+    template <class C0, class C1, typename W> struct at_precision<CoordinatePackND<C0, C1>, W> {
+      using type = CoordinatePackND<typename at_precision<C0, W>::type, typename at_precision<C1, W>::type>;
+      static type make(const CoordinatePackND<C0, C1> &c)
+      {
+        return type(at_precision<C0, W>::make(c.c0), at_precision<C1, W>::make(c.c1));
+      }
+    };
+    template <class C0, class C1, class C2, typename W> struct at_precision<CoordinatePackND<C0, C1, C2>, W> {
+      using type = CoordinatePackND<typename at_precision<C0, W>::type, typename at_precision<C1, W>::type,
+                                    typename at_precision<C2, W>::type>;
+      static type make(const CoordinatePackND<C0, C1, C2> &c)
+      {
+        return type(at_precision<C0, W>::make(c.c0), at_precision<C1, W>::make(c.c1),
+                    at_precision<C2, W>::make(c.c2));
+      }
+    };
+  } // namespace gbint_detail
 
   namespace gbint_detail
   {
@@ -360,7 +434,7 @@ namespace DiFfRG
     DT *data() const { return store_->host.data(); }
     const Coordinates &get_coordinates() const { return coordinates; }
 
-    __host__ __device__ NT operator()(const ctype x) const
+    template <typename X> __host__ __device__ NT operator()(const X x) const
     {
 #ifdef __CUDA_ARCH__
       const DT *d = d_data_;
@@ -368,14 +442,17 @@ namespace DiFfRG
       const DT *d = h_data_;
 #endif
       uint i;
-      ctype f;
-      gbint_detail::cell<ctype>(coordinates.backward(x), size, i, f);
+      W f;
+      gbint_detail::cell<W>(coords_w.backward((W)x), size, i, f);
       if (size < 2) return (NT)d[0];
-      return (NT)((ctype)d[i] + f * ((ctype)d[i + 1] - (ctype)d[i]));
+      return (NT)((W)d[i] + f * ((W)d[i + 1] - (W)d[i]));
     }
 
   protected:
+    using W = gbint_detail::map_precision<NT, ctype>;
     Coordinates coordinates;
+    typename gbint_detail::at_precision<Coordinates, W>::type coords_w =
+        gbint_detail::at_precision<Coordinates, W>::make(coordinates);
     uint size;
     gbint_detail::Store<DT> *store_;
     const DT *h_data_;
@@ -417,27 +494,30 @@ namespace DiFfRG
     DT *data() const { return store_->host.data(); }
     const Coordinates &get_coordinates() const { return coordinates; }
 
-    __host__ __device__ NT operator()(const ctype x, const ctype y) const
+    template <typename X, typename Y> __host__ __device__ NT operator()(const X x, const Y y) const
     {
 #ifdef __CUDA_ARCH__
       const DT *d = d_data_;
 #else
       const DT *d = h_data_;
 #endif
-      const auto idx = coordinates.backward(x, y);
+      const auto idx = coords_w.backward((W)x, (W)y);
       uint i, j;
-      ctype fx, fy;
-      gbint_detail::cell<ctype>(idx[0], n0, i, fx);
-      gbint_detail::cell<ctype>(idx[1], n1, j, fy);
+      W fx, fy;
+      gbint_detail::cell<W>(idx[0], n0, i, fx);
+      gbint_detail::cell<W>(idx[1], n1, j, fy);
       const uint i1 = n0 > 1 ? i + 1 : i, j1 = n1 > 1 ? j + 1 : j;
-      const ctype y00 = d[(size_t)i * n1 + j], y10 = d[(size_t)i1 * n1 + j];
-      const ctype y01 = d[(size_t)i * n1 + j1], y11 = d[(size_t)i1 * n1 + j1];
-      const ctype lo = y00 + fx * (y10 - y00), hi = y01 + fx * (y11 - y01);
+      const W y00 = d[(size_t)i * n1 + j], y10 = d[(size_t)i1 * n1 + j];
+      const W y01 = d[(size_t)i * n1 + j1], y11 = d[(size_t)i1 * n1 + j1];
+      const W lo = y00 + fx * (y10 - y00), hi = y01 + fx * (y11 - y01);
       return (NT)(lo + fy * (hi - lo));
     }
 
   protected:
+    using W = gbint_detail::map_precision<NT, ctype>;
     Coordinates coordinates;
+    typename gbint_detail::at_precision<Coordinates, W>::type coords_w =
+        gbint_detail::at_precision<Coordinates, W>::make(coordinates);
     uint n0, n1;
     gbint_detail::Store<DT> *store_;
     const DT *h_data_;
@@ -479,32 +559,35 @@ namespace DiFfRG
     DT *data() const { return store_->host.data(); }
     const Coordinates &get_coordinates() const { return coordinates; }
 
-    __host__ __device__ NT operator()(const ctype x, const ctype y, const ctype z) const
+    template <typename X, typename Y, typename Z> __host__ __device__ NT operator()(const X x, const Y y, const Z z) const
     {
 #ifdef __CUDA_ARCH__
       const DT *d = d_data_;
 #else
       const DT *d = h_data_;
 #endif
-      const auto idx = coordinates.backward(x, y, z);
+      const auto idx = coords_w.backward((W)x, (W)y, (W)z);
       uint i, j, l;
-      ctype fx, fy, fz;
-      gbint_detail::cell<ctype>(idx[0], n0, i, fx);
-      gbint_detail::cell<ctype>(idx[1], n1, j, fy);
-      gbint_detail::cell<ctype>(idx[2], n2, l, fz);
+      W fx, fy, fz;
+      gbint_detail::cell<W>(idx[0], n0, i, fx);
+      gbint_detail::cell<W>(idx[1], n1, j, fy);
+      gbint_detail::cell<W>(idx[2], n2, l, fz);
       const uint i1 = n0 > 1 ? i + 1 : i, j1 = n1 > 1 ? j + 1 : j, l1 = n2 > 1 ? l + 1 : l;
-      auto at = [&](uint a, uint b, uint c) -> ctype { return (ctype)d[((size_t)a * n1 + b) * n2 + c]; };
-      auto lx = [&](uint b, uint c) -> ctype {
-        const ctype v0 = at(i, b, c);
+      auto at = [&](uint a, uint b, uint c) -> W { return (W)d[((size_t)a * n1 + b) * n2 + c]; };
+      auto lx = [&](uint b, uint c) -> W {
+        const W v0 = at(i, b, c);
         return v0 + fx * (at(i1, b, c) - v0);
       };
-      const ctype c00 = lx(j, l), c10 = lx(j1, l), c01 = lx(j, l1), c11 = lx(j1, l1);
-      const ctype c0 = c00 + fy * (c10 - c00), c1 = c01 + fy * (c11 - c01);
+      const W c00 = lx(j, l), c10 = lx(j1, l), c01 = lx(j, l1), c11 = lx(j1, l1);
+      const W c0 = c00 + fy * (c10 - c00), c1 = c01 + fy * (c11 - c01);
       return (NT)(c0 + fz * (c1 - c0));
     }
 
   protected:
+    using W = gbint_detail::map_precision<NT, ctype>;
     Coordinates coordinates;
+    typename gbint_detail::at_precision<Coordinates, W>::type coords_w =
+        gbint_detail::at_precision<Coordinates, W>::make(coordinates);
     uint n0, n1, n2;
     gbint_detail::Store<DT> *store_;
     const DT *h_data_;
@@ -560,26 +643,29 @@ namespace DiFfRG
     const float &operator[](const uint i) const { return store_->host[i]; }
     const Coordinates &get_coordinates() const { return coordinates; }
 
-    __host__ __device__ NT operator()(const ctype m, const ctype p) const
+    template <typename M, typename P> __host__ __device__ NT operator()(const M m, const P p) const
     {
 #ifdef __CUDA_ARCH__
       const float *d = d_data_;
 #else
       const float *d = h_data_;
 #endif
-      const auto mp = coordinates.backward(m, p);
+      const auto mp = coords_w.backward((W)m, (W)p);
       int s = (int)std::get<0>(mp);
       s = s < 0 ? 0 : (s >= (int)stack_size ? (int)stack_size - 1 : s);
       uint i;
-      ctype f;
-      gbint_detail::cell<ctype>((ctype)std::get<1>(mp), p_size, i, f);
+      W f;
+      gbint_detail::cell<W>((W)std::get<1>(mp), p_size, i, f);
       const float *row = d + (size_t)s * p_size;
       if (p_size < 2) return (NT)row[0];
-      return (NT)((ctype)row[i] + f * ((ctype)row[i + 1] - (ctype)row[i]));
+      return (NT)((W)row[i] + f * ((W)row[i + 1] - (W)row[i]));
     }
 
   protected:
+    using W = gbint_detail::map_precision<NT, ctype>;
     Coordinates coordinates;
+    typename gbint_detail::at_precision<Coordinates, W>::type coords_w =
+        gbint_detail::at_precision<Coordinates, W>::make(coordinates);
     uint stack_size, p_size;
     gbint_detail::Store<float> *store_;
     const float *h_data_;
