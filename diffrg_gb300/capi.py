@@ -34,7 +34,7 @@ EXPORTS = [
     "gb_serve_start", "gb_serve_stop", "gb_submit", "gb_poll", "gb_wait", "gb_cancel",
     "gb_get_stats", "gb_reset_stats", "gb_measure_peaks",
     "gb_buffer_create", "gb_buffer_upload", "gb_buffer_destroy",
-    "gb_slot_acquire", "gb_slot_wait", "gb_slot_release", "gb_device_info",
+    "gb_slot_acquire", "gb_slot_wait", "gb_slot_release", "gb_slot_host", "gb_device_info",
     "gb_graph_capture_begin", "gb_graph_capture_end", "gb_graph_launch", "gb_graph_info", "gb_graph_destroy",
     "gb_autotune", "gb_tune_set", "gb_selftest_wait", "gb_table_group_begin", "gb_table_group_end",
 ]

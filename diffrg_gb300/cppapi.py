@@ -69,13 +69,15 @@ def compile_program(src: str, out: str, extra=()) -> str:
     libdir = os.path.dirname(lib)
     os.makedirs(os.path.dirname(out), exist_ok=True)
     h = hashlib.sha256()
-    for p in (src, os.path.join(B.INCLUDE, "gbint.h"), os.path.join(B.INCLUDE, "gbint", "integrators.hh"),
-              os.path.join(B.INCLUDE, "gbint", "interpolators.hh"), os.path.join(B.INCLUDE, "gbint", "autodiff.hh"),
-              os.path.join(B.INCLUDE, "gbint", "regulators.hh"),
-              os.path.join(B.INCLUDE, "gbint", "flow_utils.hh"),
-              os.path.join(B.INCLUDE, "gbint", "kernel_math.hh"),
-              os.path.join(B.INCLUDE, "gbint", "device", "families.cuh")):
-        h.update(open(p, "rb").read())
+    h.update(open(src, "rb").read())
+    _headers_digest(h)
+    extra = list(extra)
+    for i, a in enumerate(extra):  # the files of extra include directories (e.g. a flows/ tree)
+        if a == "-I" and i + 1 < len(extra) and os.path.isdir(extra[i + 1]) and not extra[i + 1].startswith(B.INCLUDE):
+            for d, _, fs in sorted(os.walk(extra[i + 1])):
+                for f in sorted(fs):
+                    h.update(open(os.path.join(d, f), "rb").read())
+    h.update(" ".join(extra).encode())
     h.update(open(lib, "rb").read()[:4096])
     stamp = out + ".stamp"
     if os.path.exists(out) and os.path.exists(stamp) and open(stamp).read() == h.hexdigest():
@@ -93,3 +95,14 @@ def compile_program(src: str, out: str, extra=()) -> str:
 
 def build_tests() -> str:
     return compile_program(TEST_SRC, TEST_BIN)
+
+
+DROPIN_SRC = os.path.join(os.path.dirname(os.path.abspath(__file__)), "bench", "dropin_bench.cu")
+DROPIN_BIN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "bench", "bin", "dropin_bench")
+
+
+def build_dropin_bench() -> str:
+    """The C++ drop-in benchmark (bench.py's cpp_dropin leg): the generator-layout vertex loop of
+    tests/cpp/genflows through the drop-in headers, compiled as a user translation unit."""
+    return compile_program(DROPIN_SRC, DROPIN_BIN,
+                           extra=["-std=c++20", "-I", COMPAT, "-I", os.path.join(ROOT, "tests", "cpp", "genflows")])

@@ -1022,6 +1022,22 @@ namespace gbint
   }
 } // namespace gbint
 
+namespace gbint
+{
+  // Device copy of a rule array, allocated and zero-filled to a multiple of 16 bytes: the C++
+  // layer's fused kernel stages these arrays into shared memory with TMA bulk copies, whose size
+  // must be a multiple of 16 bytes and stay inside the allocation.
+  template <typename T> int rule_device_copy(gb_ctx *ctx, const std::vector<double> &h, T **d)
+  {
+    const size_t bytes = h.size() * sizeof(T), padded = (bytes + 15) & ~size_t(15);
+    std::vector<T> v(padded / sizeof(T), T(0));
+    for (size_t i = 0; i < h.size(); ++i) v[i] = (T)h[i];
+    GB_CUDA(cudaMalloc(d, padded));
+    GB_CUDA(cudaMemcpy(*d, v.data(), padded, cudaMemcpyHostToDevice));
+    return GB_OK;
+  }
+} // namespace gbint
+
 // ============================================================================ C ABI
 extern "C" {
 
@@ -1158,20 +1174,17 @@ static int rule_out(gb_ctx *ctx, GLRule &r, int order, int dtype, const double *
     GB_CUDA(cudaSetDevice(ctx->device));
     if (dtype == GB_DTYPE_F64) {
       if (!r.d64x) {
-        GB_CUDA(cudaMalloc(&r.d64x, order * sizeof(double)));
-        GB_CUDA(cudaMalloc(&r.d64w, order * sizeof(double)));
-        GB_CUDA(cudaMemcpy(r.d64x, r.x.data(), order * sizeof(double), cudaMemcpyHostToDevice));
-        GB_CUDA(cudaMemcpy(r.d64w, r.w.data(), order * sizeof(double), cudaMemcpyHostToDevice));
+        int rc = rule_device_copy(ctx, r.x, &r.d64x);
+        if (!rc) rc = rule_device_copy(ctx, r.w, &r.d64w);
+        if (rc) return rc;
       }
       if (dx) *dx = r.d64x;
       if (dw) *dw = r.d64w;
     } else {
       if (!r.d32x) {
-        std::vector<float> fx(r.x.begin(), r.x.end()), fw(r.w.begin(), r.w.end());
-        GB_CUDA(cudaMalloc(&r.d32x, order * sizeof(float)));
-        GB_CUDA(cudaMalloc(&r.d32w, order * sizeof(float)));
-        GB_CUDA(cudaMemcpy(r.d32x, fx.data(), order * sizeof(float), cudaMemcpyHostToDevice));
-        GB_CUDA(cudaMemcpy(r.d32w, fw.data(), order * sizeof(float), cudaMemcpyHostToDevice));
+        int rc = rule_device_copy(ctx, r.x, &r.d32x);
+        if (!rc) rc = rule_device_copy(ctx, r.w, &r.d32w);
+        if (rc) return rc;
       }
       if (dx) *dx = r.d32x;
       if (dw) *dw = r.d32w;
@@ -1252,20 +1265,17 @@ int gb_quad_matsubara(gb_ctx *ctx, double T, double E, int dtype, int *size, con
     GB_CUDA(cudaSetDevice(ctx->device));
     if (dtype == GB_DTYPE_F64) {
       if (!m.d64x) {
-        GB_CUDA(cudaMalloc(&m.d64x, n * sizeof(double)));
-        GB_CUDA(cudaMalloc(&m.d64w, n * sizeof(double)));
-        GB_CUDA(cudaMemcpy(m.d64x, m.rule.x.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-        GB_CUDA(cudaMemcpy(m.d64w, m.rule.w.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+        int rc = rule_device_copy(ctx, m.rule.x, &m.d64x);
+        if (!rc) rc = rule_device_copy(ctx, m.rule.w, &m.d64w);
+        if (rc) return rc;
       }
       if (dx) *dx = m.d64x;
       if (dw) *dw = m.d64w;
     } else {
       if (!m.d32x) {
-        std::vector<float> fx(m.rule.x.begin(), m.rule.x.end()), fw(m.rule.w.begin(), m.rule.w.end());
-        GB_CUDA(cudaMalloc(&m.d32x, n * sizeof(float)));
-        GB_CUDA(cudaMalloc(&m.d32w, n * sizeof(float)));
-        GB_CUDA(cudaMemcpy(m.d32x, fx.data(), n * sizeof(float), cudaMemcpyHostToDevice));
-        GB_CUDA(cudaMemcpy(m.d32w, fw.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+        int rc = rule_device_copy(ctx, m.rule.x, &m.d32x);
+        if (!rc) rc = rule_device_copy(ctx, m.rule.w, &m.d32w);
+        if (rc) return rc;
       }
       if (dx) *dx = m.d32x;
       if (dw) *dw = m.d32w;

@@ -14,6 +14,8 @@ namespace gbint
     gb_slot pub{};
     cudaStream_t stream = nullptr;
     double *host_result = nullptr;  // pinned
+    void *host_staging = nullptr;   // pinned, grown on demand (gb_slot_host)
+    size_t host_staging_bytes = 0;
     bool busy = false;
   };
   struct SlotPool {
@@ -37,6 +39,7 @@ namespace gbint
       cudaFree(s->pub.partials);
       cudaFree(s->pub.counters);
       cudaFreeHost(s->host_result);
+      if (s->host_staging) cudaFreeHost(s->host_staging);
       cudaStreamDestroy(s->stream);
       delete s;
     }
@@ -120,6 +123,33 @@ int gb_slot_wait(gb_ctx *ctx, const gb_slot *slot, double *out)
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "slot wait");
   *out = *s->host_result;
+  return GB_OK;
+}
+
+int gb_slot_host(gb_ctx *ctx, const gb_slot *slot, size_t bytes, void **host)
+{
+  if (!ctx || !slot || !host || !ctx->slotpool) return set_error(ctx, GB_EINVAL, "bad slot");
+  SlotRec *s = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(ctx->slotpool->mu);
+    if (slot->id < 0 || slot->id >= (int)ctx->slotpool->all.size()) return set_error(ctx, GB_EINVAL, "bad slot id");
+    s = ctx->slotpool->all[slot->id];
+  }
+  if (s->host_staging_bytes < bytes) {
+    // the slot's previous work has drained (the slot is held by its caller); grow 1.5x
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (s->host_staging) cudaFreeHost(s->host_staging);
+    s->host_staging = nullptr;
+    s->host_staging_bytes = 0;
+    const size_t cap = std::max(bytes, (size_t)64 << 10) + bytes / 2;
+    if (e == cudaSuccess) e = cudaMallocHost(&s->host_staging, cap);
+    if (e != cudaSuccess) {
+      s->host_staging = nullptr;
+      return cuda_fail(ctx, e, "slot host staging");
+    }
+    s->host_staging_bytes = cap;
+  }
+  *host = s->host_staging;
   return GB_OK;
 }
 

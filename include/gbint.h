@@ -259,6 +259,9 @@ int gb_buffer_destroy(gb_ctx *ctx, void *d_ptr);
 int gb_slot_acquire(gb_ctx *ctx, int units, gb_slot *out);
 int gb_slot_wait(gb_ctx *ctx, const gb_slot *slot, double *out);
 int gb_slot_release(gb_ctx *ctx, const gb_slot *slot);
+/* A pinned host buffer of at least `bytes` owned by the slot (kept and grown across uses) for
+ * the uploads and read-backs of a batched launch; valid while the slot is held. */
+int gb_slot_host(gb_ctx *ctx, const gb_slot *slot, size_t bytes, void **host);
 int gb_device_info(gb_ctx *ctx, int *device, int *num_sms);
 
 /* ------------------------------------------------------------------ autotuner

@@ -8,10 +8,13 @@
 //   update_interpolator(futures, interpolator)    interpolator[i] = futures[i].get(); update()
 //   get_data<NT>(dest, fun, grid, k, args... | std::tuple<args...>)
 //                                                 dest[i] = fun.get<NT>(k, point..., args...)
-// With the integrators of gbint/integrators.hh every request() launches at once on a pooled
-// stream, so the requests of a grid overlap on the GPU; get_data issues all requests before it
-// collects (the reference runs the gets on TBB threads instead).  C++17: the reference's
-// IsCoordinate / IsContainer constraints are checked with traits.
+// request_data opens a RequestBatch (gbint/integrators.hh) around the grid: every request() of
+// the drop-in integrators issued for the grid -- also through the wrapper classes of generated
+// flows -- joins one persistent launch per kernel type, launched before request_data returns
+// (the reference launches one kernel and runs one reduction with its synchronisation per point).
+// get_data issues all requests before it collects (the reference runs the gets on TBB threads
+// instead).  Results equal single get()s bit for bit.  C++17: the reference's IsCoordinate /
+// IsContainer constraints are checked with traits.
 #pragma once
 
 #include <array>
@@ -23,6 +26,7 @@
 #include <utility>
 #include <vector>
 
+#include "gbint/integrators.hh"
 #include "gbint/interpolators.hh"
 
 namespace DiFfRG
@@ -81,6 +85,7 @@ namespace DiFfRG
   std::shared_ptr<std::vector<std::future<NT>>> request_data(FUN &fun, const GRID &grid, const double k, T... args)
   {
     auto futures = std::make_shared<std::vector<std::future<NT>>>();
+    RequestBatch batch;  // one launch for the grid, at the end of this scope
     if constexpr (gbint_detail::is_coordinates<GRID>::value) {
       const auto points = make_grid(grid);
       futures->reserve(points.size());

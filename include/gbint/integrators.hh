@@ -17,8 +17,12 @@
 //   QuadratureProvider                    .../common/quadrature/quadrature_provider.hh:138-248
 //
 // The user KERNEL (static kernel(...) / constant(...)) is compiled here, in the user's
-// translation unit (nvcc), into one fused kernel per family: points are evaluated, reduced in
-// FP64 per block and finished by the last block -- no per-point global buffer and no CUB pass.
+// translation unit (nvcc), into one fused persistent kernel per family and argument signature
+// (gbint/device/user_batch.cuh): nodes, weights and interpolator tables staged into shared memory
+// by TMA bulk copies, points evaluated and reduced in FP64 per work unit, each integral finished
+// by its last unit -- no per-point global buffer and no CUB pass.  request() launches at once,
+// or, inside a RequestBatch scope (request_data / get_data open one per external grid), joins one
+// launch with every other request of the scope.
 // NT = double evaluates in FP64; NT = float in FP32 with Kahan-compensated accumulation.
 // Everything else goes through the C ABI of libgbint (gbint.h): quadrature storage, streams,
 // reduction scratch, result transfer.  Errors throw std::runtime_error, as the reference does.
@@ -29,8 +33,11 @@
 // (gbint::Table views), not 8-bit-fraction texture filtering.
 #pragma once
 
+#include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <future>
 #include <map>
@@ -39,6 +46,8 @@
 #include <stdexcept>
 #include <string>
 #include <type_traits>
+#include <typeindex>
+#include <typeinfo>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -46,6 +55,7 @@
 
 #include "gbint.h"
 #include "gbint/device/families.cuh"
+#include "gbint/device/user_batch.cuh"
 
 namespace DiFfRG
 {
@@ -259,192 +269,357 @@ namespace DiFfRG
   };
 
   // ---------------------------------------------------------------------------------------
-  // the fused kernel and its launch
+  // batched launches of the fused kernel (gbint/device/user_batch.cuh)
   // ---------------------------------------------------------------------------------------
   namespace gbint_detail
   {
-    // forward declaration: the definition (a kernel launch) is compiled only by nvcc; a host
-    // compiler translation unit (e.g. a flow's FlowEquations source, compiled by g++ as in the
-    // reference's build) sees the integrator classes complete but cannot launch them
-    template <typename NT> class Pending;
-    template <class FAM, class KERNEL, typename NT, typename ctype, class... T>
-    std::shared_ptr<Pending<NT>> launch(QuadratureProvider &qp, std::shared_ptr<gb_ctx> keep,
-                                        const gbint::fam::Params<ctype> &P, NT constant, const T &...t);
-  } // namespace gbint_detail
+    constexpr int kMaxBatchItems = 16384;       // a batch launches when it reaches this size
+    constexpr unsigned kStageCapBytes = 32768;  // shared memory a launch stages per CTA
 
-  namespace gbint_detail
-  {
-    constexpr int kThreads = 256;
-    constexpr int kPPT = 4;
-    constexpr int kUnit = kThreads * kPPT;
-
-#ifdef __CUDACC__
-    __device__ __forceinline__ double warp_sum(double v)
+    // launches in which a CTA read its staged arrays from global memory instead (staging wait
+    // ran out, or an array was not 16-byte aligned) -- results are valid either way
+    inline std::atomic<long long> &staging_fallbacks()
     {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-      return v;
+      static std::atomic<long long> n{0};
+      return n;
     }
 
-    // persistent CTAs pull units of kUnit points; FP64 block sums per unit and component; the
-    // last unit to arrive adds the unit partials in order (deterministic) and writes the C result
-    // components to partials[n_units * C + c] (component 0 also to *result)
-    template <class FAM, class KERNEL, typename NT, typename ctype, class... T>
-    __global__ void __launch_bounds__(kThreads)
-        k_user(const gbint::fam::Params<ctype> P, long long n_points, int n_units, double *partials, int *counters,
-               double *result, T... t)
-    {
-      using TR = nt_traits<NT>;
-      constexpr int C = TR::C;
-      using S = typename TR::S;
-      __shared__ double red[C][32];
-      __shared__ int s_unit, s_last;
-      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-      for (;;) {
-        if (threadIdx.x == 0) s_unit = atomicAdd(&counters[0], 1);
-        __syncthreads();
-        const int u = s_unit;
-        if (u >= n_units) break;
-        const long long begin = (long long)u * kUnit;
-        double acc[C];
-        if constexpr (std::is_same_v<S, float>) {
-          float s[C], c[C];  // Kahan per component
-#pragma unroll
-          for (int m = 0; m < C; ++m) s[m] = c[m] = 0.f;
-#pragma unroll 1
-          for (int k = 0; k < kPPT; ++k) {
-            const long long idx = begin + threadIdx.x + k * kThreads;
-            if (idx < n_points) {
-              const NT v = FAM::template eval<KERNEL, NT>(P, idx, t...);
-#pragma unroll
-              for (int m = 0; m < C; ++m) {
-                const float y = __fsub_rn((float)TR::get(v, m), c[m]);
-                const float tt = __fadd_rn(s[m], y);
-                c[m] = __fsub_rn(__fsub_rn(tt, s[m]), y);
-                s[m] = tt;
-              }
-            }
-          }
-#pragma unroll
-          for (int m = 0; m < C; ++m) acc[m] = (double)s[m] - (double)c[m];
-        } else {
-#pragma unroll
-          for (int m = 0; m < C; ++m) acc[m] = 0.0;
-#pragma unroll 1
-          for (int k = 0; k < kPPT; ++k) {
-            const long long idx = begin + threadIdx.x + k * kThreads;
-            if (idx < n_points) {
-              const NT v = FAM::template eval<KERNEL, NT>(P, idx, t...);
-#pragma unroll
-              for (int m = 0; m < C; ++m) acc[m] += (double)TR::get(v, m);
-            }
-          }
-        }
-#pragma unroll
-        for (int m = 0; m < C; ++m) {
-          acc[m] = warp_sum(acc[m]);
-          if (lane == 0) red[m][wid] = acc[m];
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-#pragma unroll
-          for (int m = 0; m < C; ++m) {
-            double s = 0;
-            for (int i = 0; i < kThreads / 32; ++i) s += red[m][i];
-            partials[(size_t)u * C + m] = s;
-          }
-          __threadfence();
-          s_last = (atomicAdd(&counters[1], 1) == n_units - 1);
-        }
-        __syncthreads();
-        if (s_last) {
-          __threadfence();
-          double v[C];
-#pragma unroll
-          for (int m = 0; m < C; ++m) v[m] = 0.0;
-          for (int i = threadIdx.x; i < n_units; i += kThreads)
-#pragma unroll
-            for (int m = 0; m < C; ++m) v[m] += __ldcg(&partials[(size_t)i * C + m]);
-#pragma unroll
-          for (int m = 0; m < C; ++m) {
-            v[m] = warp_sum(v[m]);
-            if (lane == 0) red[m][wid] = v[m];
-          }
-          __syncthreads();
-          if (threadIdx.x == 0) {
-#pragma unroll
-            for (int m = 0; m < C; ++m) {
-              double s = 0;
-              for (int i = 0; i < kThreads / 32; ++i) s += red[m][i];
-              partials[(size_t)n_units * C + m] = s;
-              if (m == 0) *result = s;
-            }
-          }
-        }
-        __syncthreads();
-      }
-    }
-
-#endif // __CUDACC__
-
-    // one launched request: resolves to constant + integral
-    template <typename NT> class Pending
+    // The device results of one launch.  wait() copies them (and the launch's error word) to the
+    // host once through the slot's pinned staging, releases the request slot and turns a CUDA
+    // error into an exception.
+    class LaunchResult
     {
     public:
-      Pending(std::shared_ptr<gb_ctx> ctx, gb_slot slot, NT constant, int n_units)
-          : ctx_(std::move(ctx)), slot_(slot), c_(constant), n_units_(n_units)
+      LaunchResult(std::shared_ptr<gb_ctx> keep, gb_slot slot, int n_values, const double *d_values, const int *d_err,
+                   double *pinned)
+          : keep_(std::move(keep)), slot_(slot), host_(n_values), d_values_(d_values), d_err_(d_err), pinned_(pinned)
       {
       }
-      NT get()
+      ~LaunchResult()
       {
-        constexpr int C = nt_traits<NT>::C;
-        double v[C] = {};
-        int rc = gb_slot_wait(ctx_.get(), &slot_, &v[0]);
-        if (rc == GB_OK && C > 1) {  // the other components, from the partials tail (stream is idle)
-          const cudaError_t e = cudaMemcpy(&v[1], slot_.partials + (size_t)n_units_ * C + 1, (C - 1) * sizeof(double),
-                                           cudaMemcpyDeviceToHost);
-          if (e != cudaSuccess) rc = GB_ECUDA;
+        if (!done_) {  // never waited for: drain and give the slot back
+          cudaStreamSynchronize((cudaStream_t)slot_.stream);
+          gb_slot_release(keep_.get(), &slot_);
         }
-        gb_slot_release(ctx_.get(), &slot_);
-        check(ctx_.get(), rc, "request");
-        return c_ + nt_traits<NT>::make(v);
+      }
+      const double *wait()
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (!done_) {
+          cudaStream_t s = (cudaStream_t)slot_.stream;
+          int *perr = reinterpret_cast<int *>(pinned_ + host_.size());
+          cudaError_t e = cudaMemcpyAsync(pinned_, d_values_, host_.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
+          if (e == cudaSuccess) e = cudaMemcpyAsync(perr, d_err_, sizeof(int), cudaMemcpyDeviceToHost, s);
+          if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+          if (e == cudaSuccess) {
+            std::memcpy(host_.data(), pinned_, host_.size() * sizeof(double));
+            // staging that gave up only means the CTA read global memory: results are valid
+            if (*perr != 0) staging_fallbacks()++;
+          }
+          gb_slot_release(keep_.get(), &slot_);
+          done_ = true;
+          if (e != cudaSuccess) error_ = std::string("integrator kernel: ") + cudaGetErrorString(e);
+        }
+        if (!error_.empty()) throw std::runtime_error(error_);
+        return host_.data();
       }
 
     private:
-      std::shared_ptr<gb_ctx> ctx_;
+      std::shared_ptr<gb_ctx> keep_;
       gb_slot slot_;
-      NT c_;
-      int n_units_;
+      std::vector<double> host_;
+      const double *d_values_;
+      const int *d_err_;
+      double *pinned_;
+      std::mutex mu_;
+      bool done_ = false;
+      std::string error_;
+    };
+
+    // A batch of integrals of one fused-kernel type (family, KERNEL, result and argument types):
+    // add() collects them, launch() runs them all in one persistent launch.
+    class BatchBase
+    {
+    public:
+      virtual ~BatchBase() = default;
+      virtual void launch() = 0;
+      virtual size_t size() const = 0;
+      virtual bool launched() const = 0;
+    };
+
+    template <class FAM, class KERNEL, typename NT, typename ctype, class... T> class UserBatch : public BatchBase
+    {
+    public:
+      using ItemT = gbint::ub::Item<ctype, T...>;
+      UserBatch(QuadratureProvider &qp, std::shared_ptr<gb_ctx> keep) : qp_(&qp), keep_(std::move(keep)) {}
+
+      int add(const gbint::fam::Params<ctype> &P, const T &...t)
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (launched_) throw std::logic_error("integrator batch: add after launch");
+        const long long n = FAM::points(P);
+        if (n <= 0) throw std::runtime_error("integrator: empty quadrature grid");
+        const long long per = gbint::ub::unit_points(n);
+        const long long u = (n + per - 1) / per;
+        if (units_ + u > (1ll << 28)) throw std::runtime_error("integrator: grid too large");
+        if (items_.empty()) {  // the staging plan follows the first integral
+          if constexpr (sizeof...(T) > 0) tables_ = tables_of(t...);
+        }
+        items_.push_back(ItemT{P, gbint::ub::make_pack(t...)});
+        unit_begin_.push_back((int)units_);
+        units_ += u;
+        return (int)items_.size() - 1;
+      }
+      size_t size() const override
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        return items_.size();
+      }
+      bool launched() const override
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        return launched_;
+      }
+      void launch() override;
+      // the launch's results (launching the batch first if nobody has)
+      std::shared_ptr<LaunchResult> result()
+      {
+        launch();
+        return result_;
+      }
+
+    private:
+      // (device pointer, bytes) of every interpolator argument with a device table
+      template <class A> static void table_of(const A &a, std::vector<std::pair<const void *, unsigned>> &out)
+      {
+        if constexpr (gbint::ub::is_stageable<A>::value) out.emplace_back(a.device_data(), (unsigned)a.table_bytes());
+      }
+      static std::vector<std::pair<const void *, unsigned>> tables_of(const T &...t)
+      {
+        std::vector<std::pair<const void *, unsigned>> out;
+        (table_of(t, out), ...);
+        return out;
+      }
+      // shared arrays of the launch, from its first integral: rule arrays (axes, Matsubara), then
+      // interpolator tables, each once, while they fit the staging budget
+      gbint::ub::StagePlan plan() const
+      {
+        gbint::ub::StagePlan pl;
+        const ItemT &it = items_.front();
+        auto add = [&](const void *src, size_t bytes) {
+          if (!src || bytes == 0 || pl.n >= gbint::ub::kMaxStage) return;
+          if (reinterpret_cast<uintptr_t>(src) & 15) return;
+          for (int s = 0; s < pl.n; ++s)
+            if (pl.src[s] == src) return;
+          const unsigned b = (unsigned)((bytes + 15) & ~size_t(15));
+          if (pl.total + b > kStageCapBytes) return;
+          pl.src[pl.n] = src;
+          pl.off[pl.n] = pl.total;
+          pl.bytes[pl.n] = b;
+          pl.total += b;
+          ++pl.n;
+        };
+        for (int a = 0; a < 4; ++a)
+          if (it.P.n[a] > 0) {
+            add(it.P.x[a], (size_t)it.P.n[a] * sizeof(ctype));
+            add(it.P.w[a], (size_t)it.P.n[a] * sizeof(ctype));
+          }
+        if (it.P.nm > 0) {
+          add(it.P.mx, (size_t)it.P.nm * sizeof(ctype));
+          add(it.P.mw, (size_t)it.P.nm * sizeof(ctype));
+        }
+        for (const auto &t : tables_) add(t.first, t.second);
+        return pl;
+      }
+
+      QuadratureProvider *qp_;
+      std::shared_ptr<gb_ctx> keep_;
+      std::vector<ItemT> items_;
+      std::vector<std::pair<const void *, unsigned>> tables_;
+      std::vector<int> unit_begin_;
+      long long units_ = 0;
+      mutable std::mutex mu_;
+      bool launched_ = false;
+      std::shared_ptr<LaunchResult> result_;
     };
 
 #ifdef __CUDACC__
     template <class FAM, class KERNEL, typename NT, typename ctype, class... T>
-    std::shared_ptr<Pending<NT>> launch(QuadratureProvider &qp, std::shared_ptr<gb_ctx> keep,
-                                        const gbint::fam::Params<ctype> &P, NT constant, const T &...t)
+    void UserBatch<FAM, KERNEL, NT, ctype, T...>::launch()
     {
-      constexpr int C = nt_traits<NT>::C;
-      const long long n_points = FAM::points(P);
-      if (n_points <= 0) throw std::runtime_error("integrator: empty quadrature grid");
-      const long long units_ll = (n_points + kUnit - 1) / kUnit;
-      if (units_ll > (1ll << 28)) throw std::runtime_error("integrator: grid too large");
-      const int n_units = (int)units_ll;
+      std::lock_guard<std::mutex> lk(mu_);
+      if (launched_) return;
+      launched_ = true;
+      if (items_.empty()) return;
+      using TR = nt_traits<NT>;
+      constexpr int C = TR::C;
+      const int n = (int)items_.size();
+      const int units = (int)units_;
+      // one slot arena, in doubles: partials | results | error word | arrivals | unit_begin | items
+      static_assert(alignof(ItemT) <= 16, "integrator batch: argument types aligned beyond 16 bytes");
+      const size_t d_part = (size_t)units * C, d_res = (size_t)n * C, d_err = 1;
+      const size_t d_arr = ((size_t)n * sizeof(int) + 7) / 8;
+      const size_t d_head = d_part + d_res + d_err + d_arr;
+      const size_t ub_d = ((size_t)(n + 1) * sizeof(int) + 7) / 8;
+      // unit_begin padded so that the items start on a 16-byte boundary
+      const size_t d_ub = n > 1 ? ub_d + ((d_head + ub_d) & 1) : 0;
+      const size_t d_items = n > 1 ? (n * sizeof(ItemT) + 7) / 8 : 0;
+      const size_t total = d_head + d_ub + d_items;
+      if (total > (size_t)(1u << 30)) throw std::runtime_error("integrator batch: too large");
       gb_slot slot;
-      check(qp.ctx(), gb_slot_acquire(qp.ctx(), (n_units + 1) * C, &slot), "gb_slot_acquire");
-      const int ctas = (int)std::min<long long>(n_units, (long long)qp.num_sms() * 8);
-      k_user<FAM, KERNEL, NT, ctype, T...><<<ctas, kThreads, 0, (cudaStream_t)slot.stream>>>(
-          P, n_points, n_units, slot.partials, slot.counters, slot.result, t...);
-      const cudaError_t e = cudaGetLastError();
+      check(qp_->ctx(), gb_slot_acquire(qp_->ctx(), (int)total, &slot), "gb_slot_acquire");
+      double *base = slot.partials;
+      double *partials = base, *results = base + d_part;
+      int *err = reinterpret_cast<int *>(base + d_part + d_res);
+      int *arrivals = reinterpret_cast<int *>(base + d_part + d_res + d_err);
+      int *d_unit_begin = n > 1 ? reinterpret_cast<int *>(base + d_head) : nullptr;
+      ItemT *d_itemsp = n > 1 ? reinterpret_cast<ItemT *>(base + d_head + d_ub) : nullptr;
+      cudaStream_t s = (cudaStream_t)slot.stream;
+      // pinned host staging of the slot: [read-back: C doubles per integral + error word | upload]
+      const size_t up_bytes = (d_ub + d_items) * sizeof(double), back_bytes = (d_res + 1) * sizeof(double);
+      void *pin = nullptr;
+      const int rc = gb_slot_host(qp_->ctx(), &slot, back_bytes + up_bytes, &pin);
+      if (rc != GB_OK) {
+        gb_slot_release(qp_->ctx(), &slot);
+        check(qp_->ctx(), rc, "gb_slot_host");
+      }
+      cudaError_t e = cudaMemsetAsync(err, 0, (d_err + d_arr) * sizeof(double), s);
+      if (n > 1 && e == cudaSuccess) {
+        char *up = static_cast<char *>(pin) + back_bytes;
+        int *ub = reinterpret_cast<int *>(up);
+        std::memcpy(ub, unit_begin_.data(), n * sizeof(int));
+        ub[n] = units;
+        std::memcpy(up + d_ub * sizeof(double), items_.data(), n * sizeof(ItemT));
+        e = cudaMemcpyAsync(d_unit_begin, up, up_bytes, cudaMemcpyHostToDevice, s);
+      }
+      const gbint::ub::StagePlan pl = plan();
+      // persistent grid: as many CTAs as fit on the GPU at once (each stages the shared arrays);
+      // the occupancy per staging size is looked up once per kernel type
+      auto kern = gbint::ub::k_user_batch<FAM, KERNEL, NT, ctype, TR, T...>;
+      static std::mutex occ_mu;
+      static std::map<unsigned, int> occ;
+      int per_sm = 0;
+      {
+        std::lock_guard<std::mutex> lk2(occ_mu);
+        auto it = occ.find(pl.total);
+        if (it != occ.end())
+          per_sm = it->second;
+        else {
+          if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, gbint::ub::kThreads, pl.total) != cudaSuccess ||
+              per_sm < 1)
+            per_sm = 1;
+          occ[pl.total] = per_sm;
+        }
+      }
+      const int ctas = (int)std::min<long long>(units, (long long)qp_->num_sms() * per_sm);
+      if (e == cudaSuccess) {
+        kern<<<ctas, gbint::ub::kThreads, pl.total, s>>>(items_.front(), d_itemsp, d_unit_begin, n, units, pl, partials,
+                                                          slot.counters, arrivals, results, err);
+        e = cudaGetLastError();
+      }
       if (e != cudaSuccess) {
-        gb_slot_release(qp.ctx(), &slot);
+        cudaStreamSynchronize(s);
+        gb_slot_release(qp_->ctx(), &slot);
         check_cuda(e, "integrator kernel launch");
       }
-      return std::make_shared<Pending<NT>>(std::move(keep), slot, constant, n_units);
+      result_ = std::make_shared<LaunchResult>(keep_, slot, n * C, results, err, static_cast<double *>(pin));
     }
 #endif // __CUDACC__
 
-    template <typename NT> std::future<NT> as_future(std::shared_ptr<Pending<NT>> p)
+    // the future of integral `idx` of a batch: constant + its components
+    template <typename NT, class B> std::future<NT> batch_future(std::shared_ptr<B> b, int idx, NT constant)
     {
-      return std::async(std::launch::deferred, [p]() { return p->get(); });
+      return std::async(std::launch::deferred, [b, idx, constant]() {
+        const double *v = b->result()->wait() + (size_t)idx * nt_traits<NT>::C;
+        return constant + nt_traits<NT>::make(v);
+      });
+    }
+  } // namespace gbint_detail
+
+  // ---------------------------------------------------------------------------------------
+  // RequestBatch: the requests a thread issues while one is alive go into one launch per kernel
+  // type, launched when the scope ends (or flush(), or a future's get()).  request_data and
+  // get_data open one around a whole external grid, so that all its integrals run in a single
+  // persistent launch instead of one launch each.  Results are bit-identical to single gets.
+  // ---------------------------------------------------------------------------------------
+  class RequestBatch;
+  namespace gbint_detail
+  {
+    // the innermost RequestBatch alive on this thread (nullptr: requests launch at once)
+    inline RequestBatch *&tl_request_scope_ptr()
+    {
+      static thread_local RequestBatch *p = nullptr;
+      return p;
+    }
+  } // namespace gbint_detail
+
+  class RequestBatch
+  {
+  public:
+    RequestBatch() : prev_(gbint_detail::tl_request_scope_ptr()) { gbint_detail::tl_request_scope_ptr() = this; }
+    ~RequestBatch()
+    {
+      try {
+        flush();
+      } catch (...) {
+        // a failed launch surfaces again at the futures' get()
+      }
+      gbint_detail::tl_request_scope_ptr() = prev_;
+    }
+    RequestBatch(const RequestBatch &) = delete;
+    RequestBatch &operator=(const RequestBatch &) = delete;
+
+    // launch everything collected so far
+    void flush()
+    {
+      auto order = std::move(order_);
+      order_.clear();
+      open_.clear();
+      for (auto &b : order) b->launch();
+    }
+
+    // the open batch of type B for the provider's context
+    template <class B> std::shared_ptr<B> batch(QuadratureProvider &qp, std::shared_ptr<gb_ctx> keep)
+    {
+      const auto key = std::make_pair((const void *)qp.ctx(), std::type_index(typeid(B)));
+      auto it = open_.find(key);
+      // a batch that is full, or that a future's get() already launched, is closed
+      if (it != open_.end() && (it->second->launched() || it->second->size() >= (size_t)gbint_detail::kMaxBatchItems)) {
+        it->second->launch();
+        open_.erase(it);
+        it = open_.end();
+      }
+      if (it == open_.end()) {
+        auto b = std::make_shared<B>(qp, std::move(keep));
+        order_.push_back(b);
+        it = open_.emplace(key, b).first;
+      }
+      return std::static_pointer_cast<B>(it->second);
+    }
+
+  private:
+    RequestBatch *prev_;
+    std::map<std::pair<const void *, std::type_index>, std::shared_ptr<gbint_detail::BatchBase>> open_;
+    std::vector<std::shared_ptr<gbint_detail::BatchBase>> order_;
+  };
+
+  namespace gbint_detail
+  {
+    // one request: into the thread's open RequestBatch if there is one, else launched at once
+    template <class FAM, class KERNEL, typename NT, typename ctype, class... T>
+    std::future<NT> submit(QuadratureProvider &qp, std::shared_ptr<gb_ctx> keep, const gbint::fam::Params<ctype> &P,
+                           NT constant, const T &...t)
+    {
+      using B = UserBatch<FAM, KERNEL, NT, ctype, T...>;
+      if (RequestBatch *scope = tl_request_scope_ptr()) {
+        auto b = scope->template batch<B>(qp, std::move(keep));
+        const int idx = b->add(P, t...);
+        return batch_future<NT>(b, idx, constant);
+      }
+      auto b = std::make_shared<B>(qp, std::move(keep));
+      const int idx = b->add(P, t...);
+      b->launch();
+      return batch_future<NT>(b, idx, constant);
     }
   } // namespace gbint_detail
 
@@ -472,7 +647,7 @@ namespace DiFfRG
         gbint::fam::Params<ctype> P = P_;
         P.k = k;
         const NT c = (NT)KERNEL::constant(k, t...);
-        return as_future(launch<FAM, KERNEL, NT, ctype>(*qp_, keep(), P, c, t...));
+        return submit<FAM, KERNEL, NT, ctype>(*qp_, keep(), P, c, t...);
       }
 
     protected:
@@ -703,8 +878,8 @@ namespace DiFfRG
       gbint::fam::Params<ctype> P = P_;
       P.k = k;
       const NT c = (NT)KERNEL::constant(k, t...);
-      return gbint_detail::as_future(gbint_detail::launch<FAM, KERNEL, NT, ctype>(
-          *qp_, std::shared_ptr<gb_ctx>(qp_->ctx(), [](gb_ctx *) {}), P, c, t...));
+      return gbint_detail::submit<FAM, KERNEL, NT, ctype>(*qp_, std::shared_ptr<gb_ctx>(qp_->ctx(), [](gb_ctx *) {}), P,
+                                                          c, t...);
     }
 
   private:
@@ -777,8 +952,8 @@ namespace DiFfRG
       P.log_start = std::log(start + P.off);
       P.log_ext = std::log(P.x0_extent / (start + P.off));
       const NT c = (NT)KERNEL::constant(k, t...);
-      return gbint_detail::as_future(gbint_detail::launch<FAM, KERNEL, NT, ctype>(
-          *qp_, std::shared_ptr<gb_ctx>(qp_->ctx(), [](gb_ctx *) {}), P, c, t...));
+      return gbint_detail::submit<FAM, KERNEL, NT, ctype>(*qp_, std::shared_ptr<gb_ctx>(qp_->ctx(), [](gb_ctx *) {}), P,
+                                                          c, t...);
     }
 
   private:

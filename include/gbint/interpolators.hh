@@ -25,6 +25,7 @@
 
 #include <array>
 #include <cmath>
+#include <cstring>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
@@ -94,6 +95,7 @@ namespace DiFfRG
       idx_per_log_ = (NT)((grid_extent - 1.) / bias);
       log_per_idx_ = (NT)(bias / (grid_extent - 1.));
       span_ = (stop - start) / std::expm1(bias);
+      inv_span_ = (NT)1 / span_;
     }
     template <typename NT2>
     LogarithmicCoordinates1D(const LogarithmicCoordinates1D<NT2> &other)
@@ -101,14 +103,14 @@ namespace DiFfRG
     {
     }
     __host__ __device__ NT forward(const uint &x) const { return span_ * expm1(log_per_idx_ * x) + start; }
-    __host__ __device__ NT backward(const NT &y) const { return log1p((y - start) / span_) * idx_per_log_; }
+    __host__ __device__ NT backward(const NT &y) const { return log1p((y - start) * inv_span_) * idx_per_log_; }
     __host__ __device__ NT backward_derivative(const NT &y) const { return idx_per_log_ / (y - start); }
     __host__ __device__ uint size() const { return n_; }
     NT start, stop, bias;
 
   private:
     uint n_;
-    NT idx_per_log_, log_per_idx_, span_;
+    NT idx_per_log_, log_per_idx_, span_, inv_span_;
   };
 
   // integer stack index and Matsubara frequencies (stack axes of the finite-T coordinates)
@@ -357,12 +359,17 @@ namespace DiFfRG
       if (!ctx) throw std::runtime_error("No CUDA devices found! (interpolator context)");
       return ctx;
     }
+    // the buffer is a multiple of 16 bytes (zero padding): the fused kernels stage tables into
+    // shared memory with TMA bulk copies, whose sizes are multiples of 16 bytes
+    inline size_t padded_bytes(size_t bytes) { return (bytes + 15) & ~size_t(15); }
     template <typename T> T *device_copy(const std::vector<T> &h)
     {
       void *d = nullptr;
       gb_ctx *c = interp_ctx();
-      if (gb_buffer_create(c, h.size() * sizeof(T), &d) != GB_OK ||
-          gb_buffer_upload(c, d, h.data(), h.size() * sizeof(T)) != GB_OK)
+      const size_t bytes = h.size() * sizeof(T);
+      std::vector<char> pad(padded_bytes(bytes), 0);
+      if (bytes) std::memcpy(pad.data(), h.data(), bytes);
+      if (gb_buffer_create(c, pad.size(), &d) != GB_OK || gb_buffer_upload(c, d, pad.data(), pad.size()) != GB_OK)
         throw std::runtime_error("interpolator: device buffer");
       return static_cast<T *>(d);
     }
@@ -448,6 +455,14 @@ namespace DiFfRG
       return (NT)((W)d[i] + f * ((W)d[i + 1] - (W)d[i]));
     }
 
+
+    // staging interface of the fused kernels (gbint/device/user_batch.cuh): the device table,
+    // its size in bytes (a multiple of 16, see device_copy) and a copy reading another buffer
+    using gbint_stageable_table = DT;
+    __host__ __device__ const void *device_data() const { return d_data_; }
+    size_t table_bytes() const { return gbint_detail::padded_bytes(store_->host.size() * sizeof(DT)); }
+    __host__ __device__ void retarget(const void *p) { d_data_ = static_cast<const DT *>(p); }
+
   protected:
     using W = gbint_detail::map_precision<NT, ctype>;
     Coordinates coordinates;
@@ -512,6 +527,14 @@ namespace DiFfRG
       const W lo = y00 + fx * (y10 - y00), hi = y01 + fx * (y11 - y01);
       return (NT)(lo + fy * (hi - lo));
     }
+
+
+    // staging interface of the fused kernels (gbint/device/user_batch.cuh): the device table,
+    // its size in bytes (a multiple of 16, see device_copy) and a copy reading another buffer
+    using gbint_stageable_table = DT;
+    __host__ __device__ const void *device_data() const { return d_data_; }
+    size_t table_bytes() const { return gbint_detail::padded_bytes(store_->host.size() * sizeof(DT)); }
+    __host__ __device__ void retarget(const void *p) { d_data_ = static_cast<const DT *>(p); }
 
   protected:
     using W = gbint_detail::map_precision<NT, ctype>;
@@ -582,6 +605,14 @@ namespace DiFfRG
       const W c0 = c00 + fy * (c10 - c00), c1 = c01 + fy * (c11 - c01);
       return (NT)(c0 + fz * (c1 - c0));
     }
+
+
+    // staging interface of the fused kernels (gbint/device/user_batch.cuh): the device table,
+    // its size in bytes (a multiple of 16, see device_copy) and a copy reading another buffer
+    using gbint_stageable_table = DT;
+    __host__ __device__ const void *device_data() const { return d_data_; }
+    size_t table_bytes() const { return gbint_detail::padded_bytes(store_->host.size() * sizeof(DT)); }
+    __host__ __device__ void retarget(const void *p) { d_data_ = static_cast<const DT *>(p); }
 
   protected:
     using W = gbint_detail::map_precision<NT, ctype>;
@@ -660,6 +691,14 @@ namespace DiFfRG
       if (p_size < 2) return (NT)row[0];
       return (NT)((W)row[i] + f * ((W)row[i + 1] - (W)row[i]));
     }
+
+
+    // staging interface of the fused kernels (gbint/device/user_batch.cuh): the device table,
+    // its size in bytes (a multiple of 16, see device_copy) and a copy reading another buffer
+    using gbint_stageable_table = float;
+    __host__ __device__ const void *device_data() const { return d_data_; }
+    size_t table_bytes() const { return gbint_detail::padded_bytes(store_->host.size() * sizeof(float)); }
+    __host__ __device__ void retarget(const void *p) { d_data_ = static_cast<const float *>(p); }
 
   protected:
     using W = gbint_detail::map_precision<NT, ctype>;

@@ -397,6 +397,26 @@ struct KExt2 {  // two external arguments (p1, p2) from a 2D coordinate pack
   }
   static __host__ __device__ double constant(double, double, double, const Coeffs &C) { return C.a[0]; }
 };
+struct KTabArg {  // two interpolator arguments (their tables are staged in shared memory)
+  template <class TAB>
+  static __host__ __device__ double kernel(double q, double c, double k, double p, const TAB &Z, const TAB &Y)
+  {
+    const double r = sqrt(q * q + p * p - 2 * p * q * c);
+    return Z(q) * Y(r) * q * q / (1 + q * q * q * q) * (1 + 0.5 * c * k);
+  }
+  template <class TAB> static __host__ __device__ double constant(double, double p, const TAB &Z, const TAB &) { return Z(p); }
+};
+struct KTabDual {  // dual result: the seeded argument s enters through exp(-s q^2)
+  template <class TAB>
+  static __host__ __device__ autodiff::real kernel(double q, double c, double k, const autodiff::real &s, const TAB &Z)
+  {
+    return Z(q) * exp(-s * q * q) * (1 + c * c) * k;
+  }
+  template <class TAB> static __host__ __device__ autodiff::real constant(double, const autodiff::real &, const TAB &)
+  {
+    return autodiff::real(0.0);
+  }
+};
 int fanout_cases()
 {
   QuadratureProvider qp;
@@ -439,6 +459,50 @@ int fanout_cases()
   for (size_t i = 0; i < g2.size(); ++i) d2[i] = I2.get(k, g2[i][0], g2[i][1], A);
   update_data(request_data<double>(I2, pack, k, A), v2.data());
   report("request_data_pack2d", v2, d2);
+
+  // RequestBatch scope: integrals of two integrators of one type with different grids and of
+  // several k in one launch; a get() inside the scope launches the open batch, later requests
+  // start a new one; a kernel with TexLinearInterpolator1D arguments (staged tables) and a dual
+  // result type alongside.  Every value bit-identical to its single get().
+  IntegratorAngleGPU<4, double, KExt1> I1b(qp, {{48, 12}}, 1.2);
+  IntegratorAngleGPU<4, double, KTabArg> IT(qp, {{40, 20}}, 2.0);
+  IntegratorAngleGPU<4, autodiff::real, KTabDual> ID(qp, {{24, 8}}, 1.7);
+  IntegratorAngleGPU<4, double, KExt1> IB(qp, {{160, 128}}, 1.4);  // 20480 points: two points per thread
+  const LogarithmicCoordinates1D<float> tc(48, 1e-3f, 20.f, 4.f);
+  std::vector<double> zv(48), yv(48);
+  for (int i = 0; i < 48; ++i) zv[i] = 1.0 + 0.3 * std::sin(0.37 * i), yv[i] = 0.5 + 0.01 * i * i;
+  const TexLinearInterpolator1D<double, LogarithmicCoordinates1D<float>> Z(zv, tc), Y(yv, tc);
+  std::vector<std::future<double>> fs;
+  std::vector<std::future<autodiff::real>> fd;
+  std::vector<double> want;
+  std::vector<autodiff::real> wantd;
+  for (int i = 0; i < 10; ++i) want.push_back(I1.get(0.5 + 0.05 * i, grid[i], A));
+  for (int i = 0; i < 10; ++i) want.push_back(I1b.get(0.7, grid[i], A));
+  for (int i = 0; i < 4; ++i) want.push_back(I1.get(0.9, grid[i], A));
+  for (int i = 0; i < 3; ++i) want.push_back(IB.get(0.8, grid[i], A));
+  for (int i = 0; i < 8; ++i) want.push_back(IT.get(1.1, grid[i], Z, Y));
+  for (int i = 0; i < 6; ++i) wantd.push_back(ID.get(1.0, autodiff::real(0.2 + 0.1 * i, 1.0), Z));
+  double early = 0;
+  {
+    RequestBatch rb;
+    for (int i = 0; i < 10; ++i) fs.push_back(I1.request(0.5 + 0.05 * i, grid[i], A));
+    for (int i = 0; i < 10; ++i) fs.push_back(I1b.request(0.7, grid[i], A));
+    early = fs[3].get();  // launches the open batch of this kernel type
+    for (int i = 0; i < 4; ++i) fs.push_back(I1.request(0.9, grid[i], A));
+    for (int i = 0; i < 3; ++i) fs.push_back(IB.request(0.8, grid[i], A));
+    for (int i = 0; i < 8; ++i) fs.push_back(IT.request(1.1, grid[i], Z, Y));
+    for (int i = 0; i < 6; ++i) fd.push_back(ID.request(1.0, autodiff::real(0.2 + 0.1 * i, 1.0), Z));
+  }
+  std::vector<double> got, wd, gd;
+  for (size_t i = 0; i < fs.size(); ++i) got.push_back(i == 3 ? early : fs[i].get());
+  for (size_t i = 0; i < fd.size(); ++i) {
+    const autodiff::real v = fd[i].get();
+    gd.push_back(autodiff::val(v)), gd.push_back(autodiff::derivative(v));
+    wd.push_back(autodiff::val(wantd[i])), wd.push_back(autodiff::derivative(wantd[i]));
+  }
+  report("request_batch_scope", got, want);
+  report("request_batch_scope_dual", gd, wd);
+  std::printf("FAN staging_fallbacks %lld 1\n", (long long)gbint_detail::staging_fallbacks().load());
   return 0;
 }
 

@@ -228,12 +228,15 @@ def test_regulators_host_device_and_derivatives(binary):
 def test_fanout_helpers_equal_direct_gets(binary):
     """request_data / update_data / update_interpolator / get_data / make_grid (gbint/flow_utils.hh,
     the reference's DiFfRG/include/DiFfRG/physics/utils.hh:31-220) over a grid of external
-    momenta, a 1D coordinates object (arguments as a tuple) and a 2D coordinate pack: bit-identical
-    to one get() per point."""
+    momenta, a 1D coordinates object (arguments as a tuple) and a 2D coordinate pack, and a
+    RequestBatch scope mixing grids, k values, integral sizes, staged interpolator tables and a
+    dual result type with a get() inside the scope: every batched value bit-identical to one get()
+    per point."""
     out = run(binary, [], extra=["--fanout"])
     rows = {l.split()[1]: (float(l.split()[2]), int(l.split()[3])) for l in out if l.startswith("FAN")}
     assert set(rows) == {"request_data_vector", "request_data_coordinates_tuple", "get_data", "update_interpolator",
-                         "request_data_pack2d"}
+                         "request_data_pack2d", "request_batch_scope", "request_batch_scope_dual", "staging_fallbacks"}
+    assert rows["staging_fallbacks"][0] == 0.0  # every launch read its staged arrays from shared memory
     for what, (diff, n) in rows.items():
         assert n > 0 and diff == 0.0, (what, diff, n)
 
