@@ -48,14 +48,16 @@ UNIT = "integrals/s"
 #   C5 VERT4: r2 (2), one log index shared by both tables (3), two bilinears (2 x 7), Z r2 + R (2),
 #             products + sum (4); log, expm1, div, rcp
 PER_POINT = {"C1": (12, 4), "C2": (18, 4), "C3": (30, 6), "C5": (25, 4)}
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant kernel, from the
-# ncu captures summarised in profiles/ (k_fp32c_S2acc_C2_finiteT.md, k_fp32c_S3acc_C3_uneven3D.md,
-# k_fp32c_S5Z_C5_vertex4D.md)
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant kernel, from one ncu
+# capture of that kernel (summaries under profiles/, named for kernel and workload); a changed
+# kernel needs a new capture -- the JSON line carries these as "traffic" with their source
 TRAFFIC_BYTES_PER_LAUNCH = {"C2": 1495808, "C3": 7070720, "C5": 733184}
 # thread instructions executed per integrand point by the dominant kernel (smsp__inst_executed.sum
 # x 32 / points, same captures): with the measured step time they give the issue rate, the
 # bound this double-float code actually meets (one warp instruction per SM sub-partition and cycle)
 INSTR_PER_POINT = {"C2": 44, "C3": 218, "C5": 113}
+CAPTURE_NOTE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,smsp__inst_executed.sum capture of the "
+                "dominant kernel on this workload (profiles/)")
 
 
 def parse():
@@ -68,6 +70,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the C4 serving measurement")
+    ap.add_argument("--no-legs", action="store_true", help="skip the C1/C3/C5 and C++ drop-in measurements")
     return ap.parse_args()
 
 
@@ -163,8 +166,8 @@ def run_reference(args):
     w = getattr(W, args.workload.lower())()
     threads = os.cpu_count() or 1
     n = len(w["p"]) if "p" in w else len(w["P"])
-    # each step: a bounded sample of the workload (every 4th integral)
-    sub = np.arange(0, n, 4)
+    # each step: the whole workload (all integrals), as the GPU arm's step
+    sub = np.arange(n)
     for _ in range(max(1, args.warmup)):
         W.oracle_values(w, O, threads=threads, subset=sub[:8])
     t0 = time.perf_counter()
@@ -179,10 +182,113 @@ def run_reference(args):
             "config": {"workload": workload_name(args.workload), "integrals_per_step": int(sub.size),
                        "l2": "n/a (CPU)"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "%d of %d %s integrals per step (every 4th), FP64 restatement of the "
-                                       "reference CPU integrators, OpenMP over integrals" % (sub.size, n, args.workload)},
+                             "sample": "all %d %s integrals per step, FP64 restatement of the reference CPU "
+                                       "integrators, OpenMP over integrals" % (n, args.workload)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def workload_leg(name, ctx, stream, flush, steps, warmup, oracle_threads):
+    """One further workload (C1, C3, C5) measured the way the headline is: `value` = fused FP32C
+    integrals/s with inputs resident in HBM (CUDA events, L2 flushed between steps), `e2e` = the
+    same through the C ABI with the tables uploaded from pinned host memory and the results read
+    back every step; the reference-pattern FP64 GPU path; max/median relative error of every
+    integral of the workload against the FP64 oracle."""
+    import ctypes as C
+
+    import torch
+
+    from diffrg_gb300 import capi
+    from diffrg_gb300 import workloads as W
+
+    L = capi.lib()
+    sh = stream.cuda_stream
+    w = getattr(W, name.lower())()
+    items, tabs = W.engine_items(w)
+    n_int = len(items)
+    T = [ctx.table(sp, d) for sp, d in tabs]
+    ctx.autotune(items, T, "fp32c")
+    b32 = ctx.batch(items, T, "fp32c")
+    points = b32.points
+    for _ in range(warmup):
+        b32.run(stream=sh)
+    torch.cuda.synchronize()
+    per = []
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b32.run(stream=sh)
+        e1.record(stream)
+        per.append((e0, e1))
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in per]
+    res32 = b32.results(stream=sh)
+    pinned = [torch.from_numpy(np.ascontiguousarray(d, dtype=np.float32)).pin_memory() for _, d in tabs]
+    host_out = torch.zeros(n_int, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        for t, pt in zip(T, pinned):
+            ctx.check(L.gb_table_update(ctx.h, t.h, C.cast(pt.data_ptr(), C.POINTER(C.c_float)), C.c_void_p(sh)))
+        ctx.check(L.gb_batch_run_graph(ctx.h, b32.h, C.c_void_p(sh)))
+        ctx.check(L.gb_batch_results(ctx.h, b32.h, C.cast(host_out.data_ptr(), C.POINTER(C.c_double)), C.c_void_p(sh)))
+
+    for _ in range(warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    lat = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        e2e_step()
+        lat.append(time.perf_counter() - s0)
+    b64 = ctx.batch(items, T, "fp64")
+    b64.run_plain(16)  # warm-up
+    t0 = time.perf_counter()
+    resp = b64.run_plain(16)
+    plain_dt = time.perf_counter() - t0
+    out = {"workload": workload_name(name), "integrals_per_step": n_int, "points_per_step": points,
+           "value": n_int / (statistics.mean(ms) / 1e3), "unit": UNIT, "ms_per_step": statistics.mean(ms),
+           "steps": steps, "e2e": {"value": n_int / statistics.mean(lat), "unit": UNIT,
+                                   "h2d_bytes_per_step": sum(pt.numel() * 4 for pt in pinned),
+                                   "d2h_bytes_per_step": n_int * 8},
+           "plain_fp64_gpu": {"value": n_int / plain_dt, "unit": UNIT, "ms_per_step": plain_dt * 1e3}}
+    out["fp32c_over_plain_fp64"] = out["value"] / out["plain_fp64_gpu"]["value"]
+    if name in PER_POINT:
+        F, S = PER_POINT[name]
+        out["per_point"] = {"F": F, "S": S}
+    if oracle_threads:
+        from oracle import oracle as O
+
+        O.build()
+        t0 = time.perf_counter()
+        ref = W.oracle_values(w, O, threads=oracle_threads)
+        cpu_dt = time.perf_counter() - t0
+        e = np.abs(res32 - ref) / np.abs(ref)
+        ep = np.abs(resp - ref) / np.abs(ref)
+        out["accuracy"] = {"fp32c_max_rel_err_vs_oracle": float(e.max()), "fp32c_median_rel_err": float(np.median(e)),
+                           "plain_fp64_max_rel_err_vs_oracle": float(ep.max()), "integrals_checked": int(n_int)}
+        out["cpu_oracle"] = {"value": n_int / cpu_dt, "unit": UNIT, "cores": oracle_threads, "kind": "port"}
+    b32.close()
+    b64.close()
+    for t in T:
+        t.close()
+    return out
+
+
+def cpp_dropin(steps):
+    """The C++ drop-in path on a generator-layout flow (diffrg_gb300/bench/dropin_bench.cu): a
+    seven-table vertex loop through IntegratorAngleGPU::request over 128 external momenta, batched
+    (get_data: one persistent launch), one launch per request, and the reference's execution
+    pattern (per-integral kernel, thrust::reduce when the future is read)."""
+    from diffrg_gb300 import cppapi
+
+    exe = cppapi.build_dropin_bench()
+    r = subprocess.run([exe, str(max(3, steps)), "3"], capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        return {"error": (r.stdout + r.stderr)[-500:]}
+    return json.loads(r.stdout.strip().splitlines()[-1])
 
 
 def serving_c4(device):
@@ -377,7 +483,7 @@ def main():
             "achieved": xu_achieved if fracxu >= frac32 else fp32_achieved,
             "peak": mufu_peak if fracxu >= frac32 else fp32_peak,
             "unit": "Gop/s" if fracxu >= frac32 else "TFLOP/s",
-            "frac": max(frac32, fracxu), "traffic": traffic,
+            "frac": max(frac32, fracxu), "traffic": traffic, "traffic_source": CAPTURE_NOTE,
             "fp32": {"achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": frac32},
             "xu": {"achieved": xu_achieved, "peak": mufu_peak, "unit": "Gop/s", "frac": fracxu},
             "per_point": {"F": flops_pp, "S": specials_pp},
@@ -412,6 +518,15 @@ def main():
 
     serve = None if args.no_serve else serving_c4(local)
 
+    # ---------------------------------------------------------------- the other workloads, C++ drop-in path
+    legs = {}
+    if not args.no_legs:
+        for other in ("C1", "C3", "C5"):
+            if other != args.workload:
+                legs[other] = workload_leg(other, ctx, stream, flush, max(3, min(args.steps, 10)), 3,
+                                           (os.cpu_count() or 1) if (rank == 0 and not args.no_cpu) else 0)
+    dropin = None if args.no_legs else cpp_dropin(min(args.steps, 20))
+
     lat_ms = sorted(x * 1e3 for x in lat)
     sl_ms = sorted(x * 1e3 for x in sl)
 
@@ -439,6 +554,8 @@ def main():
             "accuracy": err,
             "autotune": {"cta_threads_by_kind_slot": tuned},
             "serving": serve,
+            "workloads": legs,
+            "cpp_dropin": dropin,
             "cpu_baseline": cpu}
     if serve:
         line["latency_ms"]["serving_c4_p50"] = serve["poisson"]["p50_ms"]
