@@ -25,6 +25,7 @@
 
 #include <cmath>
 #include <functional>
+#include <initializer_list>
 #include <iomanip>
 #include <iostream>
 #include <sstream>
@@ -89,6 +90,45 @@ namespace DiFfRG
       return extent;
     }
 
+    // the settings a flow base reads: a rule order "/integration/<axis>_quadrature_order", the
+    // jacobian rule's order (factor times the order, truncated), a tolerance, the verbosity
+    template <class JSON> unsigned rule_order(const JSON &json, const char *axis)
+    {
+      return json.get_uint(std::string("/integration/") + axis + "_quadrature_order");
+    }
+    inline unsigned jacobian_order(double factor, unsigned order) { return (unsigned)(factor * order); }
+    template <class JSON> double setting(const JSON &json, const char *key)
+    {
+      return json.get_double(std::string("/integration/") + key);
+    }
+
+    // "[logname] <title>:" and one "<label>: <value>" line per row, labels right-aligned in
+    // label_width, values in value_width (0: as printed)
+    struct ParamRow {
+      const char *label;
+      std::string value;
+    };
+    template <typename V> ParamRow row(const char *label, const V &v)
+    {
+      std::ostringstream o;
+      o << v;
+      return ParamRow{label, o.str()};
+    }
+    inline void log_rows(std::ostream &os, const std::string &logname, const char *title,
+                         std::initializer_list<ParamRow> rows, int label_width, int value_width)
+    {
+      std::ostringstream out;
+      out << title << ":";
+      for (const ParamRow &r : rows) {
+        out << "\n" << std::setw(label_width) << (std::string(r.label) + ": ");
+        if (value_width > 0)
+          out << std::setw(value_width) << r.value;
+        else
+          out << r.value;
+      }
+      os << "[" << logname << "] " << out.str() << std::endl;
+    }
+
     // optimize_x vanishes at x = 1 + 1e-3 + (1.5^i - 1), i < 10 (flow_equations.cc:70-79)
     inline bool vanishes_on_probe(const std::function<double(double)> &f)
     {
@@ -103,19 +143,19 @@ namespace DiFfRG
   class FlowEquations
   {
   protected:
+    // members in declaration order: each rule from its order, the jacobian rules from the
+    // factor, x_extent starts at 1 and is fitted at once
     template <class JSON>
     FlowEquations(const JSON &json, std::function<double(double)> optimize_x)
-        : x_quadrature_order(json.get_uint("/integration/x_quadrature_order")),
-          x_quadrature(QGauss<1>(x_quadrature_order)), x_extent(1.),
-          angle_quadrature_order(json.get_uint("/integration/angle_quadrature_order")),
-          angle_quadrature(QGauss<1>(angle_quadrature_order)),
-          jacobian_quadrature_factor(json.get_double("/integration/jacobian_quadrature_factor")),
-          jac_x_quadrature_order(jacobian_quadrature_factor * x_quadrature_order),
-          jac_x_quadrature(QGauss<1>(jac_x_quadrature_order)),
-          jac_angle_quadrature_order(jacobian_quadrature_factor * angle_quadrature_order),
-          jac_angle_quadrature(QGauss<1>(jac_angle_quadrature_order)),
-          x_extent_tolerance(json.get_double("/integration/x_extent_tolerance")), optimize_x(optimize_x), k(1),
-          unoptimized(true), verbosity(json.get_int("/output/verbosity"))
+        : x_quadrature_order(gbint_detail::rule_order(json, "x")), x_quadrature(x_quadrature_order), x_extent(1.),
+          angle_quadrature_order(gbint_detail::rule_order(json, "angle")), angle_quadrature(angle_quadrature_order),
+          jacobian_quadrature_factor(gbint_detail::setting(json, "jacobian_quadrature_factor")),
+          jac_x_quadrature_order(gbint_detail::jacobian_order(jacobian_quadrature_factor, x_quadrature_order)),
+          jac_x_quadrature(jac_x_quadrature_order),
+          jac_angle_quadrature_order(gbint_detail::jacobian_order(jacobian_quadrature_factor, angle_quadrature_order)),
+          jac_angle_quadrature(jac_angle_quadrature_order),
+          x_extent_tolerance(gbint_detail::setting(json, "x_extent_tolerance")), optimize_x(std::move(optimize_x)),
+          k(1), unoptimized(true), verbosity(json.get_int("/output/verbosity"))
     {
       update_x_extent();
       unoptimized = false;
@@ -125,16 +165,16 @@ namespace DiFfRG
   public:
     void set_k(const double k) { this->k = k; }
 
+    // the reference's log layout: labels right-aligned in 40 columns, values in 10
     void print_parameters(const std::string logname, std::ostream &os = std::cout) const
     {
-      std::stringstream stream;
-      stream << "FlowEquations:" << "\n"
-             << std::setw(40) << "x_quadrature_order: " << std::setw(10) << x_quadrature_order << "\n"
-             << std::setw(40) << "jac_x_quadrature_order: " << std::setw(10) << jac_x_quadrature_order << "\n"
-             << std::setw(40) << "x_extent: " << std::setw(10) << x_extent << "\n"
-             << std::setw(40) << "angle_quadrature_order: " << std::setw(10) << angle_quadrature_order << "\n"
-             << std::setw(40) << "jac_angle_quadrature_order: " << std::setw(10) << jac_angle_quadrature_order;
-      os << "[" << logname << "] " << stream.str() << std::endl;
+      using gbint_detail::row;
+      gbint_detail::log_rows(os, logname, "FlowEquations",
+                             {row("x_quadrature_order", x_quadrature_order),
+                              row("jac_x_quadrature_order", jac_x_quadrature_order), row("x_extent", x_extent),
+                              row("angle_quadrature_order", angle_quadrature_order),
+                              row("jac_angle_quadrature_order", jac_angle_quadrature_order)},
+                             40, 10);
     }
 
     template <typename NT, int d, typename FUN> NT integrate(const FUN &fun) const { return integrate<NT, d>(fun, k); }
@@ -225,33 +265,30 @@ namespace DiFfRG
   class FlowEquationsFiniteT
   {
   protected:
+    // members in declaration order, as in FlowEquations, with the x0 and q0 axes (summands,
+    // rule, extent 0 until fitted) and the temperature
     template <class JSON>
     FlowEquationsFiniteT(const JSON &json, const double T, std::function<double(double)> optimize_x,
                          std::function<double(double)> optimize_x0, std::function<double(double)> optimize_q0)
-        : x_quadrature_order(json.get_uint("/integration/x_quadrature_order")),
-          x_quadrature(QGauss<1>(x_quadrature_order)), x_extent(1.),
-          x0_summands(json.get_uint("/integration/x0_summands")),
-          x0_quadrature_order(json.get_uint("/integration/x0_quadrature_order")),
-          x0_quadrature(QGauss<1>(x0_quadrature_order)), x0_extent(0),
-          q0_summands(json.get_uint("/integration/q0_summands")),
-          q0_quadrature_order(json.get_uint("/integration/q0_quadrature_order")),
-          q0_quadrature(QGauss<1>(q0_quadrature_order)), q0_extent(0),
-          angle_quadrature_order(json.get_uint("/integration/angle_quadrature_order")),
-          angle_quadrature(QGauss<1>(angle_quadrature_order)),
-          jacobian_quadrature_factor(json.get_double("/integration/jacobian_quadrature_factor")),
-          jac_x_quadrature_order(jacobian_quadrature_factor * x_quadrature_order),
-          jac_x_quadrature(QGauss<1>(jac_x_quadrature_order)),
-          jac_x0_quadrature_order(jacobian_quadrature_factor * x0_quadrature_order),
-          jac_x0_quadrature(QGauss<1>(jac_x0_quadrature_order)),
-          jac_q0_quadrature_order(jacobian_quadrature_factor * q0_quadrature_order),
-          jac_q0_quadrature(QGauss<1>(jac_q0_quadrature_order)),
-          jac_angle_quadrature_order(jacobian_quadrature_factor * angle_quadrature_order),
-          jac_angle_quadrature(QGauss<1>(jac_angle_quadrature_order)),
-          x_extent_tolerance(json.get_double("/integration/x_extent_tolerance")),
-          x0_extent_tolerance(json.get_double("/integration/x0_extent_tolerance")),
-          q0_extent_tolerance(json.get_double("/integration/q0_extent_tolerance")), T(T), optimize_x(optimize_x),
-          optimize_x0(optimize_x0), optimize_q0(optimize_q0), k(1.), unoptimized(true),
-          verbosity(json.get_int("/output/verbosity"))
+        : x_quadrature_order(gbint_detail::rule_order(json, "x")), x_quadrature(x_quadrature_order), x_extent(1.),
+          x0_summands(json.get_uint("/integration/x0_summands")), x0_quadrature_order(gbint_detail::rule_order(json, "x0")),
+          x0_quadrature(x0_quadrature_order), x0_extent(0), q0_summands(json.get_uint("/integration/q0_summands")),
+          q0_quadrature_order(gbint_detail::rule_order(json, "q0")), q0_quadrature(q0_quadrature_order), q0_extent(0),
+          angle_quadrature_order(gbint_detail::rule_order(json, "angle")), angle_quadrature(angle_quadrature_order),
+          jacobian_quadrature_factor(gbint_detail::setting(json, "jacobian_quadrature_factor")),
+          jac_x_quadrature_order(gbint_detail::jacobian_order(jacobian_quadrature_factor, x_quadrature_order)),
+          jac_x_quadrature(jac_x_quadrature_order),
+          jac_x0_quadrature_order(gbint_detail::jacobian_order(jacobian_quadrature_factor, x0_quadrature_order)),
+          jac_x0_quadrature(jac_x0_quadrature_order),
+          jac_q0_quadrature_order(gbint_detail::jacobian_order(jacobian_quadrature_factor, q0_quadrature_order)),
+          jac_q0_quadrature(jac_q0_quadrature_order),
+          jac_angle_quadrature_order(gbint_detail::jacobian_order(jacobian_quadrature_factor, angle_quadrature_order)),
+          jac_angle_quadrature(jac_angle_quadrature_order),
+          x_extent_tolerance(gbint_detail::setting(json, "x_extent_tolerance")),
+          x0_extent_tolerance(gbint_detail::setting(json, "x0_extent_tolerance")),
+          q0_extent_tolerance(gbint_detail::setting(json, "q0_extent_tolerance")), T(T),
+          optimize_x(std::move(optimize_x)), optimize_x0(std::move(optimize_x0)), optimize_q0(std::move(optimize_q0)),
+          k(1.), unoptimized(true), verbosity(json.get_int("/output/verbosity"))
     {
       update_x_extent();
       if (x0_summands > 0) update_x0_extent();
@@ -263,23 +300,19 @@ namespace DiFfRG
   public:
     void set_k(const double k) { this->k = k; }
 
+    // the reference's log layout: labels right-aligned in 10 columns, values as printed
     void print_parameters(const std::string logname, std::ostream &os = std::cout) const
     {
-      std::stringstream stream;
-      stream << "FlowEquationsFiniteT:" << "\n"
-             << std::setw(47) << std::setw(10) << "x_quadrature_order: " << x_quadrature_order << "\n"
-             << std::setw(47) << std::setw(10) << "jac_x_quadrature_order: " << jac_x_quadrature_order << "\n"
-             << std::setw(47) << std::setw(10) << "x_extent: " << x_extent << "\n"
-             << std::setw(47) << std::setw(10) << "x0_quadrature_order: " << x0_quadrature_order << "\n"
-             << std::setw(47) << std::setw(10) << "jac_x0_quadrature_order: " << jac_x0_quadrature_order << "\n"
-             << std::setw(47) << std::setw(10) << "x0_extent: " << x0_extent << "\n"
-             << std::setw(47) << std::setw(10) << "q0_quadrature_order: " << q0_quadrature_order << "\n"
-             << std::setw(47) << std::setw(10) << "jac_q0_quadrature_order: " << jac_q0_quadrature_order << "\n"
-             << std::setw(47) << std::setw(10) << "q0_extent: " << q0_extent << "\n"
-             << std::setw(47) << std::setw(10) << "angle_quadrature_order: " << angle_quadrature_order << "\n"
-             << std::setw(47) << std::setw(10) << "jac_angle_quadrature_order: " << jac_angle_quadrature_order << "\n"
-             << std::setw(47) << std::setw(10) << "T: " << T;
-      os << "[" << logname << "] " << stream.str() << std::endl;
+      using gbint_detail::row;
+      gbint_detail::log_rows(
+          os, logname, "FlowEquationsFiniteT",
+          {row("x_quadrature_order", x_quadrature_order), row("jac_x_quadrature_order", jac_x_quadrature_order),
+           row("x_extent", x_extent), row("x0_quadrature_order", x0_quadrature_order),
+           row("jac_x0_quadrature_order", jac_x0_quadrature_order), row("x0_extent", x0_extent),
+           row("q0_quadrature_order", q0_quadrature_order), row("jac_q0_quadrature_order", jac_q0_quadrature_order),
+           row("q0_extent", q0_extent), row("angle_quadrature_order", angle_quadrature_order),
+           row("jac_angle_quadrature_order", jac_angle_quadrature_order), row("T", T)},
+          10, 0);
     }
 
     template <typename NT, int d, typename FUN> NT integrate(const FUN &fun) const { return integrate<NT, d>(fun, k); }

@@ -15,6 +15,8 @@
 //                              -> "x_extent" of a FlowEquations, or "throw <message>"
 //   fet x_order angle_order jac_factor x_tol x0_order x0_tol x0_summands q0_order q0_tol q0_summands T FX FX0 FQ0
 //                              -> "x_extent x0_extent q0_extent" of a FlowEquationsFiniteT
+//   fe ... FX print / fet ... FQ0 print
+//                              -> the print_parameters log with '|' for the newlines
 //   jac x_order angle_order jac_factor x_tol FX k
 //                              -> "a b": FlowEquations::integrate<AD,4>(FX) for a result type AD
 //        marked for the jacobian rules, and LoopIntegrals::integrate<double,4> over
@@ -223,7 +225,15 @@ int main()
                {"/integration/jacobian_quadrature_factor", jf}, {"/integration/x_extent_tolerance", tol},
                {"/output/verbosity", 0}};
         Flow flow(j, named(fx));
-        if (mode == "fe") {
+        std::string extra;
+        if (mode == "fe" && (in >> extra) && extra == "print") {  // the parameter log, '|' for newlines
+          std::ostringstream log;
+          flow.print_parameters("log", log);
+          std::string t = log.str();
+          for (char &c : t)
+            if (c == '\n') c = '|';
+          std::printf("%s\n", t.c_str());
+        } else if (mode == "fe") {
           std::printf("%.17g\n", flow.xe());
         } else {
           double k;
@@ -247,7 +257,16 @@ int main()
                {"/integration/q0_extent_tolerance", q0t},   {"/integration/q0_summands", q0s},
                {"/output/verbosity", 0}};
         FlowT flow(j, T, named(fx), named(fx0), named(fq0));
-        std::printf("%.17g %.17g %.17g\n", flow.xe(), flow.x0e(), flow.q0e());
+        std::string extra;
+        if ((in >> extra) && extra == "print") {
+          std::ostringstream log;
+          flow.print_parameters("log", log);
+          std::string t = log.str();
+          for (char &c : t)
+            if (c == '\n') c = '|';
+          std::printf("%s\n", t.c_str());
+        } else
+          std::printf("%.17g %.17g %.17g\n", flow.xe(), flow.x0e(), flow.q0e());
       } else {
         std::printf("error unknown mode %s\n", mode.c_str());
       }

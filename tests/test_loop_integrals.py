@@ -322,6 +322,21 @@ def test_finite_T_extent_fits_match_the_restated_fits(driver, x0s, q0s):
     assert q0e == (L.fit_q0_extent(FX["gauss0"], 16, 1e-3, rxe)[0] if q0s else 0.0)
 
 
+def test_print_parameters_layout(driver):
+    """The parameter logs in the reference's layout (S/physics/flow_equations.cc print_parameters):
+    FlowEquations labels right-aligned in 40 columns and values in 10; FlowEquationsFiniteT labels
+    right-aligned in 10 columns, values as printed."""
+    line = run(driver, ["fe 16 8 2 1e-3 gauss print"])[0]
+    xe = float(run(driver, ["fe 16 8 2 1e-3 gauss"])[0])
+    rows = [("x_quadrature_order", "16"), ("jac_x_quadrature_order", "32"), ("x_extent", "%g" % xe),
+            ("angle_quadrature_order", "8"), ("jac_angle_quadrature_order", "16")]
+    want = "[log] FlowEquations:" + "".join("|%40s%10s" % (k + ": ", v) for k, v in rows) + "|"
+    assert line == want, (line, want)
+    line = run(driver, ["fet 32 8 2 1e-3 16 1e-4 0 16 1e-3 0 0.1 gauss rational0 gauss0 print"])[0]
+    assert line.startswith("[log] FlowEquationsFiniteT:|x_quadrature_order: 32|jac_x_quadrature_order: 64|")
+    assert line.endswith("|jac_angle_quadrature_order: 16|%10s0.1|" % "T: "), line
+
+
 def test_marked_result_types_take_the_jacobian_rules(driver):
     a, b = (float(t) for t in run(driver, ["jac 16 8 2 1e-3 rational 0.8"])[0].split())
     assert a == b
