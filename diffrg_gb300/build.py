@@ -21,7 +21,7 @@ OUT_DIR = os.path.join(HERE, "lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgbint.so")
 
-SOURCES = ["engine.cu", "kernels_generic.cu", "kernels_fp32c.cu", "host_quadrature.cc", "serve.cc", "noalloc.cu",
+SOURCES = ["engine.cu", "kernels_generic.cu", "kernels_fp32c.cu", "host_quadrature.cc", "serve.cc", "dloop.cu", "noalloc.cu",
            "slots.cu", "autotune.cc", "trace.cc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -31,7 +31,7 @@ EXPORTS = [
     "gb_table_destroy",
     "gb_batch_create", "gb_batch_run", "gb_batch_run_graph", "gb_batch_results", "gb_batch_get",
     "gb_batch_run_plain", "gb_batch_info", "gb_batch_destroy", "gb_get", "gb_get_noalloc",
-    "gb_serve_start", "gb_serve_stop", "gb_submit", "gb_poll", "gb_wait", "gb_cancel",
+    "gb_serve_start", "gb_serve_start_device", "gb_serve_device_info", "gb_serve_stop", "gb_submit", "gb_poll", "gb_wait", "gb_cancel",
     "gb_get_stats", "gb_reset_stats", "gb_measure_peaks",
     "gb_buffer_create", "gb_buffer_upload", "gb_buffer_destroy",
     "gb_slot_acquire", "gb_slot_wait", "gb_slot_release", "gb_slot_host", "gb_device_info",
@@ -116,6 +116,8 @@ def load(path: str = LIB_PATH):
     L.gb_get_noalloc.argtypes = [vp, C.POINTER(Integral), C.POINTER(vp), C.c_int, dp]
     L.gb_serve_start.argtypes = [vp, C.c_int, C.c_int]
     L.gb_serve_stop.argtypes = [vp]
+    L.gb_serve_start_device.argtypes = [vp, C.c_int, C.c_int, C.c_longlong, C.c_double]
+    L.gb_serve_device_info.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.gb_submit.argtypes = [vp, C.POINTER(Integral), C.c_int, C.POINTER(vp), C.c_int, C.c_int,
                             C.POINTER(C.c_uint64)]
     L.gb_poll.argtypes = [vp, C.c_uint64, dp]

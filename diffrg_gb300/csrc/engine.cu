@@ -1108,6 +1108,7 @@ int gb_ctx_destroy(gb_ctx *ctx)
 {
   if (!ctx) return GB_EINVAL;
   if (ctx->serve) serve_stop(ctx);
+  if (ctx->dloop) dloop_stop(ctx);
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
   destroy_slots(ctx);
@@ -1441,6 +1442,10 @@ static int table_update_impl(gb_ctx *ctx, gb_table *t, const float *src, cudaMem
     const int rc = serve_fence_tables(ctx, s);
     if (rc) return rc;
   }
+  if (ctx->dloop) {
+    const int rc = dloop_fence_tables(ctx);
+    if (rc) return rc;
+  }
   GB_CUDA(cudaMemcpyAsync(t->buf[back], src, (size_t)t->elems * 4, kind, s));
   // publish the new buffer in the directory, ordered after the data on the same stream (the
   // host copy of the entry changes only once the device write is enqueued)
@@ -1504,6 +1509,10 @@ int gb_table_update_many(gb_ctx *ctx, int n, gb_table *const *tables, const floa
   // serving batches still reading the back buffers (an older epoch) finish first
   if (ctx->serve) {
     const int rc = serve_fence_tables(ctx, s);
+    if (rc) return rc;
+  }
+  if (ctx->dloop) {
+    const int rc = dloop_fence_tables(ctx);
     if (rc) return rc;
   }
   std::vector<TableDev> dir(n);
@@ -1795,18 +1804,62 @@ int gb_get(gb_ctx *ctx, const gb_integral *item, gb_table *const *tables, int n_
 }
 
 // ------------------------------------------------------------------ serving
-int gb_serve_start(gb_ctx *ctx, int max_inflight, int max_items) { return serve_start(ctx, max_inflight, max_items); }
-int gb_serve_stop(gb_ctx *ctx) { return serve_stop(ctx); }
+int gb_serve_start(gb_ctx *ctx, int max_inflight, int max_items)
+{
+  if (ctx && ctx->dloop) return set_error(ctx, GB_EINVAL, "serving already started");
+  return serve_start(ctx, max_inflight, max_items);
+}
+int gb_serve_start_device(gb_ctx *ctx, int ring_slots, int max_items, long long max_units, double idle_seconds)
+{
+  return dloop_start(ctx, ring_slots, max_items, max_units, idle_seconds);
+}
+int gb_serve_device_info(gb_ctx *ctx, long long *launches, int *idle_exits, int *running)
+{
+  if (!ctx) return GB_EINVAL;
+  if (!ctx->dloop) return set_error(ctx, GB_EINVAL, "device request loop not started (gb_serve_start_device)");
+  return dloop_info(ctx, launches, idle_exits, running);
+}
+int gb_serve_stop(gb_ctx *ctx)
+{
+  if (ctx && ctx->dloop) return dloop_stop(ctx);
+  return serve_stop(ctx);
+}
 int gb_submit(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
               gb_ticket *out)
 {
+  if (ctx && ctx->dloop) return dloop_submit(ctx, items, n, tables, n_tables, precision, out);
   return serve_submit(ctx, items, n, tables, n_tables, precision, out);
 }
-int gb_poll(gb_ctx *ctx, gb_ticket t, double *out) { return serve_poll(ctx, t, out, false, 0.0); }
-int gb_wait(gb_ctx *ctx, gb_ticket t, double *out, double timeout_s) { return serve_poll(ctx, t, out, true, timeout_s); }
-int gb_cancel(gb_ctx *ctx, gb_ticket t) { return serve_cancel(ctx, t); }
-int gb_get_stats(gb_ctx *ctx, gb_stats *out) { return serve_stats(ctx, out); }
-int gb_reset_stats(gb_ctx *ctx) { return serve_reset_stats(ctx); }
+int gb_poll(gb_ctx *ctx, gb_ticket t, double *out)
+{
+  if (ctx && ctx->dloop) return dloop_poll(ctx, t, out, false, 0.0);
+  return serve_poll(ctx, t, out, false, 0.0);
+}
+int gb_wait(gb_ctx *ctx, gb_ticket t, double *out, double timeout_s)
+{
+  if (ctx && ctx->dloop) return dloop_poll(ctx, t, out, true, timeout_s);
+  return serve_poll(ctx, t, out, true, timeout_s);
+}
+int gb_cancel(gb_ctx *ctx, gb_ticket t)
+{
+  if (ctx && ctx->dloop) return GB_EAGAIN;  // published at submit: already on the GPU
+  return serve_cancel(ctx, t);
+}
+int gb_get_stats(gb_ctx *ctx, gb_stats *out)
+{
+  if (ctx && ctx->dloop && out) {
+    *out = gb_stats{};
+    out->bytes_in_use = ctx->in_use;
+    out->bytes_budget = ctx->budget;
+    return dloop_stats(ctx, out);
+  }
+  return serve_stats(ctx, out);
+}
+int gb_reset_stats(gb_ctx *ctx)
+{
+  if (ctx && ctx->dloop) return dloop_reset_stats(ctx);
+  return serve_reset_stats(ctx);
+}
 
 int gb_selftest_wait(gb_ctx *ctx, long long max_cycles)
 {

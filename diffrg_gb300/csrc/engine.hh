@@ -70,6 +70,7 @@ namespace gbint
 
   struct Ticket;
   struct ServeState;
+  struct DLoopState;
   struct SlotPool;
 } // namespace gbint
 
@@ -156,6 +157,8 @@ struct gb_ctx {
   double *plain_res_h = nullptr;   // pinned host
   // serving
   gbint::ServeState *serve = nullptr;
+  // device-resident request loop (dloop.cu), the other serving mode
+  gbint::DLoopState *dloop = nullptr;
   // request slots of the C++ class templates
   gbint::SlotPool *slotpool = nullptr;
   // gb_buffer_* allocations and their sizes
@@ -187,6 +190,16 @@ namespace gbint
   int serve_cancel(gb_ctx *ctx, gb_ticket t);
   int serve_stats(gb_ctx *ctx, gb_stats *out);
   int serve_reset_stats(gb_ctx *ctx);
+  // device-resident request loop
+  int dloop_start(gb_ctx *ctx, int ring_slots, int max_items, long long max_units, double idle_s);
+  int dloop_stop(gb_ctx *ctx);
+  int dloop_fence_tables(gb_ctx *ctx);
+  int dloop_submit(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
+                   gb_ticket *out);
+  int dloop_poll(gb_ctx *ctx, gb_ticket t, double *out, bool wait, double timeout_s);
+  int dloop_stats(gb_ctx *ctx, gb_stats *out);
+  int dloop_reset_stats(gb_ctx *ctx);
+  int dloop_info(gb_ctx *ctx, long long *launches, int *idle_exits, int *running);
   void destroy_slots(gb_ctx *ctx);
 } // namespace gbint
 

@@ -333,6 +333,18 @@ class Context:
         queued requests up to `max_items` integrals."""
         self.check(capi.lib().gb_serve_start(self.h, max_inflight, max_items))
 
+    def serve_start_device(self, ring_slots: int = 16, max_items: int = 2048, max_units: int = 1 << 21,
+                           idle_seconds: float = 5e-3):
+        """The device-resident request loop (gb_serve_start_device): gb_submit / Ticket.wait then
+        go through a ring the GPU's persistent loop kernel reads; FP64 results."""
+        self.check(capi.lib().gb_serve_start_device(self.h, ring_slots, max_items, max_units, idle_seconds))
+
+    def device_loop_info(self) -> dict:
+        """{"launches", "idle_exits", "running"} of the device-resident request loop."""
+        la, ex, ru = C.c_longlong(), C.c_int(), C.c_int()
+        self.check(capi.lib().gb_serve_device_info(self.h, C.byref(la), C.byref(ex), C.byref(ru)))
+        return {"launches": la.value, "idle_exits": ex.value, "running": bool(ru.value)}
+
     def serve_stop(self):
         self.check(capi.lib().gb_serve_stop(self.h))
 

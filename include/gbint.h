@@ -315,6 +315,23 @@ int gb_graph_destroy(gb_ctx *ctx, gb_graph *g);
  * gb_get_stats: counts, busy time, p50/p99/max latency (submit -> result ready, nearest rank)
  *   since gb_serve_start / gb_reset_stats, and the budget in use. */
 int gb_serve_start(gb_ctx *ctx, int max_inflight_batches, int max_batch_items);
+/* The device-resident request loop, the other serving mode (north star "serving": a loop on the
+ * GPU that takes request() calls as they arrive; replaces the same fan-out as gb_serve_start).
+ * gb_submit then writes each request straight into a ring the GPU reads (descriptors and a
+ * snapshot of its tables' directory entries in the request's ring slot, then the published
+ * work-unit count in mapped host memory); a persistent kernel claims published units of 1024
+ * grid points as CTAs free up, so requests arriving while others run are batched continuously;
+ * results and a done flag land in mapped host memory.  Requests are evaluated in FP64, equal to
+ * gb_get(..., GB_PREC_FP64) to rounding and bit-identical alone or in any mix.  ring_slots (1..64) requests in
+ * flight, each up to max_items integrals and max_units work units (device memory reserved at
+ * start against the HBM budget; larger requests: GB_EBUDGET); a request waits for its slot.  The
+ * loop leaves after idle_seconds without work (a bounded clock64 spin, counted as an idle exit)
+ * and is relaunched by the next gb_submit / gb_wait; table updates wait for published requests.
+ * gb_poll / gb_wait / gb_get_stats / gb_reset_stats / gb_serve_stop act on it as on the host
+ * loop; gb_cancel returns GB_EAGAIN (published at submit). */
+int gb_serve_start_device(gb_ctx *ctx, int ring_slots, int max_items, long long max_units, double idle_seconds);
+/* launches of the loop kernel so far, CTAs that left after the idle budget, whether it runs now */
+int gb_serve_device_info(gb_ctx *ctx, long long *launches, int *idle_exits, int *running);
 int gb_serve_stop(gb_ctx *ctx);
 int gb_submit(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
               gb_ticket *out);
