@@ -208,6 +208,7 @@ def workload_leg(name, ctx, stream, flush, steps, warmup, oracle_threads):
     n_int = len(items)
     T = [ctx.table(sp, d) for sp, d in tabs]
     ctx.autotune(items, T, "fp32c")
+    tune = ctx.tune_report()
     b32 = ctx.batch(items, T, "fp32c")
     points = b32.points
     for _ in range(warmup):
@@ -255,6 +256,7 @@ def workload_leg(name, ctx, stream, flush, steps, warmup, oracle_threads):
                                    "d2h_bytes_per_step": n_int * 8},
            "plain_fp64_gpu": {"value": n_int / plain_dt, "unit": UNIT, "ms_per_step": plain_dt * 1e3}}
     out["fp32c_over_plain_fp64"] = out["value"] / out["plain_fp64_gpu"]["value"]
+    out["autotune"] = tune
     if name in PER_POINT:
         F, S = PER_POINT[name]
         out["per_point"] = {"F": F, "S": S}
@@ -335,6 +337,54 @@ def serving_c4(device):
     b.close()
     f.close()
     ctx.close()
+    out["fp64_loops"] = serving_loops(device)
+    return out
+
+
+def serving_loops(device):
+    """One C4 right-hand side (4096 integrals, 1.12e9 points) in FP64 through the host dispatcher
+    (gb_serve_start) and through the device-resident loop (gb_serve_start_device), saturated and
+    with Poisson arrivals at 2000 integrals/s.  Both loops see the same request sizes and arrival
+    times (same seed); latency = submit -> result in host memory."""
+    from diffrg_gb300 import serving as SV
+    from diffrg_gb300.engine import Context
+
+    w = SV.c4()
+    out = {"workload": "C4 right-hand side in FP64 (4096 integrals in requests of 8-2048), same sizes and "
+                       "arrival times for both loops", "precision": "fp64"}
+    vals = {}
+    for name in ("host", "device"):
+        ctx = Context(device)
+        f = None
+        try:
+            if name == "host":
+                ctx.serve_start(8, 2048)
+            else:
+                ctx.serve_start_device(ring_slots=16, max_items=2048, max_units=1 << 21, idle_seconds=0.05)
+            f = SV.Flow(ctx, w, precision="fp64", rate=None)
+            f.integrals_at(0.0, w["y0"])  # warm-up: arenas, quadrature axes, module load
+            res = {}
+            for mode, rate in (("saturated", None), ("poisson", w["rate"])):
+                f.rate = rate
+                f.rng = np.random.default_rng(SV.SEEDS["C4"] + 11)
+                ctx.reset_stats()
+                t0 = time.perf_counter()
+                v = f.integrals_at(0.0, w["y0"])
+                wall = time.perf_counter() - t0
+                st = ctx.stats()
+                res[mode] = {"requests": st["completed"], "wall_s": wall, "integrals_per_s": v.size / wall,
+                             "p50_ms": st["p50_latency_s"] * 1e3, "p99_ms": st["p99_latency_s"] * 1e3,
+                             "max_ms": st["max_latency_s"] * 1e3}
+                vals[(name, mode)] = v.ravel()
+            if name == "device":
+                res["loop"] = ctx.device_loop_info()
+            out[name] = res
+        finally:
+            if f is not None:
+                f.close()
+            ctx.close()
+    a, b = vals[("host", "poisson")], vals[("device", "poisson")]
+    out["device_vs_host_max_rel_diff"] = float(np.max(np.abs(a - b) / np.abs(a)))
     return out
 
 
@@ -366,6 +416,7 @@ def main():
     T = [ctx.table(s, d) for s, d in tabs]
     # CTA widths of the FP32-compensated kernels for this GPU and workload (library autotuner)
     tuned = ctx.autotune(items, T, "fp32c")
+    tune_report = ctx.tune_report()
     b32 = ctx.batch(items, T, "fp32c")
     b64 = ctx.batch(items, T, "fp64")
     points = b32.points
@@ -552,7 +603,7 @@ def main():
             "latency_ms": {"batch_e2e_p50": pct(lat_ms, 0.5), "batch_e2e_p99": pct(lat_ms, 0.99),
                            "single_integral_get_p50": pct(sl_ms, 0.5), "single_integral_get_p99": pct(sl_ms, 0.99)},
             "accuracy": err,
-            "autotune": {"cta_threads_by_kind_slot": tuned},
+            "autotune": {"cta_threads_by_kind_slot": tuned, "report": tune_report},
             "serving": serve,
             "workloads": legs,
             "cpp_dropin": dropin,

@@ -36,7 +36,7 @@ EXPORTS = [
     "gb_buffer_create", "gb_buffer_upload", "gb_buffer_destroy",
     "gb_slot_acquire", "gb_slot_wait", "gb_slot_release", "gb_slot_host", "gb_device_info",
     "gb_graph_capture_begin", "gb_graph_capture_end", "gb_graph_launch", "gb_graph_info", "gb_graph_destroy",
-    "gb_autotune", "gb_tune_set", "gb_selftest_wait", "gb_table_group_begin", "gb_table_group_end",
+    "gb_autotune", "gb_tune_set", "gb_tune_set_schedule", "gb_tune_get_schedule", "gb_tune_report", "gb_selftest_wait", "gb_table_group_begin", "gb_table_group_end",
 ]
 
 
@@ -50,6 +50,13 @@ class Integral(C.Structure):
                 ("x_extent", C.c_double), ("x0_extent", C.c_double), ("x0_summands", C.c_int),
                 ("T", C.c_double), ("E", C.c_double), ("k", C.c_double),
                 ("qmin", C.c_double * 3), ("qmax", C.c_double * 3), ("args", C.c_double * GB_MAX_ARGS)]
+
+
+class Schedule(C.Structure):
+    _fields_ = [("threads", C.c_int), ("rows_per_thread", C.c_int), ("inner_split", C.c_int), ("unit_order", C.c_int)]
+
+
+GB_ORDER_ITEM, GB_ORDER_COST = 0, 1
 
 
 class Stats(C.Structure):
@@ -131,6 +138,9 @@ def load(path: str = LIB_PATH):
     L.gb_graph_launch.argtypes = [vp, vp, vp]
     L.gb_graph_info.argtypes = [vp, vp, C.POINTER(C.c_int)]
     L.gb_graph_destroy.argtypes = [vp, vp]
+    L.gb_tune_set_schedule.argtypes = [vp, C.c_int, C.POINTER(Schedule)]
+    L.gb_tune_get_schedule.argtypes = [vp, C.c_int, C.POINTER(Schedule)]
+    L.gb_tune_report.argtypes = [vp, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]
     L.gb_autotune.argtypes = [vp, C.POINTER(Integral), C.c_int, C.POINTER(vp), C.c_int, C.c_int, C.c_char_p, C.c_int,
                               C.POINTER(C.c_int)]
     L.gb_tune_set.argtypes = [vp, C.c_int, C.c_int]

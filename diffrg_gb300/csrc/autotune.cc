@@ -1,12 +1,17 @@
-// autotune.cc -- CTA-width autotuner of the FP32-compensated kernels.
+// autotune.cc -- work-unit schedule autotuner of the FP32-compensated kernels.
 //
-// The S kinds map one quadrature row to one thread and one CTA to one work unit, so the CTA
-// width fixes both the unit size (scheduling granularity of the persistent grid) and the
-// occupancy.  gb_autotune times every width the kernels are built for (128, 256, 512) on the
-// caller's integrals, kind by kind, and keeps the fastest in the context; batches created
-// afterwards use it.  Choices are cached per GPU model in a text file (one line per kind slot:
-// "<gpu name>|<SM count>|<slot>|<threads>|<ms>", slot = base kind + 8 for the double-float form),
-// so that a later process on the same model skips the timing.
+// The S kinds map quadrature rows to threads and CTAs to work units that a persistent grid
+// claims from an atomic counter.  A schedule (gb_schedule) fixes the CTA width, the rows per
+// thread of a unit (together: the unit size, i.e. the scheduling granularity, and the
+// occupancy), the split of each row's inner loop over several threads (S3, S5Z: more threads
+// per row for integrals with few rows and long inner loops), and the order the units go out in
+// (item order, or largest cost first against the tail of uneven batches).  gb_autotune times
+// the parameters one at a time on the caller's integrals, kind by kind, each at the best of the
+// ones before, keeps the fastest in the context and records every measurement for
+// gb_tune_report.  Choices are cached per GPU model in a text file (one line per kind slot:
+// "<gpu name>|<SM count>|<slot>|<threads>|<ms>|<rows per thread>|<split>|<order>", slot = base
+// kind + 8 for the double-float form), so that a later process on the same model skips the
+// timing.
 #include "engine.hh"
 #include "kernels.hh"
 #include "trace.hh"
@@ -15,12 +20,22 @@
 #include <cstdio>
 #include <fstream>
 #include <sstream>
+#include <tuple>
 
 namespace gbint
 {
   namespace
   {
     constexpr int kCandidates[3] = {128, 256, 512};
+    constexpr int kRowsPerThread[3] = {1, 2, 4};
+    constexpr int kSplits[3] = {1, 2, 4};
+    // a candidate replaces the incumbent only when it is faster by more than this fraction
+    constexpr double kMargin = 0.01;
+
+    template <size_t N> bool one_of(int v, const int (&set)[N])
+    {
+      return std::find(std::begin(set), std::end(set), v) != std::end(set);
+    }
 
     std::string gpu_key(gb_ctx *ctx)
     {
@@ -31,10 +46,10 @@ namespace gbint
       return name + "|" + std::to_string(ctx->num_sms);
     }
 
-    // cache lines "<gpu>|<sms>|<slot>|<threads>|<ms>" -> slot -> threads
-    std::map<int, int> read_cache(const char *path, const std::string &gpu)
+    // cache lines "<gpu>|<sms>|<slot>|<threads>|<ms>[|<rows per thread>|<split>|<order>]"
+    std::map<int, gb_schedule> read_cache(const char *path, const std::string &gpu)
     {
-      std::map<int, int> m;
+      std::map<int, gb_schedule> m;
       if (!path) return m;
       std::ifstream f(path);
       std::string line;
@@ -44,14 +59,20 @@ namespace gbint
         std::string t;
         while (std::getline(ss, t, '|')) tok.push_back(t);
         if (tok.size() < 4 || tok[0] + "|" + tok[1] != gpu) continue;
-        const int slot = std::atoi(tok[2].c_str()), th = std::atoi(tok[3].c_str());
-        if (slot >= 0 && slot < 16 && std::find(std::begin(kCandidates), std::end(kCandidates), th) != std::end(kCandidates))
-          m[slot] = th;
+        gb_schedule sc{};
+        const int slot = std::atoi(tok[2].c_str());
+        sc.threads = std::atoi(tok[3].c_str());
+        sc.rows_per_thread = tok.size() > 5 ? std::atoi(tok[5].c_str()) : 1;
+        sc.inner_split = tok.size() > 6 ? std::atoi(tok[6].c_str()) : 1;
+        sc.unit_order = tok.size() > 7 ? std::atoi(tok[7].c_str()) : GB_ORDER_ITEM;
+        if (slot >= 0 && slot < 16 && one_of(sc.threads, kCandidates) && one_of(sc.rows_per_thread, kRowsPerThread) &&
+            one_of(sc.inner_split, kSplits) && (sc.unit_order == GB_ORDER_ITEM || sc.unit_order == GB_ORDER_COST))
+          m[slot] = sc;
       }
       return m;
     }
 
-    void write_cache(const char *path, const std::string &gpu, const std::map<int, std::pair<int, double>> &best)
+    void write_cache(const char *path, const std::string &gpu, const std::map<int, std::pair<gb_schedule, double>> &best)
     {
       if (!path) return;
       std::vector<std::string> keep;
@@ -67,7 +88,19 @@ namespace gbint
       }
       std::ofstream f(path, std::ios::trunc);
       for (const auto &l : keep) f << l << "\n";
-      for (const auto &kv : best) f << gpu << "|" << kv.first << "|" << kv.second.first << "|" << kv.second.second << "\n";
+      for (const auto &kv : best) {
+        const gb_schedule &sc = kv.second.first;
+        f << gpu << "|" << kv.first << "|" << sc.threads << "|" << kv.second.second << "|" << sc.rows_per_thread << "|"
+          << sc.inner_split << "|" << sc.unit_order << "\n";
+      }
+    }
+
+    std::string sched_json(const gb_schedule &s)
+    {
+      char b[160];
+      std::snprintf(b, sizeof b, "{\"threads\": %d, \"rows_per_thread\": %d, \"inner_split\": %d, \"unit_order\": \"%s\"}",
+                    s.threads, s.rows_per_thread, s.inner_split, s.unit_order == GB_ORDER_COST ? "cost" : "item");
+      return b;
     }
 
     int slot_of(int kind) { return kind_base(kind) + (kind_acc(kind) ? 8 : 0); }
@@ -143,55 +176,147 @@ extern "C" int gb_autotune(gb_ctx *ctx, const gb_integral *items, int n, gb_tabl
       if (p) cudaFree(p);
     }
   } free_flush{flush};
-  const std::map<int, int> cached = (flags & GB_TUNE_REFRESH) ? std::map<int, int>{} : read_cache(cache_path, gpu);
-  std::map<int, std::pair<int, double>> best;
+  const std::map<int, gb_schedule> cached =
+      (flags & GB_TUNE_REFRESH) ? std::map<int, gb_schedule>{} : read_cache(cache_path, gpu);
+  std::map<int, std::pair<gb_schedule, double>> best;
+  std::string report = "{\"gpu\": \"" + gpu + "\", \"kinds\": [";
+  bool first_kind = true;
   for (int kind : kinds) {
-    const int slot = slot_of(kind);
+    const int slot = kind_base(kind) + (kind_acc(kind) ? 8 : 0);
+    const gb_schedule saved = ctx->sched[slot];
     auto c = cached.find(slot);
     if (c != cached.end()) {
-      ctx->threads_override[slot] = c->second;
+      ctx->sched[slot] = c->second;
+      report += std::string(first_kind ? "" : ", ") + "{\"slot\": " + std::to_string(slot) +
+                ", \"cached\": true, \"chosen\": " + sched_json(resolve_schedule(ctx, kind)) + "}";
+      first_kind = false;
       continue;
     }
-    double best_ms = 1e300;
-    int best_t = kind_default_threads(kind);
-    for (int th : kCandidates) {
-      ctx->threads_override[slot] = th;
+    // median ms of one schedule (memoised); < 0 when the schedule cannot launch these integrals
+    std::map<std::tuple<int, int, int, int>, double> seen;
+    int rc = GB_OK;
+    auto time_of = [&](gb_schedule sc) -> double {
+      ctx->sched[slot] = sc;
+      const gb_schedule r = resolve_schedule(ctx, kind);
+      const auto key = std::make_tuple(r.threads, r.rows_per_thread, r.inner_split, r.unit_order);
+      auto it = seen.find(key);
+      if (it != seen.end()) return it->second;
       gb_batch *b = nullptr;
-      int rc = build_batch(ctx, items, n, tables, n_tables, precision, &b);
-      if (rc == GB_EINVAL) continue;  // this width cannot launch with these tables/records
-      if (rc) {
-        ctx->threads_override[slot] = 0;
-        return rc;
+      double ms = -1;
+      const int brc = build_batch(ctx, items, n, tables, n_tables, precision, &b);
+      if (brc == GB_OK) {
+        const int trc = time_batch(ctx, b, 9, ms, flush, flush_bytes);
+        cudaStreamSynchronize(ctx->stream);
+        free_batch(ctx, b);
+        if (trc) {
+          rc = trc;
+          ms = -1;
+        }
+      } else if (brc != GB_EINVAL) {  // GB_EINVAL: this shape cannot launch with these tables/records
+        rc = brc;
       }
-      double ms = 0;
-      rc = time_batch(ctx, b, 9, ms, flush, flush_bytes);
-      cudaStreamSynchronize(ctx->stream);
-      free_batch(ctx, b);
-      if (rc) {
-        ctx->threads_override[slot] = 0;
-        return rc;
+      seen[key] = ms;
+      return ms;
+    };
+    const gb_schedule def = kind_default_schedule(kind);
+    const double def_ms = time_of(def);
+    gb_schedule cur = def;
+    double cur_ms = def_ms;
+    std::string steps;
+    // one parameter at a time, each at the best of the previous ones
+    auto sweep = [&](const char *name, const int *vals, int nv, int gb_schedule::*field) {
+      std::string row = std::string("\"") + name + "\": [";
+      gb_schedule keep = cur;
+      for (int v = 0; v < nv && rc == GB_OK; ++v) {
+        gb_schedule sc = cur;
+        sc.*field = vals[v];
+        const double ms = time_of(sc);
+        char e[64];
+        std::snprintf(e, sizeof e, "%s[%d, %.4f]", v ? ", " : "", vals[v], ms);
+        row += e;
+        if (ms > 0 && (cur_ms <= 0 || ms < cur_ms * (1.0 - kMargin))) {
+          keep = sc;
+          cur_ms = ms;
+        }
       }
-      if (ms < best_ms) {
-        best_ms = ms;
-        best_t = th;
-      }
+      cur = keep;
+      steps += (steps.empty() ? "" : ", ") + row + "]";
+    };
+    sweep("threads", kCandidates, 3, &gb_schedule::threads);
+    sweep("rows_per_thread", kRowsPerThread, 3, &gb_schedule::rows_per_thread);
+    const int kb = kind_base(kind);
+    if (kb == K_S3 || kb == K_S3R || kb == K_S5Z) sweep("inner_split", kSplits, 3, &gb_schedule::inner_split);
+    static const int kOrders[2] = {GB_ORDER_ITEM, GB_ORDER_COST};
+    sweep("unit_order", kOrders, 2, &gb_schedule::unit_order);
+    if (rc) {
+      ctx->sched[slot] = saved;
+      return rc;
     }
-    ctx->threads_override[slot] = best_t;
-    best[slot] = {best_t, best_ms};
-    if (log_enabled()) log_event("autotune", jfields("\"slot\": %d, \"threads\": %d, \"ms\": %.4f", slot, best_t, best_ms));
+    if (cur_ms <= 0) cur = def;
+    ctx->sched[slot] = cur;
+    best[slot] = {cur, cur_ms};
+    char tail[160];
+    std::snprintf(tail, sizeof tail, ", \"default_ms\": %.4f, \"chosen_ms\": %.4f}", def_ms, cur_ms);
+    report += std::string(first_kind ? "" : ", ") + "{\"slot\": " + std::to_string(slot) +
+              ", \"cached\": false, \"default\": " + sched_json(def) + ", \"chosen\": " + sched_json(cur) +
+              ", \"steps\": {" + steps + "}" + tail;
+    first_kind = false;
+    if (log_enabled())
+      log_event("autotune", jfields("\"slot\": %d, \"threads\": %d, \"rows_per_thread\": %d, \"inner_split\": %d, "
+                                    "\"unit_order\": %d, \"ms\": %.4f, \"default_ms\": %.4f",
+                                    slot, cur.threads, cur.rows_per_thread, cur.inner_split, cur.unit_order, cur_ms,
+                                    def_ms));
   }
+  report += "]}";
+  ctx->tune_report = report;
   if (!best.empty()) write_cache(cache_path, gpu, best);
   if (chosen)
-    for (int k = 0; k < 16; ++k) chosen[k] = ctx->threads_override[k];
+    for (int k = 0; k < 16; ++k) chosen[k] = ctx->sched[k].threads;
   return GB_OK;
 }
 
 extern "C" int gb_tune_set(gb_ctx *ctx, int kind_slot, int threads)
 {
   if (!ctx || kind_slot < 0 || kind_slot >= 16) return GB_EINVAL;
-  if (threads != 0 && std::find(std::begin(kCandidates), std::end(kCandidates), threads) == std::end(kCandidates))
+  if (threads != 0 && !one_of(threads, kCandidates))
     return set_error(ctx, GB_EINVAL, "gb_tune_set: threads must be 0 (default), 128, 256 or 512");
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-  ctx->threads_override[kind_slot] = threads;
+  ctx->sched[kind_slot].threads = threads;
+  return GB_OK;
+}
+
+extern "C" int gb_tune_set_schedule(gb_ctx *ctx, int kind_slot, const gb_schedule *s)
+{
+  if (!ctx || !s || kind_slot < 0 || kind_slot >= 16) return GB_EINVAL;
+  if ((s->threads && !one_of(s->threads, kCandidates)) || (s->rows_per_thread && !one_of(s->rows_per_thread, kRowsPerThread)) ||
+      (s->inner_split && !one_of(s->inner_split, kSplits)) || (s->unit_order != GB_ORDER_ITEM && s->unit_order != GB_ORDER_COST))
+    return set_error(ctx, GB_EINVAL,
+                     "gb_tune_set_schedule: threads 0/128/256/512, rows_per_thread 0/1/2/4, inner_split 0/1/2/4, "
+                     "unit_order GB_ORDER_ITEM/GB_ORDER_COST");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  ctx->sched[kind_slot] = *s;
+  return GB_OK;
+}
+
+extern "C" int gb_tune_get_schedule(gb_ctx *ctx, int kind_slot, gb_schedule *out)
+{
+  if (!ctx || !out || kind_slot < 0 || kind_slot >= 16) return GB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  const int kind = (kind_slot & 7) | ((kind_slot & 8) ? K_ACC : 0);
+  *out = resolve_schedule(ctx, kind);
+  return GB_OK;
+}
+
+extern "C" int gb_tune_report(gb_ctx *ctx, char *buf, size_t cap, size_t *len)
+{
+  if (!ctx) return GB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  const std::string &r = ctx->tune_report.empty() ? std::string("{}") : ctx->tune_report;
+  if (len) *len = r.size();
+  if (buf && cap) {
+    const size_t m = std::min(cap - 1, r.size());
+    std::memcpy(buf, r.data(), m);
+    buf[m] = 0;
+  }
   return GB_OK;
 }

@@ -87,15 +87,16 @@ namespace gbint
     }
 
     // ------------------------------------------------------------------ per-integral finish
-    // Each unit stores its FP64 partial; the last unit of an item to arrive (atomic counter)
-    // sums the item's partials in unit order with the whole block -> deterministic result,
-    // identical whether the item ran alone or inside a larger batch.
-    __device__ __forceinline__ void unit_finish(const RunParams &P, int unit, int item_idx, double block_total,
+    // Each unit stores its FP64 partial in its slot (its position in item order, whatever order
+    // the units were claimed in); the last unit of an item to arrive (atomic counter) sums the
+    // item's partials in slot order with the whole block -> deterministic result, identical
+    // whether the item ran alone or inside a larger batch, and whatever the unit order.
+    __device__ __forceinline__ void unit_finish(const RunParams &P, int slot, int item_idx, double block_total,
                                                 double *red, int *s_flag)
     {
       const ItemDev &it = P.items[item_idx];
       if (threadIdx.x == 0) {
-        P.partials[unit] = block_total;
+        P.partials[slot] = block_total;
         __threadfence();
         const int prev = atomicAdd(&P.item_count[item_idx], 1);
         *s_flag = (prev == it.n_units - 1);

@@ -13,11 +13,15 @@
 // integral to arrive sums the integral's unit partials in unit order, so every result is
 // bit-identical alone and in any mix, and equals gb_get(..., GB_PREC_FP64) to rounding (the
 // same function and order, compiled into another kernel).  Results and a per-request
-// done flag go to mapped host memory, where gb_poll / gb_wait find them without a CUDA call.
+// done flag go to mapped host memory.  A watcher thread reads the done flags every 20 us while
+// requests are outstanding (it sleeps otherwise): it stamps each request's completion (latency =
+// submit -> results in host memory), frees its ring slot, and relaunches the kernel when work is
+// published but no loop runs; gb_poll / gb_wait then find the results without a CUDA call.
 //
 // Every wait is bounded.  A CTA that finds no published work polls with a clock64 budget (the
 // idle time given at start) and an iteration cap, then counts an idle exit and leaves; the host
-// relaunches the kernel when a request is published or waited for while no loop runs.  The loop
+// relaunches the kernel when a request is published, or (the watcher) when a request was
+// published just as the last CTA left.  The loop
 // also leaves (and is relaunched fresh) around table updates and after the node pool recycled
 // storage, so no CTA keeps stale L1 lines of a table buffer or node range the host rewrote.
 //
@@ -38,6 +42,8 @@
 #include <cstdint>
 #include <cstring>
 #include <chrono>
+#include <condition_variable>
+#include <thread>
 #include <cmath>
 #include <thread>
 
@@ -273,6 +279,10 @@ namespace gbint
     uint64_t submitted = 0, completed = 0, rejected = 0, points = 0;
     std::vector<double> lat;
     double t_start = 0;
+    // completion watcher (guarded by ctx->mu)
+    std::thread watcher;
+    std::condition_variable_any wake;
+    bool stop_watcher = false;
   };
 
   namespace
@@ -342,6 +352,27 @@ namespace gbint
       release_axes(ctx, k.held);
       D->slots[k.slot].busy = false;
       return true;
+    }
+
+    // the watcher: reaps finished requests as they finish and keeps a loop running while
+    // published work is outstanding
+    void watch(gb_ctx *ctx, DLoopState *D)
+    {
+      cudaSetDevice(ctx->device);
+      std::unique_lock<std::recursive_mutex> lk(ctx->mu);
+      while (!D->stop_watcher) {
+        bool pending = false;
+        for (auto &kv : D->tickets)
+          if (!kv.second.done && !reap(ctx, D, kv.first)) pending = true;
+        if (pending && !loop_running(D)) launch_loop(ctx, D);  // a failure resurfaces at gb_wait
+        if (pending) {
+          lk.unlock();
+          std::this_thread::sleep_for(std::chrono::microseconds(20));
+          lk.lock();
+        } else {
+          D->wake.wait_for(lk, std::chrono::milliseconds(50));
+        }
+      }
     }
 
     void free_state(DLoopState *D)
@@ -426,14 +457,21 @@ namespace gbint
     ctx->in_use += total;
     D->t_start = now_s();
     ctx->dloop = D.release();
+    ctx->dloop->watcher = std::thread(watch, ctx, ctx->dloop);
     return GB_OK;
   }
 
   int dloop_stop(gb_ctx *ctx)
   {
     if (!ctx || !ctx->dloop) return GB_OK;
-    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
     DLoopState *D = ctx->dloop;
+    {
+      std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+      D->stop_watcher = true;
+      D->wake.notify_all();
+    }
+    if (D->watcher.joinable()) D->watcher.join();
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
     // published requests finish first (the loop is relaunched for them if it left)
     const double deadline = now_s() + 30.0;
@@ -458,8 +496,7 @@ namespace gbint
     DLoopState *D = ctx->dloop;
     const double deadline = now_s() + 30.0;
     for (auto &kv : D->tickets) {
-      DLTicket &k = kv.second;
-      while (!k.done && D->h_map->done[k.slot] != k.seq) {
+      while (!reap(ctx, D, kv.first)) {
         if (now_s() > deadline) return set_error(ctx, GB_ETIMEDOUT, "table update: device-loop requests did not finish");
         if (!loop_running(D)) {
           const int rc = launch_loop(ctx, D);
@@ -602,6 +639,7 @@ namespace gbint
       const int rc = launch_loop(ctx, D);
       if (rc) return rc;
     }
+    D->wake.notify_all();
     *out = id;
     return GB_OK;
   }

@@ -580,6 +580,7 @@ namespace gbint
       break;
     }
     case K_S3:
+    case K_S3R:
       aux.push_back(df2(p, g.args[2]));                   // P, cos(theta)
       aux.push_back(df2(p * p, 0.25 * p * p));           // P^2, P^2 / 4
       aux.push_back(df2(g.args[3], 0.0));                 // sin(theta)
@@ -611,12 +612,58 @@ namespace gbint
     const int jspan = std::min(it.ax[1].n, (rpu - 1) / it.ax[0].n + 2);
     return it.ax[2].n + it.ax[3].n + (jspan * ns0 + 1) / 2;  // NodeRec units (32 B = 2 slice entries)
   }
+  // S3R: whether tables B, C, D carry cell records and B its regulator coefficients, and the
+  // bytes staged (B's coefficients, then each table's records and difference low words)
+  bool s3r_ready(const gb_ctx *ctx, const ItemDev &it)
+  {
+    for (int t = 1; t < 4; ++t) {
+      if (it.tab[t] < 0) return false;
+      const TableDev &D = ctx->h_dir[it.tab[t]];
+      if (!D.cr_off || D.n1 != 0) return false;
+    }
+    return ctx->h_dir[it.tab[1]].rq_off > 0;
+  }
+  int s3r_tab_bytes(const gb_ctx *ctx, const ItemDev &it)
+  {
+    int b = 48 * (ctx->h_dir[it.tab[1]].n0 - 1);
+    for (int t = 1; t < 4; ++t) {
+      const int c = ctx->h_dir[it.tab[t]].n0 - 1;
+      b += 16 * c + (4 * c + 15) / 16 * 16;
+    }
+    return b;
+  }
   size_t s5z_smem_bytes(const gb_ctx *ctx, const ItemDev &it, int rpu)
   {
     const size_t tab = ((size_t)s5z_tab_bytes(ctx, it) + 127) / 128 * 128;
     const size_t rec = ((size_t)s5z_rec_cap(ctx, it, rpu) + 3) / 4 * 4;
     return tab + 2 * rec * sizeof(NodeRec);
   }
+
+  gb_schedule resolve_schedule(const gb_ctx *ctx, int kind)
+  {
+    gb_schedule s = ctx->sched[kind_base(kind) + (kind_acc(kind) ? 8 : 0)];
+    const gb_schedule d = kind_default_schedule(kind);
+    if (s.threads <= 0) s.threads = d.threads;
+    if (s.rows_per_thread <= 0) s.rows_per_thread = d.rows_per_thread;
+    if (s.inner_split <= 0) s.inner_split = d.inner_split;
+    const int kb = kind_base(kind);
+    if (kb != K_S3 && kb != K_S3R && kb != K_S5Z) s.inner_split = 1;
+    if (s.unit_order != GB_ORDER_COST) s.unit_order = GB_ORDER_ITEM;
+    return s;
+  }
+
+  namespace
+  {
+    int log2_exact(int v)
+    {
+      int l = 0;
+      while ((1 << l) < v) ++l;
+      return l;
+    }
+
+    // quadrature rows a work unit of the schedule spans (before the inner split)
+    int base_rows_per_unit(const gb_schedule &s) { return s.threads * s.rows_per_thread / s.inner_split; }
+  } // namespace
 
   int plan_batch(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *const *item_tables,
                  const int *item_ntables, int precision, gb_batch *b)
@@ -702,7 +749,12 @@ namespace gbint
       // 4D vertex, accurate form: the 2D tables read through slices along their cos axis when
       // table A's slices at the c1 nodes of one work unit (double buffered) fit shared memory at
       // the widest CTA
-      if (kind == (K_S5 | K_ACC) && s5z_smem_bytes(ctx, it, 512) <= kS5zSmemLimit) kind = K_S5Z | K_ACC;
+      if (kind == (K_S5 | K_ACC) &&
+          s5z_smem_bytes(ctx, it, base_rows_per_unit(resolve_schedule(ctx, K_S5Z | K_ACC))) <= kS5zSmemLimit)
+        kind = K_S5Z | K_ACC;
+      // 3D loop, accurate form: the three point-dependent tables through their cell records
+      // when all three carry them and table B its regulator coefficients
+      if (kind == (K_S3 | K_ACC) && s3r_ready(ctx, it)) kind = K_S3R | K_ACC;
       it.kind = kind;
       item_kind[i] = kind;
       long long rows;
@@ -710,7 +762,8 @@ namespace gbint
       switch (kb) {
       case K_S1: rows = it.ax[0].n; break;
       case K_S2: rows = (long long)it.ax[1].n * it.ax[2].n; break;  // (q, cos); inner: modes
-      case K_S3: rows = (long long)it.ax[0].n * it.ax[1].n; break;
+      case K_S3:
+      case K_S3R: rows = (long long)it.ax[0].n * it.ax[1].n; break;
       case K_S5:
       case K_S5Z: rows = (long long)it.ax[0].n * it.ax[1].n; break;  // S5Z: ordered (c1, q)
       default: {
@@ -723,7 +776,7 @@ namespace gbint
       // hoisted segment
       if (kind != K_GENERIC) {
         SegDev S{};
-        S.kind = kb == K_S5Z ? SEG_S5 : kb;  // SEG_S* == K_S*
+        S.kind = kb == K_S5Z ? SEG_S5 : kb == K_S3R ? SEG_S3 : kb;  // SEG_S* == K_S*
         S.tab = it.tab[0];
         S.ax0 = it.ax[0];
         S.n0 = it.ax[0].n;
@@ -834,20 +887,30 @@ namespace gbint
       b->plain_threads.push_back(pt);
     }
     // units grouped by kind
-    const int kinds[10] = {K_S1,         K_S2,         K_S3,         K_S5,          K_S1 | K_ACC,
-                           K_S2 | K_ACC, K_S3 | K_ACC, K_S5 | K_ACC, K_S5Z | K_ACC, K_GENERIC};
+    const int kinds[11] = {K_S1,         K_S2,         K_S3,          K_S5,          K_S1 | K_ACC, K_S2 | K_ACC,
+                           K_S3 | K_ACC, K_S3R | K_ACC, K_S5 | K_ACC, K_S5Z | K_ACC, K_GENERIC};
     for (int kind : kinds) {
       gb_batch::KindRun run;
       run.kind = kind;
       run.unit_begin = (int)b->units.size();
       const int kb = kind_base(kind);
-      const int rpu = kind_rows_per_unit(kind, ctx->threads_override[kb + (kind_acc(kind) ? 8 : 0)]);
+      const gb_schedule sc = kind == K_GENERIC ? gb_schedule{kGenericThreads, kGenericPPT, 1, GB_ORDER_ITEM}
+                                               : resolve_schedule(ctx, kind);
+      const int rpu = kind == K_GENERIC ? kGenericUnitPoints : sc.threads * sc.rows_per_thread;
+      const int split_log2 = log2_exact(sc.inner_split);
       int tab_cap = 0, rec_cap = 0;
       bool any = false;
       for (int i = 0; i < n; ++i) {
         if (item_kind[i] != kind) continue;
         any = true;
         ItemDev &it = b->items[i];
+        if (kind != K_GENERIC) {
+          // every row becomes inner_split rows (one part of its inner loop each)
+          if (((long long)it.rows << split_log2) > (1ll << 30))
+            return set_error(ctx, GB_EINVAL, "integral too large for one item (split it)");
+          it.split_log2 = split_log2;
+          it.rows <<= split_log2;
+        }
         const int nu = (it.rows + rpu - 1) / rpu;
         it.unit_begin = (int)b->units.size() - run.unit_begin;
         it.n_units = nu;
@@ -856,6 +919,7 @@ namespace gbint
           U.item = i;
           U.row_begin = u * rpu;
           U.row_count = std::min(rpu, it.rows - u * rpu);
+          U.slot = it.unit_begin + u;
           b->units.push_back(U);
         }
         if (kind != K_GENERIC) {
@@ -866,25 +930,40 @@ namespace gbint
             tb += kind == (K_S2 | K_ACC) ? (D.rc_off ? D.bytes - 4 * D.rc_off : 0) : ctx->slots[it.tab[t]]->bytes;
           }
           if (kb == K_S5Z) tb = s5z_tab_bytes(ctx, it);
+          if (kb == K_S3R) tb = s3r_tab_bytes(ctx, it);
           tab_cap = std::max(tab_cap, tb);
           int rc_n = 0;
           if (kb == K_S1) rc_n = it.ax[1].n;
-          if (kb == K_S2 || kb == K_S3) rc_n = it.ax[2].n;
+          if (kb == K_S2 || kb == K_S3 || kb == K_S3R) rc_n = it.ax[2].n;
           if (kb == K_S5) rc_n = it.ax[2].n + it.ax[3].n;
-          if (kb == K_S5Z) rc_n = s5z_rec_cap(ctx, it, rpu);
+          if (kb == K_S5Z) rc_n = s5z_rec_cap(ctx, it, rpu >> split_log2);
           rec_cap = std::max(rec_cap, rc_n);
         }
       }
       if (!any) continue;
       run.n_units = (int)b->units.size() - run.unit_begin;
+      if (sc.unit_order == GB_ORDER_COST && kind != K_GENERIC) {
+        // largest cost (rows x points per row) first; ties keep item order
+        std::vector<double> per_row(n, 0.0);
+        for (int i = 0; i < n; ++i)
+          if (item_kind[i] == kind) {
+            const ItemDev &it = b->items[i];
+            double pts = 1;
+            for (int a = 0; a < it.n_axes; ++a) pts *= it.ax[a].n;
+            per_row[i] = pts / it.rows;
+          }
+        std::stable_sort(b->units.begin() + run.unit_begin, b->units.end(), [&](const UnitDev &x, const UnitDev &y) {
+          return x.row_count * per_row[x.item] > y.row_count * per_row[y.item];
+        });
+      }
       run.tab_cap = (tab_cap + 127) / 128 * 128;
       run.rec_cap = (rec_cap + 3) / 4 * 4;
       if (kind == K_GENERIC) {
         run.threads = kGenericThreads;
         run.ctas = std::min(run.n_units, ctx->num_sms * 8);
       } else {
-        run.threads = rpu;
-        const int occ = fp32c_occupancy(kind, rpu, run.tab_cap, run.rec_cap);
+        run.threads = sc.threads;
+        const int occ = fp32c_occupancy(kind, sc.threads, run.tab_cap, run.rec_cap);
         if (occ <= 0) return set_error(ctx, GB_EINVAL, "FP32 kernel cannot launch with this table/record size");
         run.ctas = std::min(run.n_units, ctx->num_sms * occ);
       }
@@ -1391,7 +1470,13 @@ int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
   // (cells at most 12 % wide, |t| <= 0.06: truncation < 1e-11 of the denominator)
   const bool with_rq = rc_axis >= 0 && (rc_axis == 0 ? ax0 : ax1).scale64 >= kMinScaleSq;
   const std::vector<float> rq = with_rq ? regulator_cell_coeffs(rc_axis == 0 ? ax0 : ax1) : std::vector<float>{};
-  const size_t alloc = (size_t)t->bytes + rq.size() * 4;
+  // 1D tables with reciprocals also carry per-cell records (built from the data on every update):
+  // a lookup reads the cell's reciprocal, value and difference with one 16-byte load
+  const int cells = spec->n0 - 1;
+  const bool with_cr = rc_axis == 0 && spec->n1 == 0;
+  const size_t cr_bytes = with_cr ? (size_t)cells * 16 + ((size_t)cells * 4 + 15) / 16 * 16 : 0;
+  const size_t cr_at = (size_t)t->bytes + rq.size() * 4;  // 16-byte multiple
+  const size_t alloc = cr_at + cr_bytes;
   GB_CUDA(cudaSetDevice(ctx->device));
   GB_CUDA(cudaMalloc(&t->buf[0], alloc));
   GB_CUDA(cudaMalloc(&t->buf[1], alloc));
@@ -1415,8 +1500,14 @@ int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
   D.rq_off = rq.empty() ? 0 : t->bytes / 4;
   D.rc_axis = std::max(rc_axis, 0);
   D.rc_sq = rc_axis >= 0 && (rc_axis == 0 ? ax0 : ax1).scale64 >= kMinScaleSq;
+  D.cr_off = with_cr ? (int)(cr_at / 4) : 0;
   D.a0 = ax0;
   D.a1 = ax1;
+  if (with_cr) {
+    for (int b = 0; b < 2; ++b)
+      GB_CUDA(launch_cell_records(static_cast<float *>(t->buf[b]), D.rc_off, D.cr_off, cells, ctx->stream));
+    GB_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
   GB_CUDA(cudaMemcpy(ctx->d_dir + slot, &D, sizeof(TableDev), cudaMemcpyHostToDevice));
   t->slot = slot;
   ctx->slots[slot] = t.get();
@@ -1447,6 +1538,9 @@ static int table_update_impl(gb_ctx *ctx, gb_table *t, const float *src, cudaMem
     if (rc) return rc;
   }
   GB_CUDA(cudaMemcpyAsync(t->buf[back], src, (size_t)t->elems * 4, kind, s));
+  if (ctx->h_dir[t->slot].cr_off)
+    GB_CUDA(launch_cell_records(static_cast<float *>(t->buf[back]), ctx->h_dir[t->slot].rc_off,
+                                ctx->h_dir[t->slot].cr_off, t->spec.n0 - 1, s));
   // publish the new buffer in the directory, ordered after the data on the same stream (the
   // host copy of the entry changes only once the device write is enqueued)
   TableDev D = ctx->h_dir[t->slot];
@@ -1520,6 +1614,9 @@ int gb_table_update_many(gb_ctx *ctx, int n, gb_table *const *tables, const floa
     gb_table *t = tables[i];
     const int back = t->front ^ 1;
     GB_CUDA(cudaMemcpyAsync(t->buf[back], host_data[i], (size_t)t->elems * 4, cudaMemcpyHostToDevice, s));
+    if (ctx->h_dir[t->slot].cr_off)
+      GB_CUDA(launch_cell_records(static_cast<float *>(t->buf[back]), ctx->h_dir[t->slot].rc_off,
+                                  ctx->h_dir[t->slot].cr_off, t->spec.n0 - 1, s));
     dir[i] = ctx->h_dir[t->slot];
     dir[i].data = t->buf[back];
   }

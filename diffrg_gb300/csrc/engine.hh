@@ -146,8 +146,10 @@ struct gb_ctx {
   cudaEvent_t tables_event = nullptr;  // recorded after every table update (serving orders on it)
   int update_depth = 0;                // open gb_table_group_begin blocks (guarded by mu)
   int *d_err = nullptr;
-  // kind -> thread override (autotuner)
-  int threads_override[16] = {};  // [base kind + 8 * accurate]
+  // work-unit schedule per FP32-compensated kind (autotuner; zero fields = defaults),
+  // indexed by kind slot = base kind + 8 * accurate
+  gb_schedule sched[16] = {};
+  std::string tune_report;  // JSON of the last gb_autotune's measurements
   // plain-path scratch
   std::vector<double *> plain_buf;
   std::vector<size_t> plain_buf_elems;
@@ -176,6 +178,8 @@ namespace gbint
   int plan_batch(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *const *item_tables,
                  const int *item_ntables, int precision, gb_batch *b);
   size_t batch_device_bytes(const gb_batch *b);
+  // the schedule plan_batch uses for an FP32-compensated kind, defaults filled in
+  gb_schedule resolve_schedule(const gb_ctx *ctx, int kind);
   void release_axes(gb_ctx *ctx, std::vector<AxisKey> &held);
   // the table-update stream waits for in-flight serving batches (double-buffer reuse)
   int serve_fence_tables(gb_ctx *ctx, cudaStream_t s);

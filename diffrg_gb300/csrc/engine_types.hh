@@ -41,6 +41,8 @@ namespace gbint
     K_S5 = 5,       // (q, c1, c2, phi) + VERT4, FP32c: rows (q, c1), mid c2, inner phi
     K_S5Z = 6,      // K_S5, accurate form only, with the 2D tables read through slices along their
                     // cos axis (rows ordered (c1, q); chosen when the slices fit shared memory)
+    K_S3R = 7,      // K_S3, accurate form only, with the three point-dependent tables read through
+                    // their per-cell records (chosen when all three carry records)
     K_ACC = 16      // flag on K_S*: double-float evaluation of the per-point factors
   };
   constexpr int kind_base(int k) { return k & 15; }
@@ -63,6 +65,8 @@ namespace gbint
                      // S5Z: table A at the c1 nodes
     int slice_off2;  // S5Z: table B at the c2 nodes
     int slice_off3;  // S5Z: table A at the c2 nodes
+    int split_log2;  // S3 / S5Z: each quadrature row is split into 2^split_log2 parts of its inner
+                     // (S3: phi) or middle (S5Z: c2) loop; rows counts the parts
     double k;
     double args[GB_MAX_ARGS];
   };
@@ -71,7 +75,7 @@ namespace gbint
     int item;
     int row_begin;
     int row_count;
-    int pad;
+    int slot;  // partial-sum slot: the unit's position in item order (units may run in another order)
   };
 
   // table directory entry (device): current FP32 data + axes
@@ -83,6 +87,9 @@ namespace gbint
     int rc_axis;  // the log axis they belong to (cells at most 25 % wide)
     int rc_sq;    // 1: cells at most 12 % wide, so the reciprocals also serve a squared coordinate
     int rq_off;   // float offset of the regulator's per-cell Taylor coefficients (global only); 0: none
+    int cr_off;   // float offset of the per-cell records (1D log tables with reciprocals; 0: none):
+                  // float4 {1/c_j hi, 1/c_j lo, y_j, hi(y_{j+1} - y_j)} per cell, then per cell the
+                  // low word of the difference (y_{j+1} - y_j = hi + lo exactly), rebuilt on update
     dev::AxisDev a0, a1;
   };
 

@@ -7,26 +7,18 @@
 
 namespace gbint
 {
-  struct KernelShape {
-    int threads;  // CTA size (= rows per unit for S kinds)
-    int ctas;     // persistent grid size
-    size_t smem;  // dynamic shared memory bytes
-  };
-
   // generic FP64 kernel: points per unit
   constexpr int kGenericThreads = 256;
   constexpr int kGenericPPT = 4;
   constexpr int kGenericUnitPoints = kGenericThreads * kGenericPPT;
-
-  // shape of a kind for this device (num SMs, smem opt-in); threads may be overridden (autotuner)
-  KernelShape kernel_shape(int kind, int num_sms, int threads_override);
-  int kind_rows_per_unit(int kind, int threads_override);
 
   cudaError_t launch_generic(const RunParams &P, int ctas, cudaStream_t s);
   // also zeroes the n_counters (<= 64) work counters of the batch's kind runs
   cudaError_t launch_seg(const SegDev *segs, int n_segs, int total_entries, const double *pv, const double *pw,
                          const float4 *aux, const TableDev *tabs, double *seg_out, int *counters, int n_counters,
                          cudaStream_t s);
+  // rebuilds a 1D table's per-cell records (TableDev::cr_off) from its data, in stream order
+  cudaError_t launch_cell_records(float *table, int rc_off, int cr_off, int cells, cudaStream_t s);
   // writes one table directory entry in stream order (the entry travels as a kernel parameter)
   cudaError_t launch_dir_set(TableDev *dst, const TableDev &v, cudaStream_t s);
   // writes n directory entries dir[slot[i]] = v[i] in stream order (chunks travel as parameters)
@@ -37,6 +29,8 @@ namespace gbint
   // resident CTAs per SM for that configuration (0 if it cannot launch)
   int fp32c_occupancy(int kind, int threads, int tab_bytes_cap, int rec_cap);
   int kind_default_threads(int kind);
+  // the schedule of a kind when nothing is set (every field filled in)
+  gb_schedule kind_default_schedule(int kind);
 
   // reference execution pattern: one value per (row of) point(s) into dest
   cudaError_t launch_plain(const ItemDev *item_dev, long long n_threads, int loop_axis, const double *pv,

@@ -86,11 +86,8 @@ namespace gbint
     // through t^9/9, truncation < 3e-10 of a cell.
     // SQ: x is the square of the axis coordinate (1/c_j^2 formed from 1/c_j, half the scale)
     template <bool SQ = false>
-    __device__ __forceinline__ float cell_frac_at(const AxisDev &a, const float2 *rc, df x, int j, df *t_out = nullptr)
+    __device__ __forceinline__ float cell_frac_rr(const AxisDev &a, df rr, df x, df *t_out = nullptr)
     {
-      const float2 r = rc[j];
-      df rr{r.x, r.y};
-      if constexpr (SQ) rr = df_mul(rr, rr);
       // t = x rr - 1 = th + tl: th = fl(x.hi rr.hi) - 1 is exact (the product lies in [1/2, 2]),
       // tl = the product's rounding error + the cross terms; ln(1 + th + tl) = ln(1 + th) +
       // tl (1 - th) + O(tl^2, th^2 tl)
@@ -110,6 +107,14 @@ namespace gbint
       const float kh = SQ ? 0.5f * a.kln.hi : a.kln.hi, kl = SQ ? 0.5f * a.kln.lo : a.kln.lo;
       const float a0 = __fmaf_rn(kh, th, 0.5f);
       return __fadd_rn(a0, __fmaf_rn(kh, rest, __fmul_rn(kl, th)));
+    }
+    template <bool SQ = false>
+    __device__ __forceinline__ float cell_frac_at(const AxisDev &a, const float2 *rc, df x, int j, df *t_out = nullptr)
+    {
+      const float2 r = rc[j];
+      df rr{r.x, r.y};
+      if constexpr (SQ) rr = df_mul(rr, rr);
+      return cell_frac_rr<SQ>(a, rr, x, t_out);
     }
     // the same fraction as a double-float (its FP32 rounding, ~3e-8 of a cell, is otherwise the
     // largest per-point error of a lookup; used where few points carry an integral)
@@ -246,9 +251,19 @@ namespace gbint
     // R(x) = x / expm1(x) from the Taylor coefficients about the centre of cell j of the table's
     // log axis (3 float4 per cell: a0, a1 as double-float pairs, a2..a7), t = x / c_j - 1:
     // ~30 instructions instead of the exp-based double-float form, no branch on x
-    __device__ __forceinline__ df reg_R_cell(const float4 *rq, int j, df t)
+    // (SHARED: the coefficients were staged to shared memory)
+    template <bool SHARED = false> __device__ __forceinline__ df reg_R_cell(const float4 *rq, int j, df t)
     {
-      const float4 c0 = __ldg(rq + 3 * j), c1 = __ldg(rq + 3 * j + 1), c2 = __ldg(rq + 3 * j + 2);
+      float4 c0, c1, c2;
+      if constexpr (SHARED) {
+        c0 = rq[3 * j];
+        c1 = rq[3 * j + 1];
+        c2 = rq[3 * j + 2];
+      } else {
+        c0 = __ldg(rq + 3 * j);
+        c1 = __ldg(rq + 3 * j + 1);
+        c2 = __ldg(rq + 3 * j + 2);
+      }
       const float th = t.hi;
       float p = __fmaf_rn(th, c2.y, c2.x);
       p = __fmaf_rn(th, p, c1.w);
@@ -368,6 +383,13 @@ namespace gbint
 
     // bytes of a table's cell-centre reciprocals (staged at the end of its data; 16-byte multiple)
     __device__ __forceinline__ int rc_bytes(const TableDev &T) { return T.rc_off ? T.bytes - 4 * T.rc_off : 0; }
+    // S3R staging: a 1D table's regulator coefficients (48 bytes a cell) and its cell records
+    // (16 bytes a cell, then the difference low words padded to 16 bytes)
+    __device__ __forceinline__ int s3r_rq_bytes(const TableDev &T) { return 48 * (T.n0 - 1); }
+    __device__ __forceinline__ int s3r_rec_bytes(const TableDev &T)
+    {
+      return 16 * (T.n0 - 1) + (4 * (T.n0 - 1) + 15) / 16 * 16;
+    }
 
     // ---------------------------------------------------------------- per-kind traits
     template <int KIND> struct Traits;
@@ -386,6 +408,9 @@ namespace gbint
     template <> struct Traits<K_S5Z> {
       static constexpr int kTables = 2;
     };
+    template <> struct Traits<K_S3R> {
+      static constexpr int kTables = 4;
+    };
 
     // node records a unit needs (inner axes), staged back to back
     __device__ __forceinline__ int rec_axes(int kind, const ItemDev &it, int &a0, int &a1)
@@ -397,6 +422,7 @@ namespace gbint
         return it.ax[1].n;
       case K_S2:
       case K_S3:
+      case K_S3R:
         a0 = 2;
         a1 = -1;
         return it.ax[2].n;
@@ -421,8 +447,8 @@ namespace gbint
       uint32_t zbytes = 0;
       const float4 *zsrc = nullptr;
       if (kind == K_S5Z) {
-        const int nq = it.ax[0].n, ns0 = P.tabs[it.tab[0]].n0 - 1;
-        const int j0 = U.row_begin / nq, j1 = (U.row_begin + U.row_count - 1) / nq;
+        const int nq = it.ax[0].n, ns0 = P.tabs[it.tab[0]].n0 - 1, sl = it.split_log2;
+        const int j0 = (U.row_begin >> sl) / nq, j1 = ((U.row_begin + U.row_count - 1) >> sl) / nq;
         zsrc = reinterpret_cast<const float4 *>(P.seg + it.slice_off) + (size_t)j0 * ns0;
         zbytes = (uint32_t)((j1 - j0 + 1) * ns0 * sizeof(float4));
       }
@@ -633,8 +659,10 @@ namespace gbint
     // ---------------------------------------------------------------- S3: (q, c, phi) x PROP3
     // row = (q node i, c node j); inner = phi nodes; hoisted F_i = w_q Rdot(q^2) G_A(q^2) (FP64)
     template <bool ACC>
-    __device__ __forceinline__ double row_s3(const RunParams &P, const ItemDev &it, int row, const NodeRec *rc,
-                                             const float *tab, const TableDev *sT, const int *toff)
+    // part / nsplit: this call sums the phi nodes l = part, part + nsplit, ... of the row
+    __device__ __forceinline__ double row_s3(const RunParams &P, const ItemDev &it, int row, int part, int nsplit,
+                                             const NodeRec *rc, const float *tab, const TableDev *sT,
+                                             const int *toff)
     {
       const int nc = it.ax[1].n;
       const int i = row / nc, j = row - i * nc;
@@ -664,7 +692,7 @@ namespace gbint
         const float sb = df_round(sbd);
         Kahan k;
 #pragma unroll 1
-        for (int l = 0; l < nh; ++l) {
+        for (int l = part; l < nh; l += nsplit) {
           const NodeRec r = rc[l];  // a = cos(phi), w = 2 pi w_phi
           const float r2 = fmaxf(lin_df(A, B, r.a_hi, r.a_lo), 1e-30f);
           const float t2 = fmaxf(lin_df(Ap, Bh, r.a_hi, r.a_lo), 1e-30f);
@@ -677,7 +705,7 @@ namespace gbint
       } else {
         AccDF k;
 #pragma unroll 1
-        for (int l = 0; l < nh; ++l) {
+        for (int l = part; l < nh; l += nsplit) {
           const NodeRec r = rc[l];
           const df r2 = df_max(lin_dd(A, B, r.a_hi, r.a_lo), 1e-30f);
           const df t2 = df_max(lin_dd(Ap, Bh, r.a_hi, r.a_lo), 1e-30f);
@@ -688,6 +716,126 @@ namespace gbint
         inner = k.value();
       }
       return P.seg[it.seg_off + i] * P.pw[it.ax[1].off + j] * inner;
+    }
+
+    // ---------------------------------------------------------------- S3R: S3 through cell records
+    // The accurate S3 with its three point-dependent tables (B at r2 = |q-p|^2, C at
+    // s = (q^2 + p^2 + r2)/3, D at t2 = |q-p/2|^2) read through per-cell records staged in shared
+    // memory: one 16-byte load gives a cell's reciprocal, value and difference (split exactly
+    // into two floats, so the lerp needs no two_sum of the endpoints), and B's regulator
+    // coefficients are staged beside them instead of read through L1.  t2 follows from r2
+    // (t2 = r2/2 + q^2/2 - P^2/4).  Staged layout (floats): [0] B's regulator coefficients,
+    // toff[t] for t = 1..3: the records of table t, then its difference low words.
+    struct RecTab {
+      const float4 *rec;
+      const float *dlo;
+    };
+    __device__ __forceinline__ RecTab rec_tab(const float *tab, int off, int cells)
+    {
+      return RecTab{reinterpret_cast<const float4 *>(tab + off), tab + off + 4 * cells};
+    }
+    // cell j and fraction of x (x.hi > 0 or NaN; NaN lands in a clamped cell) on a record table,
+    // clamped like log_cell_frac; r = the record of cell j; (jt, t): the cell whose centre t =
+    // x / c_jt - 1 refers to, or jt = -1 where x lies outside the table
+    __device__ __forceinline__ float rec_cell_frac(const AxisDev &a, const float4 *rec, df x, int &j, float4 &r,
+                                                   int &jt, df &t)
+    {
+      const int n = a.n;
+      jt = -1;
+      const float ua = __fmaf_rn(a.scale.hi, __log2f(x.hi), a.shift.hi);
+      if (ua < -0.01f) {
+        j = 0;
+        r = rec[0];
+        return 0.f;
+      }
+      if (ua > (float)(n - 1) + 0.01f) {
+        j = n - 2;
+        r = rec[n - 2];
+        return 1.f;
+      }
+      j = min(max((int)floorf(ua), 0), n - 2);
+      jt = j;
+      r = rec[j];
+      float f = cell_frac_rr(a, df{r.x, r.y}, x, &t);
+      if (f < 0.f) {
+        if (j > 0) {
+          j -= 1;
+          f = __fadd_rn(f, 1.f);
+          r = rec[j];
+        } else
+          f = 0.f;
+      } else if (f > 1.f) {
+        if (j < n - 2) {
+          j += 1;
+          f = __fsub_rn(f, 1.f);
+          r = rec[j];
+        } else
+          f = 1.f;
+      }
+      return fminf(fmaxf(f, 0.f), 1.f);
+    }
+    // y_j + f (y_{j+1} - y_j) from a record, unnormalised (the same operations as lerp_df_u)
+    __device__ __forceinline__ df rec_lerp_u(const float4 &r, float dlo, float f)
+    {
+      const df p = two_prod(f, r.w);
+      const df s = two_sum(r.z, p.hi);
+      return df{s.hi, __fadd_rn(s.lo, __fmaf_rn(f, dlo, p.lo))};
+    }
+    __device__ __forceinline__ df G1_rec(const RecTab &T, const float4 *rq, const AxisDev &a, df x)
+    {
+      int j, jt;
+      float4 r;
+      df t;
+      const float f = rec_cell_frac(a, T.rec, x, j, r, jt, t);
+      const df R = jt >= 0 ? reg_R_cell<true>(rq, jt, t) : reg_R_df(x);
+      return df_prop(rec_lerp_u(r, T.dlo[j], f), x, R);
+    }
+    __device__ __forceinline__ df V1_rec(const RecTab &T, const AxisDev &a, df x)
+    {
+      int j, jt;
+      float4 r;
+      df t;
+      const float f = rec_cell_frac(a, T.rec, x, j, r, jt, t);
+      return rec_lerp_u(r, T.dlo[j], f);
+    }
+    // part / nsplit: this call sums the phi nodes l = part, part + nsplit, ... of the row
+    __device__ __forceinline__ double row_s3r(const RunParams &P, const ItemDev &it, int row, int part, int nsplit,
+                                              const NodeRec *rc, const float *tab, const TableDev *sT,
+                                              const int *toff)
+    {
+      const int nc = it.ax[1].n;
+      const int i = row / nc, j = row - i * nc;
+      const NodeRec qr = P.prec[it.ax[0].off + i];
+      const NodeRec cr = P.prec[it.ax[1].off + j];
+      const float4 *aux = P.aux + it.aux_off;  // (P, cos th), (P^2, P^2/4), (sin th, -)
+      const float4 c0 = aux[0], c1 = aux[1], c2 = aux[2];
+      const df q2 = rec_a(qr);
+      const df qP = df_mul(rec_v(qr), df{c0.x, c0.y});
+      const df X = df_mul(qP, df_mul(rec_v(cr), df{c0.z, c0.w}));  // q P c cos(th)
+      const df q2pp = df_add(q2, df{c1.x, c1.y});
+      const df A = df_add(q2pp, df_scale2(df_neg(X), 2.f));  // |q-p|^2 at cos(phi) = 0
+      const df B = df_scale2(df_neg(df_mul(qP, df_mul(rec_a(cr), df{c2.x, c2.y}))), 2.f);  // -2 q P s sin(th)
+      const df Ct = df_add(df_scale2(q2, 0.5f), df_neg(df{c1.z, c1.w}));  // t2 - r2 / 2
+      const df third = dfc(1.0 / 3.0);
+      const df sbd = df_mul(q2pp, third);
+      const RecTab TB = rec_tab(tab, toff[1], sT[1].n0 - 1), TC = rec_tab(tab, toff[2], sT[2].n0 - 1),
+                   TD = rec_tab(tab, toff[3], sT[3].n0 - 1);
+      const float4 *rqB = reinterpret_cast<const float4 *>(tab + toff[0]);
+      const AxisDev aB = sT[1].a0, aC = sT[2].a0, aD = sT[3].a0;
+      const int nf = it.ax[2].n;
+      // the phi rule is symmetric and the integrand reads phi through cos(phi) only (see row_s3)
+      const int nh = (nf + 1) >> 1;
+      AccDF k;
+#pragma unroll 1
+      for (int l = part; l < nh; l += nsplit) {
+        const NodeRec r = rc[l];  // a = cos(phi), w = 2 pi w_phi
+        const df r2 = df_max(lin_dd(A, B, r.a_hi, r.a_lo), 1e-30f);
+        const df t2 = df_max(df_add(df_scale2(r2, 0.5f), Ct), 1e-30f);
+        const df sv = df_add(sbd, df_mul(r2, third));
+        const df g = df_mul_u(df_mul_u(G1_rec(TB, rqB, aB, r2), V1_rec(TC, aC, sv)), V1_rec(TD, aD, t2));
+        k.add_prod(df_scale2(rec_w(r), 2 * l + 1 == nf ? 1.f : 2.f), g);
+      }
+      return P.seg[it.seg_off + i] * P.pw[it.ax[1].off + j] * k.value();
     }
 
     // ---------------------------------------------------------------- S5: (q, c1, c2, phi) x VERT4
@@ -787,8 +935,9 @@ namespace gbint
     // slower), A at the c2 nodes (through L1, once per (row, c2)).  A point then lerps along the
     // |q-p|^2 axis only, twice, instead of two double-float bilinears.
     // row = (c1 node j, q node i), q fastest, so a unit spans few c1 nodes.
-    __device__ __forceinline__ double row_s5z(const RunParams &P, const ItemDev &it, int row, int row0,
-                                              const NodeRec *rc, const float *tab, const TableDev *sT)
+    // part / nsplit: this call sums the c2 nodes l = part, part + nsplit, ... of the row
+    __device__ __forceinline__ double row_s5z(const RunParams &P, const ItemDev &it, int row, int row0, int part,
+                                              int nsplit, const NodeRec *rc, const float *tab, const TableDev *sT)
     {
       const int nq = it.ax[0].n, n1 = it.ax[1].n;
       const int j = row / nq, i = row - j * nq;
@@ -824,7 +973,7 @@ namespace gbint
       const df Rr1 = reg_R_tab(TA, jr1, tr1, r1d);
       AccDF kmid;
 #pragma unroll 1
-      for (int l = 0; l < n2; ++l) {
+      for (int l = part; l < n2; l += nsplit) {
         const NodeRec r2r = rc[l];  // c2: v = c2, a = s2, w = 2 w_c2
         const df gr1 = df_rcp(df_add(df_mul(lerp_zd(__ldg(za2 + (size_t)l * ns0 + ir1), fr1), r1d), Rr1));
         const df Bs = df_mul(B2, rec_a(r2r));
@@ -860,9 +1009,19 @@ namespace gbint
     {
       if constexpr (KIND == K_S1) return row_s1<ACC>(P, it, row, rc, tab + toff[0], sT);
       if constexpr (KIND == K_S2) return row_s2<ACC>(P, it, row, rc, tab + toff[0], sT);
-      if constexpr (KIND == K_S3) return row_s3<ACC>(P, it, row, rc, tab, sT, toff);
+      if constexpr (KIND == K_S3) {
+        const int sl = it.split_log2;
+        return row_s3<ACC>(P, it, row >> sl, row & ((1 << sl) - 1), 1 << sl, rc, tab, sT, toff);
+      }
+      if constexpr (KIND == K_S3R) {
+        const int sl = it.split_log2;
+        return row_s3r(P, it, row >> sl, row & ((1 << sl) - 1), 1 << sl, rc, tab, sT, toff);
+      }
       if constexpr (KIND == K_S5) return row_s5<ACC>(P, it, row, rc, tab, sT, toff);
-      if constexpr (KIND == K_S5Z) return row_s5z(P, it, row, row0, rc, tab, sT);
+      if constexpr (KIND == K_S5Z) {
+        const int sl = it.split_log2;
+        return row_s5z(P, it, row >> sl, row0 >> sl, row & ((1 << sl) - 1), 1 << sl, rc, tab, sT);
+      }
       return 0.0;
     }
   } // namespace
@@ -881,7 +1040,7 @@ namespace gbint
     NodeRec *rec_s1 = rec_s0 + rec_cap;
     __shared__ __align__(8) uint64_t bar[3];
     __shared__ TableDev sT[4];
-    __shared__ int s_slot[4], s_toff[4], s_next[2], s_flag;
+    __shared__ int s_slot[4], s_toff[4], s_next[2], s_flag, s_tabok;
     __shared__ double red[32];
 
     if (threadIdx.x == 0) {
@@ -890,6 +1049,7 @@ namespace gbint
       mbar_init(&bar[2], 1);
       mbar_fence_init();
       for (int i = 0; i < 4; ++i) s_slot[i] = -2;
+      s_tabok = 1;
       const int u = atomicAdd(P.unit_counter, 1);
       s_next[0] = u;
       if (u < P.n_units) issue_records(KIND, P, u, rec_s0, &bar[0]);
@@ -915,18 +1075,36 @@ namespace gbint
             sT[t] = P.tabs[slot];
             s_slot[t] = slot;
             s_toff[t] = total / 4;
-            if constexpr (KIND != K_S5Z) total += kRcOnly ? rc_bytes(sT[t]) : sT[t].bytes;
+            if constexpr (KIND != K_S5Z && KIND != K_S3R) total += kRcOnly ? rc_bytes(sT[t]) : sT[t].bytes;
+          }
+          // S3R: B's regulator coefficients, then the records of B, C, D (table A feeds the
+          // hoisted row factors only)
+          if constexpr (KIND == K_S3R) {
+            bool has = sT[1].rq_off > 0;
+            total = s3r_rq_bytes(sT[1]);
+            for (int t = 1; t < 4; ++t) {
+              has = has && sT[t].cr_off > 0 && sT[t].n1 == 0;
+              s_toff[t] = total / 4;
+              total += s3r_rec_bytes(sT[t]);
+            }
+            if (!has) total = tab_bytes_cap + 1;  // refused below: nothing is staged or evaluated
           }
           // S5Z: table A's cell-centre reciprocals only (both tables share the |q-p|^2 fraction)
           if constexpr (KIND == K_S5Z) total = rc_bytes(sT[0]);
+          s_tabok = 1;
           if (total > tab_bytes_cap) {
             atomicOr(P.err, ERR_BAD_INDEX);
             total = 0;
+            s_tabok = 0;
           }
           mbar_expect_tx(&bar[2], (uint32_t)total);
           if (total > 0) {
             if constexpr (KIND == K_S5Z) {
               tma_bulk_g2s(tab_s, sT[0].data + sT[0].rc_off, (uint32_t)total, &bar[2]);
+            } else if constexpr (KIND == K_S3R) {
+              tma_bulk_g2s(tab_s, sT[1].data + sT[1].rq_off, (uint32_t)s3r_rq_bytes(sT[1]), &bar[2]);
+              for (int t = 1; t < 4; ++t)
+                tma_bulk_g2s(tab_s + s_toff[t], sT[t].data + sT[t].cr_off, (uint32_t)s3r_rec_bytes(sT[t]), &bar[2]);
             } else {
               for (int t = 0; t < NT; ++t) {
                 if constexpr (kRcOnly) {
@@ -942,6 +1120,9 @@ namespace gbint
         ok = mbar_wait_bounded(&bar[2], ph_tab, P.err) && ok;
         ph_tab ^= 1;
       }
+      if (!s_tabok) {
+        ok = false;  // the tables of this unit could not be staged (error word set)
+      }
       // prefetch the next unit's records into the other buffer
       if (threadIdx.x == 0) {
         const int un = atomicAdd(P.unit_counter, 1);
@@ -955,12 +1136,17 @@ namespace gbint
         ok = mbar_wait_bounded(&bar[1], ph1, P.err) && ok;
         ph1 ^= 1;
       }
+      // a unit holds rows_per_thread x THREADS rows (the schedule's choice); thread t takes rows
+      // t, t + THREADS, ...
       double acc = 0.0;
-      if (ok && (int)threadIdx.x < U.row_count)
-        acc = row_value<KIND, ACC>(P, it, U.row_begin + threadIdx.x, U.row_begin, buf ? rec_s1 : rec_s0, tab_s, sT,
-                                   s_toff);
+      if (ok) {
+#pragma unroll 1
+        for (int r = threadIdx.x; r < U.row_count; r += THREADS)
+          acc += row_value<KIND, ACC>(P, it, U.row_begin + r, U.row_begin, buf ? rec_s1 : rec_s0, tab_s, sT,
+                                      s_toff);
+      }
       const double tot = block_sum(acc, red);
-      unit_finish(P, u, U.item, tot, red, &s_flag);
+      unit_finish(P, U.slot, U.item, tot, red, &s_flag);
       buf ^= 1;
     }
   }
@@ -994,36 +1180,31 @@ namespace gbint
         return acc ? sel_threads<K_S5, true>(threads) : sel_threads<K_S5, false>(threads);
       case K_S5Z:
         return acc ? sel_threads<K_S5Z, true>(threads) : nullptr;
+      case K_S3R:
+        return acc ? sel_threads<K_S3R, true>(threads) : nullptr;
       }
       return nullptr;
     }
   } // namespace
 
-  int kind_default_threads(int kind)
+  int kind_default_threads(int kind) { return kind_default_schedule(kind).threads; }
+
+  // defaults measured on GB300 (the autotuner's landscapes on the benchmark workloads): S5Z runs
+  // 23 % faster at 256 threads with its c2 loop split over two threads than at 512 unsplit
+  gb_schedule kind_default_schedule(int kind)
   {
     switch (kind_base(kind)) {
     case K_S1:
-      return 128;
+      return gb_schedule{128, 1, 1, GB_ORDER_ITEM};
     case K_S5:
+      return gb_schedule{512, 1, 1, GB_ORDER_ITEM};
     case K_S5Z:
-      return 512;
+      return gb_schedule{256, 1, 2, GB_ORDER_ITEM};
+    case K_S3R:
+      return gb_schedule{256, 1, 1, GB_ORDER_ITEM};
     default:
-      return 256;
+      return gb_schedule{256, 1, 1, GB_ORDER_ITEM};
     }
-  }
-
-  int kind_rows_per_unit(int kind, int threads_override)
-  {
-    if (kind == K_GENERIC) return kGenericUnitPoints;
-    return threads_override > 0 ? threads_override : kind_default_threads(kind);
-  }
-
-  KernelShape kernel_shape(int kind, int num_sms, int threads_override)
-  {
-    KernelShape s{0, 0, 0};
-    s.threads = kind_rows_per_unit(kind, threads_override);
-    s.ctas = num_sms;
-    return s;
   }
 
   // the kernels' dynamic shared-memory limit is raised once per (kernel, device) to the largest

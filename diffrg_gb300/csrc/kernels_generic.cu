@@ -40,7 +40,7 @@ namespace gbint
         if (local < U.row_count) acc += eval_point_fp64(it, (long long)U.row_begin + local, P.pv, P.pw, sT);
       }
       const double tot = block_sum(acc, red);
-      unit_finish(P, u, U.item, tot, red, &s_flag);
+      unit_finish(P, U.slot, U.item, tot, red, &s_flag);
     }
   }
 
@@ -203,6 +203,26 @@ namespace gbint
     return cudaGetLastError();
   }
   __global__ void k_dir_set(TableDev *dst, const TableDev v) { *dst = v; }
+
+  // per-cell records of a 1D table: {1/c_j hi, lo, y_j, hi(d_j)} and lo(d_j), d_j = y_{j+1} - y_j
+  // split exactly into two floats
+  __global__ void k_cell_records(float *table, int rc_off, int cr_off, int cells)
+  {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= cells) return;
+    const float y0 = table[j], y1 = table[j + 1];
+    const dev::df d = dev::two_sum(y1, -y0);
+    const float2 r = reinterpret_cast<const float2 *>(table + rc_off)[j];
+    reinterpret_cast<float4 *>(table + cr_off)[j] = make_float4(r.x, r.y, y0, d.hi);
+    table[cr_off + 4 * cells + j] = d.lo;
+  }
+
+  cudaError_t launch_cell_records(float *table, int rc_off, int cr_off, int cells, cudaStream_t s)
+  {
+    if (cells <= 0) return cudaSuccess;
+    k_cell_records<<<(cells + 127) / 128, 128, 0, s>>>(table, rc_off, cr_off, cells);
+    return cudaGetLastError();
+  }
 
   cudaError_t launch_dir_set(TableDev *dst, const TableDev &v, cudaStream_t s)
   {

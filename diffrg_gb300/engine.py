@@ -300,9 +300,10 @@ class Context:
 
     # autotuner
     def autotune(self, integrals, tables=(), precision="fp32c", cache_path=None, refresh=False) -> dict:
-        """Time the CTA widths of the FP32-compensated kernels on these integrals and keep the
+        """Time the work-unit schedules of the FP32-compensated kernels on these integrals (CTA
+        width, rows per thread, inner split, unit order; one parameter at a time) and keep the
         fastest per kernel kind (batches created afterwards use them).  Returns {slot: threads}
-        for the slots that are not at their default."""
+        for the slots whose width is set; tune_report() has every measurement."""
         arr = integral_array(integrals)
         chosen = (C.c_int * 16)()
         self.check(capi.lib().gb_autotune(self.h, arr, len(arr), _table_array(tables), len(tables), PREC[precision],
@@ -311,6 +312,28 @@ class Context:
 
     def tune_set(self, slot: int, threads: int):
         self.check(capi.lib().gb_tune_set(self.h, slot, threads))
+
+    def tune_set_schedule(self, slot: int, threads=0, rows_per_thread=0, inner_split=0, unit_order="item"):
+        sc = capi.Schedule(threads, rows_per_thread, inner_split,
+                           capi.GB_ORDER_COST if unit_order == "cost" else capi.GB_ORDER_ITEM)
+        self.check(capi.lib().gb_tune_set_schedule(self.h, slot, C.byref(sc)))
+
+    def tune_get_schedule(self, slot: int) -> dict:
+        sc = capi.Schedule()
+        self.check(capi.lib().gb_tune_get_schedule(self.h, slot, C.byref(sc)))
+        return {"threads": sc.threads, "rows_per_thread": sc.rows_per_thread, "inner_split": sc.inner_split,
+                "unit_order": "cost" if sc.unit_order == capi.GB_ORDER_COST else "item"}
+
+    def tune_report(self) -> dict:
+        """The last autotune's measurements: per kind slot the default and chosen schedules with
+        their median ms and every candidate's ms, parameter by parameter."""
+        import json
+
+        n = C.c_size_t()
+        self.check(capi.lib().gb_tune_report(self.h, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value + 1)
+        self.check(capi.lib().gb_tune_report(self.h, buf, n.value + 1, C.byref(n)))
+        return json.loads(buf.value.decode())
 
     # CUDA-graph sweeps
     def capture(self, body, stream=None) -> Graph:

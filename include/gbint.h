@@ -265,22 +265,52 @@ int gb_slot_host(gb_ctx *ctx, const gb_slot *slot, size_t bytes, void **host);
 int gb_device_info(gb_ctx *ctx, int *device, int *num_sms);
 
 /* ------------------------------------------------------------------ autotuner
- * CTA width of the FP32-compensated kernels (no reference counterpart; the reference takes a
- * max_block_size from its JSON settings).  For every kernel kind present in the integrals,
- * gb_autotune times the widths the kernels are built for (128, 256, 512 threads = rows per
- * work unit) on a batch of them and keeps the fastest in the context; batches created
- * afterwards use it.  With cache_path (NULL: none) choices are read from / appended to a text
- * file keyed by GPU model and SM count, and a cached kind is not timed again unless flags has
- * GB_TUNE_REFRESH.  chosen (may be NULL) receives the 16 per-kind widths (0 = default), indexed
- * by kind slot = GB_KIND_* (+ 8 for the double-float form used by GB_PREC_FP32C/FP32A).
+ * Work-unit schedule of the FP32-compensated kernels (no reference counterpart; the reference
+ * takes a max_block_size from its JSON settings and launches one grid per integral).  The
+ * kernels evaluate quadrature rows (a row = the outer nodes of a point, its inner loop runs in
+ * one thread) in work units that persistent CTAs claim from an atomic counter.  A schedule is:
+ *   threads          CTA width, 128, 256 or 512;
+ *   rows_per_thread  rows of a work unit per thread, 1, 2 or 4 (unit = threads x this);
+ *   inner_split      GB_KIND_S3 / S3R / S5Z only: parts each row's inner (S3: phi) or middle
+ *                    (S5Z: c2) loop is split into, each on its own thread, 1, 2 or 4;
+ *   unit_order       GB_ORDER_ITEM: units go out in item order; GB_ORDER_COST: largest cost
+ *                    (rows x inner points) first, so the long units of uneven integrals do not
+ *                    end the launch.  Results do not depend on the order (every unit writes its
+ *                    partial to its item-order slot and the finish sums slots in order).
+ * gb_autotune times, for every kind present in the integrals, the schedule parameters one at a
+ * time on a batch of them (widths; then rows per thread; then the split; then the order, each
+ * at the best of the previous ones; a cold L2 before every timed run) and keeps the fastest in
+ * the context; batches created afterwards use it.  With cache_path (NULL: none) choices are
+ * read from / written to a text file keyed by GPU model and SM count, and a cached kind is not
+ * timed again unless flags has GB_TUNE_REFRESH.  chosen (may be NULL) receives the 16 per-slot
+ * widths (0 = default), indexed by kind slot = GB_KIND_* (+ 8 for the double-float form used by
+ * GB_PREC_FP32C/FP32A).  gb_tune_report copies the last gb_autotune's measurements as JSON
+ * (every candidate's median milliseconds per parameter, the default's and the chosen
+ * schedule's) into buf (cap bytes, NUL-terminated; *len = full length).
  * GB_KIND_S5Z is the 4D vertex kernel that reads its 2D tables through slices along their cos
  * axis (double-float form only; used when the slices fit shared memory, else GB_KIND_S5).
- * gb_tune_set pins one slot by hand (0 = default width). */
-enum { GB_KIND_S1 = 1, GB_KIND_S2 = 2, GB_KIND_S3 = 3, GB_KIND_S5 = 5, GB_KIND_S5Z = 6, GB_KIND_ACC = 8 };
+ * GB_KIND_S3R is the 3D loop kernel that reads its three point-dependent 1D tables through
+ * per-cell records (double-float form only; used when the tables are log tables with cells at
+ * most 12 % wide, else GB_KIND_S3).
+ * A zero field means the kind's default (S1: 128 threads; S2, S3: 256; S5: 512; S5Z: 256 with
+ * the c2 loop split in two; one row per thread, item order).  gb_tune_set pins one slot's width
+ * by hand (0 = default width); gb_tune_set_schedule pins a whole schedule; gb_tune_get_schedule
+ * reads the schedule a batch would use now, defaults filled in. */
+enum { GB_KIND_S1 = 1, GB_KIND_S2 = 2, GB_KIND_S3 = 3, GB_KIND_S5 = 5, GB_KIND_S5Z = 6, GB_KIND_S3R = 7, GB_KIND_ACC = 8 };
+enum { GB_ORDER_ITEM = 0, GB_ORDER_COST = 1 };
 #define GB_TUNE_REFRESH 1
+typedef struct gb_schedule {
+  int threads;
+  int rows_per_thread;
+  int inner_split;
+  int unit_order;
+} gb_schedule;
 int gb_autotune(gb_ctx *ctx, const gb_integral *items, int n, gb_table *const *tables, int n_tables, int precision,
                 const char *cache_path, int flags, int *chosen);
 int gb_tune_set(gb_ctx *ctx, int kind_slot, int threads);
+int gb_tune_set_schedule(gb_ctx *ctx, int kind_slot, const gb_schedule *schedule);
+int gb_tune_get_schedule(gb_ctx *ctx, int kind_slot, gb_schedule *out);
+int gb_tune_report(gb_ctx *ctx, char *buf, size_t cap, size_t *len);
 
 /* ------------------------------------------------------------------ CUDA-graph sweeps
  * A fixed sweep -- several gb_batch_run calls in order on one caller stream, e.g. every

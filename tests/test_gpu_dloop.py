@@ -9,7 +9,8 @@ published work units as CTAs free up and leaves after a bounded idle spin.
 * admission: a request that can never fit a ring slot is refused with GB_EBUDGET, a ring of two
   slots takes many requests in turn;
 * the loop left alone runs dry: every CTA counts an idle exit, the kernel ends, and the next
-  submit relaunches it cleanly with correct results.
+  submit relaunches it cleanly with correct results;
+* latency is stamped when a request finishes, not when it is waited for.
 """
 import threading
 import time
@@ -124,6 +125,20 @@ def test_alone_equals_in_mix_from_several_threads(dctx, w):
         assert np.array_equal(v, alone)
     st = c.stats()
     assert st["completed"] >= 33 and 0 < st["p50_latency_s"] <= st["p99_latency_s"] <= st["max_latency_s"]
+
+
+def test_latency_is_stamped_at_completion(dctx, w):
+    """The watcher thread stamps a request's completion when its done flag rises, not when the
+    caller gets round to waiting for it."""
+    c, _, tl = dctx
+    items = _subset(serving.rhs_items(w, 0.75), step=31, n=16)
+    c.submit(items, tl, "fp64").wait(timeout=120)  # warm: axes, module
+    c.reset_stats()
+    t = c.submit(items, tl, "fp64")
+    time.sleep(0.5)
+    t.wait(timeout=120)
+    st = c.stats()
+    assert st["completed"] == 1 and st["max_latency_s"] < 0.25, st
 
 
 def test_request_reads_one_table_epoch(dctx, w):

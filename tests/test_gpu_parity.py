@@ -355,16 +355,26 @@ def test_autotuner_choices_cache_and_accuracy(ctx, oracle, W, tmp_path):
     on the next call, and the tuned batches keep the accuracy bar."""
     cache = str(tmp_path / "tune.txt")
     try:
-        for name, slot in (("C3", 3 + 8), ("C1", 1 + 8)):
+        for name, slot in (("C3", 7 + 8), ("C1", 1 + 8)):
             w = subset(W, name)
             items, tabs = W.engine_items(w)
             T = [ctx.table(s, d) for s, d in tabs]
             got = ctx.autotune(items, T, "fp32c", cache_path=cache)
             assert got.get(slot) in (128, 256, 512)
+            rep = {k["slot"]: k for k in ctx.tune_report()["kinds"]}[slot]
+            assert not rep["cached"] and rep["chosen_ms"] > 0 and rep["default_ms"] > 0
+            assert rep["chosen_ms"] <= rep["default_ms"]
+            want = {"threads", "rows_per_thread", "unit_order"} | ({"inner_split"} if name == "C3" else set())
+            assert set(rep["steps"]) == want
+            assert all(len(rep["steps"][k]) == (2 if k == "unit_order" else 3) for k in want)
+            sched = ctx.tune_get_schedule(slot)
+            assert sched == rep["chosen"]
             lines = open(cache).read().splitlines()
             assert any(l.split("|")[2] == str(slot) for l in lines)
             again = ctx.autotune(items, T, "fp32c", cache_path=cache)
             assert again[slot] == got[slot]
+            assert ctx.tune_get_schedule(slot) == sched
+            assert {k["slot"]: k for k in ctx.tune_report()["kinds"]}[slot]["cached"]
             b = ctx.batch(items, T, "fp32c")
             val = b.get()
             b.close()
@@ -374,9 +384,45 @@ def test_autotuner_choices_cache_and_accuracy(ctx, oracle, W, tmp_path):
                 t.close()
         with pytest.raises(Exception):
             ctx.tune_set(3, 96)
+        with pytest.raises(Exception):
+            ctx.tune_set_schedule(3, rows_per_thread=3)
     finally:
         for k in range(16):
-            ctx.tune_set(k, 0)
+            ctx.tune_set_schedule(k)
+
+
+@pytest.mark.parametrize("name,slot", [("C1", 1 + 8), ("C2", 2 + 8), ("C3", 7 + 8), ("C5", 6 + 8)])
+def test_work_unit_schedules_keep_accuracy(ctx, oracle, W, name, slot):
+    """Every schedule (CTA width x rows per thread x inner split) meets the accuracy bar and is
+    deterministic; the cost order changes only which CTA runs a unit, so its results equal the
+    item order's bit for bit."""
+    w = subset(W, name)
+    items, tabs = W.engine_items(w)
+    T = [ctx.table(s, d) for s, d in tabs]
+    ref = W.oracle_values(w, oracle)
+
+    def run():
+        b = ctx.batch(items, T, "fp32c")
+        v = b.get()
+        b.close()
+        return v
+
+    splits = (1, 2, 4) if name in ("C3", "C5") else (1,)
+    shapes = [(256, 1, 1), (128, 4, 1), (512, 2, 1)] + [(256, 2, s) for s in splits[1:]] + [(128, 1, 4)] * (len(splits) > 1)
+    try:
+        for th, rpt, sp in shapes:
+            ctx.tune_set_schedule(slot, th, rpt, sp, "item")
+            sc = ctx.tune_get_schedule(slot)
+            assert (sc["threads"], sc["rows_per_thread"], sc["inner_split"]) == (th, rpt, sp)
+            v_item = run()
+            assert np.max(rel(v_item, ref)) <= TOL32[name], (th, rpt, sp)
+            assert np.array_equal(run(), v_item)
+            ctx.tune_set_schedule(slot, th, rpt, sp, "cost")
+            assert np.array_equal(run(), v_item), (th, rpt, sp)
+    finally:
+        ctx.tune_set_schedule(slot)
+        for t in T:
+            t.close()
 
 
 def test_bounded_wait_times_out_and_context_survives(ctx, W):
@@ -412,6 +458,33 @@ def test_table_update_is_seen_by_next_run(ctx, oracle, W):
     assert np.max(rel(first, second)) > 1e-3
     b.close()
     t.close()
+
+
+@pytest.mark.parametrize("many", [False, True])
+def test_table_update_rebuilds_cell_records(ctx, oracle, W, many):
+    """C3's kernel reads its three point-dependent tables through per-cell records rebuilt on
+    every update (single updates and gb_table_update_many): after an update the next run
+    matches the oracle on the new data."""
+    w = subset(W, "C3")
+    items, tabs = W.engine_items(w)
+    T = [ctx.table(s, d) for s, d in tabs]
+    b = ctx.batch(items, T, "fp32c")
+    first = b.get()
+    new = [(d * (1.0 + 0.05 * (k + 1))).astype(np.float32) for k, (_, d) in enumerate(tabs)]
+    if many:
+        ctx.update_tables([(t, d) for t, d in zip(T, new)])
+    else:
+        for t, d in zip(T, new):
+            t.update(d)
+    second = b.get()
+    w2 = dict(w)
+    w2["tables"] = [(s, d) for (s, _), d in zip(tabs, new)]
+    ref = W.oracle_values(w2, oracle)
+    assert np.max(rel(second, ref)) <= TOL32["C3"]
+    assert np.max(rel(first, second)) > 1e-3
+    b.close()
+    for t in T:
+        t.close()
 
 
 def test_errors_are_status_codes(ctx, W):
