@@ -327,6 +327,7 @@ def serving_c4(device):
     out["saturated"] = one_step(None)
     out["poisson"] = one_step(w["rate"])
     out["poisson"]["offered_integrals_per_s"] = w["rate"]
+    out["head_of_line"] = head_of_line(ctx, f.tlist, w, "fp32c")
     # the reference's pattern on the same integrals: one launch + CUB + sync per integral
     b = ctx.batch(SV.rhs_items(w, 1.0), f.tlist, "fp64")
     b.run_plain(16)
@@ -339,6 +340,38 @@ def serving_c4(device):
     ctx.close()
     out["fp64_loops"] = serving_loops(device)
     return out
+
+
+def head_of_line(ctx, tlist, w, precision, reps=20):
+    """Latency of a small request (8 2D integrals) submitted right behind a large one (2048 3D
+    integrals, the largest request size of C4) against the same small request alone: what a
+    small request pays for arriving while the GPU is full of another's work."""
+    from diffrg_gb300 import serving as SV
+
+    items = SV.rhs_items(w, 1.0)
+    per = len(w["p"])
+    big = [items[i * per + j] for i in range(1, SV.N_FUNC, 2) for j in range(per)][:2048]
+    probe = items[:8]
+
+    def lat(with_big):
+        v = []
+        for _ in range(reps):
+            tb = ctx.submit(big, tlist, precision) if with_big else None
+            t0 = time.perf_counter()
+            ctx.submit(probe, tlist, precision).wait(timeout=300)
+            v.append((time.perf_counter() - t0) * 1e3)
+            if tb is not None:
+                tb.wait(timeout=300)
+        v.sort()
+        return {"p50_ms": v[len(v) // 2], "max_ms": v[-1]}
+
+    lat(False)  # warm: axes of both sizes
+    lat(True)
+    t0 = time.perf_counter()
+    ctx.submit(big, tlist, precision).wait(timeout=300)
+    return {"precision": precision, "probe_integrals": len(probe), "large_integrals": len(big), "reps": reps,
+            "large_alone_ms": (time.perf_counter() - t0) * 1e3,
+            "probe_alone": lat(False), "probe_behind_large": lat(True)}
 
 
 def serving_loops(device):
@@ -376,6 +409,7 @@ def serving_loops(device):
                              "p50_ms": st["p50_latency_s"] * 1e3, "p99_ms": st["p99_latency_s"] * 1e3,
                              "max_ms": st["max_latency_s"] * 1e3}
                 vals[(name, mode)] = v.ravel()
+            res["head_of_line"] = head_of_line(ctx, f.tlist, w, "fp64", reps=5)
             if name == "device":
                 res["loop"] = ctx.device_loop_info()
             out[name] = res

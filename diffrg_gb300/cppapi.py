@@ -97,6 +97,15 @@ def build_tests() -> str:
     return compile_program(TEST_SRC, TEST_BIN)
 
 
+QMC_SRC = os.path.join(ROOT, "tests", "cpp", "test_qmc.cu")
+QMC_BIN = os.path.join(ROOT, "tests", "cpp", "bin", "test_qmc")
+
+
+def build_qmc_tests() -> str:
+    """The QMC integrators' test driver, compiled through the reference's header paths."""
+    return compile_program(QMC_SRC, QMC_BIN, extra=["-std=c++20", "-I", COMPAT])
+
+
 DROPIN_SRC = os.path.join(os.path.dirname(os.path.abspath(__file__)), "bench", "dropin_bench.cu")
 DROPIN_BIN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "bench", "bin", "dropin_bench")
 

@@ -8,7 +8,9 @@
 // threads per SM, so other kernels still find room) claims published units one at a time with
 // an atomic compare-and-swap on a device counter -- continuous batching: units of a request that
 // arrives while others run are claimed as soon as CTAs free up, and requests of different sizes
-// and integrand kinds share the launch.  A unit is 1024 grid points of one integral, evaluated
+// and integrand kinds share the launch.  Requests of at most 2^22 grid points are published on
+// an express lane whose units CTAs claim first, so a small request arriving behind a large one
+// starts as soon as CTAs finish their current units.  A unit is 1024 grid points of one integral, evaluated
 // with the same per-point function and reduction as the generic FP64 kernel; the last unit of an
 // integral to arrive sums the integral's unit partials in unit order, so every result is
 // bit-identical alone and in any mix, and equals gb_get(..., GB_PREC_FP64) to rounding (the
@@ -42,9 +44,8 @@
 #include <cstdint>
 #include <cstring>
 #include <chrono>
-#include <condition_variable>
-#include <thread>
 #include <cmath>
+#include <condition_variable>
 #include <thread>
 
 namespace gbint
@@ -55,21 +56,25 @@ namespace gbint
   namespace
   {
     constexpr int kDLMaxRing = 64;
+    // requests of at most this many grid points go to the express lane, whose units the loop's
+    // CTAs claim before the normal lane's: a small request does not wait behind the units of a
+    // large one that arrived first
+    constexpr uint64_t kDLExpressPoints = 1ull << 22;
     constexpr int kDLMaxTables = kMaxTables;  // distinct tables one request may read (the whole directory)
 
     // a ring slot's request, in device memory (pointers as integers: read with ld.global.cg)
     struct DLReq {
-      long long u_begin, u_end;  // its global work units
-      int n_items, seq;
+      long long u_begin, u_end;  // its work units, numbered within its lane
+      int n_items, seq, lane, pad;
       unsigned long long items, tabs, partials, item_count, done_items;
     };
     struct DLShared {  // device memory
-      unsigned long long next_unit;
+      unsigned long long next_unit[2];  // per lane: 0 normal, 1 express
       int idle_exits;
       int pad;
     };
     struct DLMapped {  // mapped pinned host memory
-      volatile unsigned long long published;
+      volatile unsigned long long published[2];  // per lane
       volatile int stop;
       volatile int pad0;
       volatile int done[kDLMaxRing];  // seq of the last finished request of each slot
@@ -105,15 +110,27 @@ namespace gbint
       for (;;) {
         if (threadIdx.x == 0) {
           long long u = -1;
+          int lane = 0;
           int polls = 0;
           long long t0 = 0;
           for (;;) {
-            const unsigned long long pub = L.m->published;
+            const unsigned long long pub1 = L.m->published[1], pub0 = L.m->published[0];
             __threadfence_system();
-            const unsigned long long n = atomicAdd(&L.sh->next_unit, 0ull);
-            if (n < pub) {
-              if (atomicCAS(&L.sh->next_unit, n, n + 1) == n) {
-                u = (long long)n;
+            // the express lane first
+            const unsigned long long n1 = atomicAdd(&L.sh->next_unit[1], 0ull);
+            if (n1 < pub1) {
+              if (atomicCAS(&L.sh->next_unit[1], n1, n1 + 1) == n1) {
+                u = (long long)n1;
+                lane = 1;
+                break;
+              }
+              continue;
+            }
+            const unsigned long long n0 = atomicAdd(&L.sh->next_unit[0], 0ull);
+            if (n0 < pub0) {
+              if (atomicCAS(&L.sh->next_unit[0], n0, n0 + 1) == n0) {
+                u = (long long)n0;
+                lane = 0;
                 break;
               }
               continue;
@@ -131,7 +148,7 @@ namespace gbint
             for (int k = 0; k < L.R; ++k) {
               const int s = (hint + k) % L.R;
               const long long b = __ldcg(&L.reqs[s].u_begin), e = __ldcg(&L.reqs[s].u_end);
-              if (u >= b && u < e) {
+              if (u >= b && u < e && __ldcg(&L.reqs[s].lane) == lane) {
                 slot = s;
                 break;
               }
@@ -269,7 +286,7 @@ namespace gbint
     bool launched = false;
     uint64_t evictions_at_launch = 0;
     long long launches = 0;
-    unsigned long long published = 0;
+    unsigned long long published[2] = {0, 0};  // per lane
     int next_seq = 1;
     gb_ticket next_ticket = 1;
     std::map<gb_ticket, DLTicket> tickets;
@@ -603,10 +620,12 @@ namespace gbint
       }
     }
     DLReq &r = *sl.h_req;
-    r.u_begin = (long long)D->published;
+    const int lane = pts <= kDLExpressPoints ? 1 : 0;
+    r.u_begin = (long long)D->published[lane];
     r.u_end = r.u_begin + units;
     r.n_items = n;
     r.seq = D->next_seq;
+    r.lane = lane;
     r.items = reinterpret_cast<unsigned long long>(sl.d_items);
     r.tabs = reinterpret_cast<unsigned long long>(sl.d_tabs);
     r.partials = reinterpret_cast<unsigned long long>(sl.d_partials);
@@ -624,8 +643,8 @@ namespace gbint
     }
     // publish: the descriptors are in device memory before the unit count the loop polls rises
     std::atomic_thread_fence(std::memory_order_seq_cst);
-    D->published = (unsigned long long)r.u_end;
-    D->h_map->published = D->published;
+    D->published[lane] = (unsigned long long)r.u_end;
+    D->h_map->published[lane] = D->published[lane];
     std::atomic_thread_fence(std::memory_order_seq_cst);
     k.seq = D->next_seq++;
     const gb_ticket id = D->next_ticket++;

@@ -764,6 +764,15 @@ namespace DiFfRG
 
   public:
     using ctype = typename B::ctype;
+    // (provider, grid sizes, x_extent, json): the generated wrapper's construction
+    // (integrator_2D_cartesian_gpu.hh:70-74)
+    template <class JSON, typename = decltype(std::declval<const JSON &>().get_uint(""))>
+    IntegratorCartesianGPU(QuadratureProvider &qp, const std::array<uint, dim> grid_sizes, const ctype x_extent,
+                           const JSON &json)
+        : IntegratorCartesianGPU(qp, grid_sizes, x_extent,
+                                 gbint_detail::json_uint(json, "/integration/cudathreadsperblock", 256))
+    {
+    }
     IntegratorCartesianGPU(QuadratureProvider &qp, const std::array<uint, dim> grid_sizes, const ctype x_extent = 0,
                            const uint max_block_size = 0)
         : B(qp, grid_sizes, x_extent)
@@ -976,6 +985,10 @@ namespace DiFfRG
   public:
     using ctype = typename get_type::ctype<NT>;
     IntegratorConstant(QuadratureProvider &, const std::array<uint, 1>, const ctype, const uint = 0) {}
+    template <class JSON, typename = decltype(std::declval<const JSON &>().get_uint(""))>
+    IntegratorConstant(QuadratureProvider &, const std::array<uint, 1>, const ctype, const JSON &)
+    {
+    }
     IntegratorConstant(QuadratureProvider &, const uint, const ctype, const uint = 0) {}
     IntegratorConstant() {}
     template <typename... T> NT get(const ctype k, const T &...t) const

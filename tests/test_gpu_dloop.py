@@ -10,7 +10,8 @@ published work units as CTAs free up and leaves after a bounded idle spin.
   slots takes many requests in turn;
 * the loop left alone runs dry: every CTA counts an idle exit, the kernel ends, and the next
   submit relaunches it cleanly with correct results;
-* latency is stamped when a request finishes, not when it is waited for.
+* latency is stamped when a request finishes, not when it is waited for;
+* a small request submitted behind a large one overtakes it (express lane).
 """
 import threading
 import time
@@ -139,6 +140,27 @@ def test_latency_is_stamped_at_completion(dctx, w):
     t.wait(timeout=120)
     st = c.stats()
     assert st["completed"] == 1 and st["max_latency_s"] < 0.25, st
+
+
+def test_small_request_overtakes_a_large_one(dctx, w):
+    """A request of at most 2^22 grid points goes to the express lane: submitted right behind a
+    large request (1024 3D integrals), it finishes while the large one is still running, and
+    both are exact."""
+    c, _, tl = dctx
+    items = serving.rhs_items(w, 0.9)
+    per = len(w["p"])
+    big = [items[i * per + j] for i in range(1, serving.N_FUNC, 2) for j in range(per)][:1024]
+    probe = items[:8]  # 2D integrals
+    c.submit(probe, tl, "fp64").wait(timeout=120)  # warm
+    c.submit(big[:8], tl, "fp64").wait(timeout=120)
+    tb = c.submit(big, tl, "fp64")
+    tp = c.submit(probe, tl, "fp64")
+    got_p = tp.wait(timeout=300)
+    assert tb.poll() is None  # the large request is still running
+    got_b = tb.wait(timeout=300)
+    assert _close(got_p, [c.get(g, tl, "fp64") for g in probe])
+    sub = big[::97]
+    assert _close(got_b[::97], [c.get(g, tl, "fp64") for g in sub])
 
 
 def test_request_reads_one_table_epoch(dctx, w):
