@@ -523,6 +523,7 @@ namespace gbint
     if (!b->arena) {
       cudaFree(b->d_items);
       cudaFree(b->d_units);
+      cudaFree(b->d_expand);
       cudaFree(b->d_segs);
       cudaFree(b->d_seg);
       cudaFree(b->d_aux);
@@ -538,8 +539,9 @@ namespace gbint
 
   size_t batch_device_bytes(const gb_batch *b)
   {
-    const size_t n = b->n, nu = b->units.size();
-    return n * sizeof(ItemDev) + nu * sizeof(UnitDev) + b->segs.size() * sizeof(SegDev) +
+    const size_t n = b->n, nu = b->n_units_total;
+    return n * sizeof(ItemDev) + nu * sizeof(UnitDev) + b->expand.size() * sizeof(ExpandDev) +
+           b->segs.size() * sizeof(SegDev) +
            b->seg_total * sizeof(double) + b->aux.size() * sizeof(float4) + nu * sizeof(double) + n * sizeof(int) +
            b->runs.size() * sizeof(int) + n * sizeof(double);
   }
@@ -886,13 +888,19 @@ namespace gbint
       b->plain_loop_axis.push_back(loop_axis);
       b->plain_threads.push_back(pt);
     }
-    // units grouped by kind
+    // units grouped by kind; built on the host only when a run goes out in cost order (a
+    // permutation), else expanded on the device from one range per integral
+    b->host_units = false;
+    for (int i = 0; i < n; ++i)
+      if (item_kind[i] != K_GENERIC && resolve_schedule(ctx, item_kind[i]).unit_order == GB_ORDER_COST)
+        b->host_units = true;
+    long long nunits = 0;
     const int kinds[11] = {K_S1,         K_S2,         K_S3,          K_S5,          K_S1 | K_ACC, K_S2 | K_ACC,
                            K_S3 | K_ACC, K_S3R | K_ACC, K_S5 | K_ACC, K_S5Z | K_ACC, K_GENERIC};
     for (int kind : kinds) {
       gb_batch::KindRun run;
       run.kind = kind;
-      run.unit_begin = (int)b->units.size();
+      run.unit_begin = (int)nunits;
       const int kb = kind_base(kind);
       const gb_schedule sc = kind == K_GENERIC ? gb_schedule{kGenericThreads, kGenericPPT, 1, GB_ORDER_ITEM}
                                                : resolve_schedule(ctx, kind);
@@ -912,16 +920,22 @@ namespace gbint
           it.rows <<= split_log2;
         }
         const int nu = (it.rows + rpu - 1) / rpu;
-        it.unit_begin = (int)b->units.size() - run.unit_begin;
+        if (nunits + nu > (long long)INT32_MAX) return set_error(ctx, GB_EINVAL, "batch has more than 2^31 work units");
+        it.unit_begin = (int)(nunits - run.unit_begin);
         it.n_units = nu;
-        for (int u = 0; u < nu; ++u) {
-          UnitDev U{};
-          U.item = i;
-          U.row_begin = u * rpu;
-          U.row_count = std::min(rpu, it.rows - u * rpu);
-          U.slot = it.unit_begin + u;
-          b->units.push_back(U);
+        if (b->host_units) {
+          for (int u = 0; u < nu; ++u) {
+            UnitDev U{};
+            U.item = i;
+            U.row_begin = u * rpu;
+            U.row_count = std::min(rpu, it.rows - u * rpu);
+            U.slot = it.unit_begin + u;
+            b->units.push_back(U);
+          }
+        } else {
+          b->expand.push_back(ExpandDev{i, (int)nunits, nu, it.rows, rpu, it.unit_begin});
         }
+        nunits += nu;
         if (kind != K_GENERIC) {
           int tb = 0;
           for (int t = 0; t < tables_needed(it.integrand); ++t) {
@@ -941,8 +955,8 @@ namespace gbint
         }
       }
       if (!any) continue;
-      run.n_units = (int)b->units.size() - run.unit_begin;
-      if (sc.unit_order == GB_ORDER_COST && kind != K_GENERIC) {
+      run.n_units = (int)(nunits - run.unit_begin);
+      if (b->host_units && sc.unit_order == GB_ORDER_COST && kind != K_GENERIC) {
         // largest cost (rows x points per row) first; ties keep item order
         std::vector<double> per_row(n, 0.0);
         for (int i = 0; i < n; ++i)
@@ -969,6 +983,7 @@ namespace gbint
       }
       b->runs.push_back(run);
     }
+    b->n_units_total = (size_t)nunits;
     return GB_OK;
   }
 
@@ -987,7 +1002,7 @@ namespace gbint
       return rc;
     }
     // device buffers
-    const size_t nu = b->units.size();
+    const size_t nu = b->n_units_total;
     const size_t bytes = batch_device_bytes(b);
     if (ctx->in_use + bytes > ctx->budget) {
       free_batch(ctx, b);
@@ -999,6 +1014,7 @@ namespace gbint
     };
     alloc((void **)&b->d_items, n * sizeof(ItemDev));
     alloc((void **)&b->d_units, nu * sizeof(UnitDev));
+    alloc((void **)&b->d_expand, b->expand.size() * sizeof(ExpandDev));
     alloc((void **)&b->d_segs, b->segs.size() * sizeof(SegDev));
     alloc((void **)&b->d_seg, b->seg_total * sizeof(double));
     alloc((void **)&b->d_aux, b->aux.size() * sizeof(float4));
@@ -1009,7 +1025,13 @@ namespace gbint
     b->bytes = bytes;
     ctx->in_use += bytes;
     if (e == cudaSuccess) e = cudaMemcpy(b->d_items, b->items.data(), n * sizeof(ItemDev), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(b->d_units, b->units.data(), nu * sizeof(UnitDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && b->host_units)
+      e = cudaMemcpy(b->d_units, b->units.data(), nu * sizeof(UnitDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !b->host_units) {
+      e = cudaMemcpy(b->d_expand, b->expand.data(), b->expand.size() * sizeof(ExpandDev), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = launch_expand_units(b->d_expand, (int)b->expand.size(), b->d_units, ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    }
     if (e == cudaSuccess && !b->segs.empty())
       e = cudaMemcpy(b->d_segs, b->segs.data(), b->segs.size() * sizeof(SegDev), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !b->aux.empty())
@@ -1044,6 +1066,7 @@ namespace gbint
     P.item_count = b->d_item_count;
     P.out = d_out ? d_out : b->d_out;
     P.err = ctx->d_err;
+    P.single = b->single ? 1 : 0;
     // the segment kernel zeroes the run counters; without segments a memset does
     if (!b->segs.empty())
       GB_CUDA(launch_seg(b->d_segs, (int)b->segs.size(), b->seg_max_entries, P.pv, P.pw, P.aux, P.tabs, b->d_seg,
@@ -1787,7 +1810,7 @@ int gb_batch_info(gb_ctx *ctx, gb_batch *b, uint64_t *points, int *n_units, int 
 {
   if (!ctx || !b) return GB_EINVAL;
   if (points) *points = b->points;
-  if (n_units) *n_units = (int)b->units.size();
+  if (n_units) *n_units = (int)b->n_units_total;
   if (n_items) *n_items = b->n;
   return GB_OK;
 }

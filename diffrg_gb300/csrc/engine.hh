@@ -89,7 +89,10 @@ struct gb_batch {
   int precision = GB_PREC_FP32C;
   std::vector<gb_integral> src;
   std::vector<gbint::ItemDev> items;
-  std::vector<gbint::UnitDev> units;
+  std::vector<gbint::UnitDev> units;       // host-built units (cost-ordered runs only)
+  std::vector<gbint::ExpandDev> expand;    // per-integral unit ranges, expanded on the device
+  size_t n_units_total = 0;
+  bool host_units = false;
   std::vector<gbint::SegDev> segs;
   std::vector<float4> aux;  // per-item constants (S kinds)
   struct KindRun {
@@ -106,6 +109,7 @@ struct gb_batch {
   // device
   gbint::ItemDev *d_items = nullptr;
   gbint::UnitDev *d_units = nullptr;
+  gbint::ExpandDev *d_expand = nullptr;
   gbint::SegDev *d_segs = nullptr;
   double *d_seg = nullptr;
   float4 *d_aux = nullptr;
@@ -120,6 +124,7 @@ struct gb_batch {
   // axes held in the node pool while the batch exists
   std::vector<gbint::AxisKey> held;
   bool arena = false;  // device buffers belong to a serving slot (not freed with the batch)
+  bool single = false;  // one CTA per work unit, each evaluating its own unit (serving)
 };
 
 struct gb_ctx {

@@ -78,6 +78,13 @@ namespace gbint
     int slot;  // partial-sum slot: the unit's position in item order (units may run in another order)
   };
 
+  // the work units of one integral, expanded on the device into UnitDev records
+  // (units[unit0 + u] = {item, u * rpu, min(rpu, rows - u * rpu), slot0 + u}): the host plans
+  // per integral, not per unit
+  struct ExpandDev {
+    int item, unit0, n_units, rows, rpu, slot0;
+  };
+
   // table directory entry (device): current FP32 data + axes
   struct TableDev {
     const float *data;
@@ -114,6 +121,9 @@ namespace gbint
     double *partials;      // per unit
     int *item_count;       // per item arrival counters (reset by the finisher)
     int *unit_counter;     // work-stealing counter (reset by the finisher of the run)
+    int single;            // 1: CTA b evaluates unit b only and retires (a grid of one CTA per
+                           // unit), so that CTAs of a later high-priority launch get SMs as soon
+                           // as units finish; 0: persistent CTAs take units from unit_counter
     int *done_counter;     // items finished in this run
     double *out;           // per item results
     int *err;              // device error word

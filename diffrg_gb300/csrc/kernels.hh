@@ -17,6 +17,8 @@ namespace gbint
   cudaError_t launch_seg(const SegDev *segs, int n_segs, int total_entries, const double *pv, const double *pw,
                          const float4 *aux, const TableDev *tabs, double *seg_out, int *counters, int n_counters,
                          cudaStream_t s);
+  // writes the UnitDev records of n integrals' unit ranges, in stream order
+  cudaError_t launch_expand_units(const ExpandDev *ex, int n, UnitDev *units, cudaStream_t s);
   // rebuilds a 1D table's per-cell records (TableDev::cr_off) from its data, in stream order
   cudaError_t launch_cell_records(float *table, int rc_off, int cr_off, int cells, cudaStream_t s);
   // writes one table directory entry in stream order (the entry travels as a kernel parameter)

@@ -1026,8 +1026,22 @@ namespace gbint
     }
   } // namespace
 
+  // resident CTAs per SM the register allocation is held to.  Left to itself the compiler gives
+  // S3R 128 registers (16 warps per SM), S2 80 and S5Z 90; these kernels are issue-bound and
+  // want the warps: S3R capped at 96 / 80 / 64 registers (128 / 256 / 512 threads) runs 6-8 %
+  // faster on C3, S2 at 64 and S5Z at 80 get back the occupancy their earlier forms had
+  // (measured on GB300; the caps spill a few words at most)
+  template <int KIND, int THREADS> constexpr int min_ctas_per_sm()
+  {
+    if constexpr (KIND == K_S3R) return THREADS == 128 ? 5 : (THREADS == 256 ? 3 : 2);
+    if constexpr (KIND == K_S2) return 1024 / THREADS;
+    if constexpr (KIND == K_S5Z) return THREADS == 128 ? 6 : (THREADS == 256 ? 3 : 2);
+    return 1;
+  }
+
   template <int KIND, bool ACC, int THREADS>
-  __global__ void __launch_bounds__(THREADS) k_fp32c(const RunParams P, int tab_bytes_cap, int rec_cap)
+  __global__ void __launch_bounds__(THREADS, (min_ctas_per_sm<KIND, THREADS>()))
+      k_fp32c(const RunParams P, int tab_bytes_cap, int rec_cap)
   {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr int NT = Traits<KIND>::kTables;
@@ -1050,7 +1064,7 @@ namespace gbint
       mbar_fence_init();
       for (int i = 0; i < 4; ++i) s_slot[i] = -2;
       s_tabok = 1;
-      const int u = atomicAdd(P.unit_counter, 1);
+      const int u = P.single ? (int)blockIdx.x : atomicAdd(P.unit_counter, 1);
       s_next[0] = u;
       if (u < P.n_units) issue_records(KIND, P, u, rec_s0, &bar[0]);
     }
@@ -1125,7 +1139,7 @@ namespace gbint
       }
       // prefetch the next unit's records into the other buffer
       if (threadIdx.x == 0) {
-        const int un = atomicAdd(P.unit_counter, 1);
+        const int un = P.single ? P.n_units : atomicAdd(P.unit_counter, 1);
         s_next[buf ^ 1] = un;
         if (un < P.n_units) issue_records(KIND, P, un, buf ? rec_s0 : rec_s1, &bar[buf ^ 1]);
       }
@@ -1201,7 +1215,7 @@ namespace gbint
     case K_S5Z:
       return gb_schedule{256, 1, 2, GB_ORDER_ITEM};
     case K_S3R:
-      return gb_schedule{256, 1, 1, GB_ORDER_ITEM};
+      return gb_schedule{128, 2, 1, GB_ORDER_ITEM};
     default:
       return gb_schedule{256, 1, 1, GB_ORDER_ITEM};
     }

@@ -21,8 +21,9 @@ namespace gbint
     __shared__ double red[32];
     __shared__ int s_unit, s_flag;
     __shared__ TableDev sT[4];
-    for (;;) {
-      if (threadIdx.x == 0) s_unit = atomicAdd(P.unit_counter, 1);
+    for (int iter = 0;; ++iter) {
+      if (threadIdx.x == 0)
+        s_unit = P.single ? (iter == 0 ? (int)blockIdx.x : P.n_units) : atomicAdd(P.unit_counter, 1);
       __syncthreads();
       const int u = s_unit;
       if (u >= P.n_units) break;
@@ -203,6 +204,29 @@ namespace gbint
     return cudaGetLastError();
   }
   __global__ void k_dir_set(TableDev *dst, const TableDev v) { *dst = v; }
+
+  // one CTA per integral (grid-stride), its threads over the integral's units
+  __global__ void k_expand_units(const ExpandDev *ex, int n, UnitDev *units)
+  {
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+      const ExpandDev e = ex[i];
+      for (int u = threadIdx.x; u < e.n_units; u += blockDim.x) {
+        UnitDev U;
+        U.item = e.item;
+        U.row_begin = u * e.rpu;
+        U.row_count = min(e.rpu, e.rows - u * e.rpu);
+        U.slot = e.slot0 + u;
+        units[(size_t)e.unit0 + u] = U;
+      }
+    }
+  }
+
+  cudaError_t launch_expand_units(const ExpandDev *ex, int n, UnitDev *units, cudaStream_t s)
+  {
+    if (n <= 0) return cudaSuccess;
+    k_expand_units<<<n < 4096 ? n : 4096, 256, 0, s>>>(ex, n, units);
+    return cudaGetLastError();
+  }
 
   // per-cell records of a 1D table: {1/c_j hi, lo, y_j, hi(d_j)} and lo(d_j), d_j = y_{j+1} - y_j
   // split exactly into two floats

@@ -58,6 +58,7 @@ namespace gbint
       size_t cap_items = 0, cap_units = 0, cap_segs = 0, cap_seg = 0, cap_aux = 0, bytes = 0;
       ItemDev *d_items = nullptr;
       UnitDev *d_units = nullptr;
+      ExpandDev *d_expand = nullptr;
       SegDev *d_segs = nullptr;
       double *d_seg = nullptr, *d_partials = nullptr, *d_out = nullptr;
       float4 *d_aux = nullptr;
@@ -65,6 +66,7 @@ namespace gbint
       // pinned staging of the same capacities
       ItemDev *h_items = nullptr;
       UnitDev *h_units = nullptr;
+      ExpandDev *h_expand = nullptr;
       SegDev *h_segs = nullptr;
       float4 *h_aux = nullptr;
       double *h_out = nullptr;
@@ -99,6 +101,7 @@ namespace gbint
     {
       cudaFree(sl.d_items);
       cudaFree(sl.d_units);
+      cudaFree(sl.d_expand);
       cudaFree(sl.d_segs);
       cudaFree(sl.d_seg);
       cudaFree(sl.d_aux);
@@ -108,6 +111,7 @@ namespace gbint
       cudaFree(sl.d_counters);
       cudaFreeHost(sl.h_items);
       cudaFreeHost(sl.h_units);
+      cudaFreeHost(sl.h_expand);
       cudaFreeHost(sl.h_segs);
       cudaFreeHost(sl.h_aux);
       cudaFreeHost(sl.h_out);
@@ -122,7 +126,8 @@ namespace gbint
 
     size_t arena_bytes(size_t items, size_t units, size_t segs, size_t seg, size_t aux)
     {
-      return items * (sizeof(ItemDev) + sizeof(double) + sizeof(int)) + units * (sizeof(UnitDev) + sizeof(double)) +
+      return items * (sizeof(ItemDev) + sizeof(ExpandDev) + sizeof(double) + sizeof(int)) +
+             units * (sizeof(UnitDev) + sizeof(double)) +
              segs * sizeof(SegDev) + seg * sizeof(double) + aux * sizeof(float4) + kMaxRunsPerBatch * sizeof(int);
     }
 
@@ -149,6 +154,7 @@ namespace gbint
       };
       dev((void **)&sl.d_items, ni * sizeof(ItemDev));
       dev((void **)&sl.d_units, nu * sizeof(UnitDev));
+      dev((void **)&sl.d_expand, ni * sizeof(ExpandDev));
       dev((void **)&sl.d_segs, ns * sizeof(SegDev));
       dev((void **)&sl.d_seg, nseg * sizeof(double));
       dev((void **)&sl.d_aux, na * sizeof(float4));
@@ -158,6 +164,7 @@ namespace gbint
       dev((void **)&sl.d_counters, kMaxRunsPerBatch * sizeof(int));
       host((void **)&sl.h_items, ni * sizeof(ItemDev));
       host((void **)&sl.h_units, nu * sizeof(UnitDev));
+      host((void **)&sl.h_expand, ni * sizeof(ExpandDev));
       host((void **)&sl.h_segs, ns * sizeof(SegDev));
       host((void **)&sl.h_aux, na * sizeof(float4));
       host((void **)&sl.h_out, ni * sizeof(double));
@@ -271,7 +278,7 @@ namespace gbint
       gb_batch *b = new gb_batch();
       int rc = plan_batch(ctx, items.data(), n, tl.data(), tn.data(), g[0]->precision, b);
       if (rc == GB_OK && b->runs.size() > (size_t)kMaxRunsPerBatch) rc = set_error(ctx, GB_EINVAL, "too many kind runs");
-      if (rc == GB_OK) rc = reserve(ctx, sl, n, b->units.size(), b->segs.size(), b->seg_total, b->aux.size());
+      if (rc == GB_OK) rc = reserve(ctx, sl, n, b->n_units_total, b->segs.size(), b->seg_total, b->aux.size());
       if (rc) {
         free_batch(ctx, b);
         return rc;
@@ -280,6 +287,7 @@ namespace gbint
       b->arena = true;
       b->d_items = sl.d_items;
       b->d_units = sl.d_units;
+      b->d_expand = sl.d_expand;
       b->d_segs = sl.d_segs;
       b->d_seg = sl.d_seg;
       b->d_aux = sl.d_aux;
@@ -287,16 +295,27 @@ namespace gbint
       b->d_item_count = sl.d_item_count;
       b->d_counters = sl.d_counters;
       b->d_out = sl.d_out;
-      for (auto &run : b->runs) run.ctas = run.n_units;  // not persistent: SMs free up per unit
+      // not persistent: one CTA per unit that retires after it, so SMs free up per unit
+      b->single = true;
+      for (auto &run : b->runs) run.ctas = run.n_units;
       std::memcpy(sl.h_items, b->items.data(), n * sizeof(ItemDev));
-      std::memcpy(sl.h_units, b->units.data(), b->units.size() * sizeof(UnitDev));
+      // the units themselves are written on the device from one range per integral (or, for a
+      // cost-ordered run, uploaded as built)
+      if (b->host_units)
+        std::memcpy(sl.h_units, b->units.data(), b->units.size() * sizeof(UnitDev));
+      else
+        std::memcpy(sl.h_expand, b->expand.data(), b->expand.size() * sizeof(ExpandDev));
       if (!b->segs.empty()) std::memcpy(sl.h_segs, b->segs.data(), b->segs.size() * sizeof(SegDev));
       if (!b->aux.empty()) std::memcpy(sl.h_aux, b->aux.data(), b->aux.size() * sizeof(float4));
       const cudaStream_t s = b->points < kSmallBatchPoints ? sl.s_hi : sl.s_lo;
       cudaError_t e = cudaStreamWaitEvent(s, ctx->tables_event, 0);
       if (e == cudaSuccess) e = cudaMemcpyAsync(sl.d_items, sl.h_items, n * sizeof(ItemDev), cudaMemcpyHostToDevice, s);
-      if (e == cudaSuccess)
+      if (e == cudaSuccess && b->host_units)
         e = cudaMemcpyAsync(sl.d_units, sl.h_units, b->units.size() * sizeof(UnitDev), cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess && !b->host_units) {
+        e = cudaMemcpyAsync(sl.d_expand, sl.h_expand, b->expand.size() * sizeof(ExpandDev), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = launch_expand_units(sl.d_expand, (int)b->expand.size(), sl.d_units, s);
+      }
       if (e == cudaSuccess && !b->segs.empty())
         e = cudaMemcpyAsync(sl.d_segs, sl.h_segs, b->segs.size() * sizeof(SegDev), cudaMemcpyHostToDevice, s);
       if (e == cudaSuccess && !b->aux.empty())

@@ -6,7 +6,8 @@
 * a request in flight reads one table epoch, never a mixture (table updates are ordered);
 * cancel / poll / unknown tickets / HBM-budget admission;
 * the node pool evicts unheld axes, so an RG flow with a new k per stage never runs out;
-* one Cash-Karp step of the C4 flow, FP32-compensated against FP64.
+* one Cash-Karp step of the C4 flow, FP32-compensated against FP64;
+* a small request behind a large one finishes first (one CTA per unit, priority streams).
 """
 
 import numpy as np
@@ -49,6 +50,28 @@ def serve_all(ctx, items, tlist, sizes, precision="fp32c"):
     for o, t in tk:
         out[o:o + t.n] = t.wait(timeout=300)
     return out
+
+
+def test_small_request_is_not_held_behind_a_large_one(sctx, tabs, w):
+    """Serving grids run one CTA per work unit, each retiring after its unit, and small batches
+    go to high-priority streams: a small request submitted right behind a large one (2048 3D
+    integrals, the largest C4 request) finishes while the large one is still running, with the
+    same bits as alone."""
+    _, tlist = tabs
+    items = serving.rhs_items(w, 0.85)
+    per = len(w["p"])
+    big = [items[i * per + j] for i in range(1, serving.N_FUNC, 2) for j in range(per)][:2048]
+    probe = items[:8]
+    alone = sctx.submit(probe, tlist, "fp32c").wait(timeout=120)
+    sctx.submit(big, tlist, "fp32c").wait(timeout=120)  # warm: arenas, axes
+    overtaken = 0
+    for _ in range(3):
+        tb = sctx.submit(big, tlist, "fp32c")
+        got = sctx.submit(probe, tlist, "fp32c").wait(timeout=120)
+        overtaken += tb.poll() is None
+        tb.wait(timeout=300)
+        assert np.array_equal(got, alone)
+    assert overtaken >= 2
 
 
 def test_served_equals_batch_and_oracle(sctx, tabs, w, oracle):
