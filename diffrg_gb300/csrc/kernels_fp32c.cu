@@ -84,8 +84,10 @@ namespace gbint
     // ln(1+t) = t + t^2 Q(t), t = x/c_j - 1 formed in double-float (p.hi - 1 is exact) and
     // |t| <= sqrt(1.25) - 1 + (one cell when j is off by one near a cell edge); Q is the series
     // through t^9/9, truncation < 3e-10 of a cell.
-    // SQ: x is the square of the axis coordinate (1/c_j^2 formed from 1/c_j, half the scale)
-    template <bool SQ = false>
+    // SQ: x is the square of the axis coordinate (1/c_j^2 formed from 1/c_j, half the scale).
+    // DEG 6: the series through t^6 (Q through t^4/6), for callers that guarantee |t| within the
+    // half-width of cells at most 6 % wide (truncation < 1e-10 of a cell)
+    template <bool SQ = false, int DEG = 9>
     __device__ __forceinline__ float cell_frac_rr(const AxisDev &a, df rr, df x, df *t_out = nullptr)
     {
       // t = x rr - 1 = th + tl: th = fl(x.hi rr.hi) - 1 is exact (the product lies in [1/2, 2]),
@@ -96,12 +98,17 @@ namespace gbint
       const float tl0 = __fadd_rn(__fmaf_rn(x.hi, rr.hi, -ph), __fmaf_rn(x.hi, rr.lo, __fmul_rn(x.lo, rr.hi)));
       const df t{th, __fmaf_rn(-th, tl0, tl0)};
       if (t_out) *t_out = df{th, tl0};  // x / c_j - 1 itself (the log's correction term aside)
-      float Q = __fmaf_rn(th, 1.11111111e-01f, -1.25e-01f);  // 1/9, -1/8
-      Q = __fmaf_rn(th, Q, 1.42857143e-01f);                  // 1/7
-      Q = __fmaf_rn(th, Q, -1.66666667e-01f);                 // -1/6
-      Q = __fmaf_rn(th, Q, 2.0e-01f);                         // 1/5
-      Q = __fmaf_rn(th, Q, -2.5e-01f);                        // -1/4
-      Q = __fmaf_rn(th, Q, 3.33333343e-01f);                  // 1/3
+      float Q;
+      if constexpr (DEG >= 9) {
+        Q = __fmaf_rn(th, 1.11111111e-01f, -1.25e-01f);  // 1/9, -1/8
+        Q = __fmaf_rn(th, Q, 1.42857143e-01f);            // 1/7
+        Q = __fmaf_rn(th, Q, -1.66666667e-01f);           // -1/6
+        Q = __fmaf_rn(th, Q, 2.0e-01f);                   // 1/5
+      } else {
+        Q = __fmaf_rn(th, -1.66666667e-01f, 2.0e-01f);  // -1/6, 1/5
+      }
+      Q = __fmaf_rn(th, Q, -2.5e-01f);        // -1/4
+      Q = __fmaf_rn(th, Q, 3.33333343e-01f);  // 1/3
       Q = __fmaf_rn(th, Q, -0.5f);
       const float rest = __fmaf_rn(__fmul_rn(th, th), Q, t.lo);  // ln(1+t) = th + rest
       const float kh = SQ ? 0.5f * a.kln.hi : a.kln.hi, kl = SQ ? 0.5f * a.kln.lo : a.kln.lo;
@@ -726,52 +733,55 @@ namespace gbint
     // coefficients are staged beside them instead of read through L1.  t2 follows from r2
     // (t2 = r2/2 + q^2/2 - P^2/4).  Staged layout (floats): [0] B's regulator coefficients,
     // toff[t] for t = 1..3: the records of table t, then its difference low words.
+    // tlo, thi: the bounds of x / c_j - 1 inside cell j (2^(-+1/2 / scale) - 1)
     struct RecTab {
       const float4 *rec;
       const float *dlo;
+      float tlo, thi;
     };
-    __device__ __forceinline__ RecTab rec_tab(const float *tab, int off, int cells)
+    __device__ __forceinline__ RecTab rec_tab(const float *tab, int off, int cells, const AxisDev &a)
     {
-      return RecTab{reinterpret_cast<const float4 *>(tab + off), tab + off + 4 * cells};
+      const float hw = __fdividef(0.5f, a.scale.hi);
+      return RecTab{reinterpret_cast<const float4 *>(tab + off), tab + off + 4 * cells, exp2f(-hw) - 1.f,
+                    exp2f(hw) - 1.f};
     }
+    // cells at most 6 % wide: the short series of cell_frac_rr applies
+    __device__ __forceinline__ bool narrow_cells(const AxisDev &a) { return a.scale.hi >= 11.9f; }
     // cell j and fraction of x (x.hi > 0 or NaN; NaN lands in a clamped cell) on a record table,
     // clamped like log_cell_frac; r = the record of cell j; (jt, t): the cell whose centre t =
-    // x / c_jt - 1 refers to, or jt = -1 where x lies outside the table
-    __device__ __forceinline__ float rec_cell_frac(const AxisDev &a, const float4 *rec, df x, int &j, float4 &r,
-                                                   int &jt, df &t)
+    // x / c_jt - 1 refers to, or jt = -1 where x lies outside the table.  The fast log2 can put
+    // x one cell off near a cell edge; that shows as x / c_j - 1 outside the cell's bounds and
+    // is corrected before the fraction, so the series only ever sees |t| within half a cell
+    // (DEG 6 for cells at most 6 % wide).
+    template <int DEG>
+    __device__ __forceinline__ float rec_cell_frac(const AxisDev &a, const RecTab &T, df x, int &j, float4 &r, int &jt,
+                                                   df &t)
     {
       const int n = a.n;
       jt = -1;
       const float ua = __fmaf_rn(a.scale.hi, __log2f(x.hi), a.shift.hi);
       if (ua < -0.01f) {
         j = 0;
-        r = rec[0];
+        r = T.rec[0];
         return 0.f;
       }
       if (ua > (float)(n - 1) + 0.01f) {
         j = n - 2;
-        r = rec[n - 2];
+        r = T.rec[n - 2];
         return 1.f;
       }
       j = min(max((int)floorf(ua), 0), n - 2);
-      jt = j;
-      r = rec[j];
-      float f = cell_frac_rr(a, df{r.x, r.y}, x, &t);
-      if (f < 0.f) {
-        if (j > 0) {
-          j -= 1;
-          f = __fadd_rn(f, 1.f);
-          r = rec[j];
-        } else
-          f = 0.f;
-      } else if (f > 1.f) {
-        if (j < n - 2) {
-          j += 1;
-          f = __fsub_rn(f, 1.f);
-          r = rec[j];
-        } else
-          f = 1.f;
+      r = T.rec[j];
+      const float th0 = __fsub_rn(__fmul_rn(x.hi, r.x), 1.0f);
+      if (th0 > T.thi && j < n - 2) {
+        j += 1;
+        r = T.rec[j];
+      } else if (th0 < T.tlo && j > 0) {
+        j -= 1;
+        r = T.rec[j];
       }
+      jt = j;
+      const float f = cell_frac_rr<false, DEG>(a, df{r.x, r.y}, x, &t);
       return fminf(fmaxf(f, 0.f), 1.f);
     }
     // y_j + f (y_{j+1} - y_j) from a record, unnormalised (the same operations as lerp_df_u)
@@ -781,21 +791,21 @@ namespace gbint
       const df s = two_sum(r.z, p.hi);
       return df{s.hi, __fadd_rn(s.lo, __fmaf_rn(f, dlo, p.lo))};
     }
-    __device__ __forceinline__ df G1_rec(const RecTab &T, const float4 *rq, const AxisDev &a, df x)
+    template <int DEG> __device__ __forceinline__ df G1_rec(const RecTab &T, const float4 *rq, const AxisDev &a, df x)
     {
       int j, jt;
       float4 r;
       df t;
-      const float f = rec_cell_frac(a, T.rec, x, j, r, jt, t);
+      const float f = rec_cell_frac<DEG>(a, T, x, j, r, jt, t);
       const df R = jt >= 0 ? reg_R_cell<true>(rq, jt, t) : reg_R_df(x);
       return df_prop(rec_lerp_u(r, T.dlo[j], f), x, R);
     }
-    __device__ __forceinline__ df V1_rec(const RecTab &T, const AxisDev &a, df x)
+    template <int DEG> __device__ __forceinline__ df V1_rec(const RecTab &T, const AxisDev &a, df x)
     {
       int j, jt;
       float4 r;
       df t;
-      const float f = rec_cell_frac(a, T.rec, x, j, r, jt, t);
+      const float f = rec_cell_frac<DEG>(a, T, x, j, r, jt, t);
       return rec_lerp_u(r, T.dlo[j], f);
     }
     // part / nsplit: this call sums the phi nodes l = part, part + nsplit, ... of the row
@@ -818,24 +828,33 @@ namespace gbint
       const df Ct = df_add(df_scale2(q2, 0.5f), df_neg(df{c1.z, c1.w}));  // t2 - r2 / 2
       const df third = dfc(1.0 / 3.0);
       const df sbd = df_mul(q2pp, third);
-      const RecTab TB = rec_tab(tab, toff[1], sT[1].n0 - 1), TC = rec_tab(tab, toff[2], sT[2].n0 - 1),
-                   TD = rec_tab(tab, toff[3], sT[3].n0 - 1);
-      const float4 *rqB = reinterpret_cast<const float4 *>(tab + toff[0]);
       const AxisDev aB = sT[1].a0, aC = sT[2].a0, aD = sT[3].a0;
+      const RecTab TB = rec_tab(tab, toff[1], sT[1].n0 - 1, aB), TC = rec_tab(tab, toff[2], sT[2].n0 - 1, aC),
+                   TD = rec_tab(tab, toff[3], sT[3].n0 - 1, aD);
+      const float4 *rqB = reinterpret_cast<const float4 *>(tab + toff[0]);
       const int nf = it.ax[2].n;
       // the phi rule is symmetric and the integrand reads phi through cos(phi) only (see row_s3)
       const int nh = (nf + 1) >> 1;
-      AccDF k;
+      auto phi_loop = [&](auto deg) {
+        constexpr int DEG = decltype(deg)::value;
+        AccDF k;
 #pragma unroll 1
-      for (int l = part; l < nh; l += nsplit) {
-        const NodeRec r = rc[l];  // a = cos(phi), w = 2 pi w_phi
-        const df r2 = df_max(lin_dd(A, B, r.a_hi, r.a_lo), 1e-30f);
-        const df t2 = df_max(df_add(df_scale2(r2, 0.5f), Ct), 1e-30f);
-        const df sv = df_add(sbd, df_mul(r2, third));
-        const df g = df_mul_u(df_mul_u(G1_rec(TB, rqB, aB, r2), V1_rec(TC, aC, sv)), V1_rec(TD, aD, t2));
-        k.add_prod(df_scale2(rec_w(r), 2 * l + 1 == nf ? 1.f : 2.f), g);
-      }
-      return P.seg[it.seg_off + i] * P.pw[it.ax[1].off + j] * k.value();
+        for (int l = part; l < nh; l += nsplit) {
+          const NodeRec r = rc[l];  // a = cos(phi), w = 2 pi w_phi
+          const df r2 = df_max(lin_dd(A, B, r.a_hi, r.a_lo), 1e-30f);
+          const df t2 = df_max(df_add(df_scale2(r2, 0.5f), Ct), 1e-30f);
+          const df sv = df_add(sbd, df_mul(r2, third));
+          const df g = df_mul_u(df_mul_u(G1_rec<DEG>(TB, rqB, aB, r2), V1_rec<DEG>(TC, aC, sv)), V1_rec<DEG>(TD, aD, t2));
+          k.add_prod(df_scale2(rec_w(r), 2 * l + 1 == nf ? 1.f : 2.f), g);
+        }
+        return k.value();
+      };
+      // the short series when all three tables have cells at most 6 % wide (one branch per row,
+      // the same for every thread of a unit)
+      const double inner = (narrow_cells(aB) && narrow_cells(aC) && narrow_cells(aD))
+                               ? phi_loop(std::integral_constant<int, 6>{})
+                               : phi_loop(std::integral_constant<int, 9>{});
+      return P.seg[it.seg_off + i] * P.pw[it.ax[1].off + j] * inner;
     }
 
     // ---------------------------------------------------------------- S5: (q, c1, c2, phi) x VERT4
@@ -1029,12 +1048,13 @@ namespace gbint
   // resident CTAs per SM the register allocation is held to.  Left to itself the compiler gives
   // S3R 128 registers (16 warps per SM), S2 80 and S5Z 90; these kernels are issue-bound and
   // want the warps: S3R capped at 96 / 80 / 64 registers (128 / 256 / 512 threads) runs 6-8 %
-  // faster on C3, S2 at 64 and S5Z at 80 get back the occupancy their earlier forms had
-  // (measured on GB300; the caps spill a few words at most)
+  // faster on C3, S2 at 48 (40 warps per SM, hiding its slice loads) 4 % faster on C2 than at
+  // 64, S5Z at 80 gets back the occupancy its earlier form had (measured on GB300; the caps
+  // spill a few words at most)
   template <int KIND, int THREADS> constexpr int min_ctas_per_sm()
   {
     if constexpr (KIND == K_S3R) return THREADS == 128 ? 5 : (THREADS == 256 ? 3 : 2);
-    if constexpr (KIND == K_S2) return 1024 / THREADS;
+    if constexpr (KIND == K_S2) return 1280 / THREADS;
     if constexpr (KIND == K_S5Z) return THREADS == 128 ? 6 : (THREADS == 256 ? 3 : 2);
     return 1;
   }

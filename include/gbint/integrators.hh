@@ -157,6 +157,9 @@ namespace DiFfRG
     }
 
     gb_ctx *ctx() const { return ctx_.get(); }
+    // the owning handle: in-flight launches hold it, so the context outlives them (copying it is
+    // an atomic increment, no allocation per request)
+    const std::shared_ptr<gb_ctx> &ctx_shared() const { return ctx_; }
     int num_sms() const { return num_sms_; }
 
     // the rules of every QuadratureType (gb_quad_rule: GSL's fixed types with a = 0, b = 1,
@@ -581,7 +584,10 @@ namespace DiFfRG
     // the open batch of type B for the provider's context
     template <class B> std::shared_ptr<B> batch(QuadratureProvider &qp, std::shared_ptr<gb_ctx> keep)
     {
-      const auto key = std::make_pair((const void *)qp.ctx(), std::type_index(typeid(B)));
+      // key: the provider's context and a per-batch-type tag address (pointer comparisons only;
+      // comparing the types' long mangled names would cost more than the request itself)
+      static const char tag = 0;
+      const auto key = std::make_pair((const void *)qp.ctx(), (const void *)&tag);
       auto it = open_.find(key);
       // a batch that is full, or that a future's get() already launched, is closed
       if (it != open_.end() && (it->second->launched() || it->second->size() >= (size_t)gbint_detail::kMaxBatchItems)) {
@@ -599,7 +605,7 @@ namespace DiFfRG
 
   private:
     RequestBatch *prev_;
-    std::map<std::pair<const void *, std::type_index>, std::shared_ptr<gbint_detail::BatchBase>> open_;
+    std::map<std::pair<const void *, const void *>, std::shared_ptr<gbint_detail::BatchBase>> open_;
     std::vector<std::shared_ptr<gbint_detail::BatchBase>> order_;
   };
 
@@ -657,7 +663,7 @@ namespace DiFfRG
         P_.x[a] = qp_->get_device_points<ctype>(n);
         P_.w[a] = qp_->get_device_weights<ctype>(n);
       }
-      std::shared_ptr<gb_ctx> keep() const { return std::shared_ptr<gb_ctx>(qp_->ctx(), [](gb_ctx *) {}); }
+      std::shared_ptr<gb_ctx> keep() const { return qp_->ctx_shared(); }
 
       QuadratureProvider *qp_;
       std::array<uint, NAX> grid_sizes_;
@@ -887,7 +893,7 @@ namespace DiFfRG
       gbint::fam::Params<ctype> P = P_;
       P.k = k;
       const NT c = (NT)KERNEL::constant(k, t...);
-      return gbint_detail::submit<FAM, KERNEL, NT, ctype>(*qp_, std::shared_ptr<gb_ctx>(qp_->ctx(), [](gb_ctx *) {}), P,
+      return gbint_detail::submit<FAM, KERNEL, NT, ctype>(*qp_, qp_->ctx_shared(), P,
                                                           c, t...);
     }
 
@@ -961,7 +967,7 @@ namespace DiFfRG
       P.log_start = std::log(start + P.off);
       P.log_ext = std::log(P.x0_extent / (start + P.off));
       const NT c = (NT)KERNEL::constant(k, t...);
-      return gbint_detail::submit<FAM, KERNEL, NT, ctype>(*qp_, std::shared_ptr<gb_ctx>(qp_->ctx(), [](gb_ctx *) {}), P,
+      return gbint_detail::submit<FAM, KERNEL, NT, ctype>(*qp_, qp_->ctx_shared(), P,
                                                           c, t...);
     }
 
