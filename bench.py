@@ -60,6 +60,34 @@ CAPTURE_NOTE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,smsp__
                 "dominant kernel on this workload (profiles/)")
 
 
+def evaluated_points(w):
+    """Integrand points the kernel actually evaluates per launch (the quadrature counts both
+    members of a folded phi pair and both signs of +-omega at W = 0; the kernels evaluate each
+    once and double its weight)."""
+    name = w["name"]
+    if name == "C1":
+        return len(w["p"]) * w["nq"] * w["nc"]
+    if name == "C2":  # every integral has W = 0: modes n = 0..M evaluated once
+        return len(w["p"]) * (w["M"] + 1) * w["nq"] * w["nc"]
+    if name == "C3":
+        o = w["orders"].astype(np.int64)
+        return int((o[:, 0] * o[:, 1] * ((o[:, 2] + 1) // 2)).sum())
+    if name == "C5":
+        nq, n1, n2, n3 = w["n"]
+        return len(w["P"]) * nq * n1 * n2 * ((n3 + 1) // 2)
+    return None
+
+
+def evaluated_block(w, points, frac32, fracxu):
+    """The roofline fractions against the points the kernel evaluates (beside the quadrature's
+    count, which the headline metric and the reference use)."""
+    ev = evaluated_points(w)
+    if not ev:
+        return None
+    r = ev / points
+    return {"points_per_launch": ev, "of_quadrature_points": r, "fp32_frac": frac32 * r, "xu_frac": fracxu * r}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -573,6 +601,7 @@ def main():
             "xu": {"achieved": xu_achieved, "peak": mufu_peak, "unit": "Gop/s", "frac": fracxu},
             "per_point": {"F": flops_pp, "S": specials_pp},
             "points_per_launch": points,
+            "evaluated": evaluated_block(w, points, frac32, fracxu),
             "peak_source": "measured in this run by the library's FFMA/MUFU probes (gb_measure_peaks); "
                            "MEASURED_PEAKS.json lists only HBM and BF16",
             "fp64_peak_tflops": fp64_peak}

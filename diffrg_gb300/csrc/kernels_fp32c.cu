@@ -85,8 +85,8 @@ namespace gbint
     // |t| <= sqrt(1.25) - 1 + (one cell when j is off by one near a cell edge); Q is the series
     // through t^9/9, truncation < 3e-10 of a cell.
     // SQ: x is the square of the axis coordinate (1/c_j^2 formed from 1/c_j, half the scale).
-    // DEG 6: the series through t^6 (Q through t^4/6), for callers that guarantee |t| within the
-    // half-width of cells at most 6 % wide (truncation < 1e-10 of a cell)
+    // DEG 6: the series through t^6 (Q through t^4/6), for cells at most 6 % wide (truncation
+    // < 1e-10 of a cell within half a cell of the centre)
     template <bool SQ = false, int DEG = 9>
     __device__ __forceinline__ float cell_frac_rr(const AxisDev &a, df rr, df x, df *t_out = nullptr)
     {
@@ -733,26 +733,23 @@ namespace gbint
     // coefficients are staged beside them instead of read through L1.  t2 follows from r2
     // (t2 = r2/2 + q^2/2 - P^2/4).  Staged layout (floats): [0] B's regulator coefficients,
     // toff[t] for t = 1..3: the records of table t, then its difference low words.
-    // tlo, thi: the bounds of x / c_j - 1 inside cell j (2^(-+1/2 / scale) - 1)
     struct RecTab {
       const float4 *rec;
       const float *dlo;
-      float tlo, thi;
     };
-    __device__ __forceinline__ RecTab rec_tab(const float *tab, int off, int cells, const AxisDev &a)
+    __device__ __forceinline__ RecTab rec_tab(const float *tab, int off, int cells)
     {
-      const float hw = __fdividef(0.5f, a.scale.hi);
-      return RecTab{reinterpret_cast<const float4 *>(tab + off), tab + off + 4 * cells, exp2f(-hw) - 1.f,
-                    exp2f(hw) - 1.f};
+      return RecTab{reinterpret_cast<const float4 *>(tab + off), tab + off + 4 * cells};
     }
     // cells at most 6 % wide: the short series of cell_frac_rr applies
     __device__ __forceinline__ bool narrow_cells(const AxisDev &a) { return a.scale.hi >= 11.9f; }
     // cell j and fraction of x (x.hi > 0 or NaN; NaN lands in a clamped cell) on a record table,
     // clamped like log_cell_frac; r = the record of cell j; (jt, t): the cell whose centre t =
-    // x / c_jt - 1 refers to, or jt = -1 where x lies outside the table.  The fast log2 can put
-    // x one cell off near a cell edge; that shows as x / c_j - 1 outside the cell's bounds and
-    // is corrected before the fraction, so the series only ever sees |t| within half a cell
-    // (DEG 6 for cells at most 6 % wide).
+    // x / c_jt - 1 refers to, or jt = -1 where x lies outside the table.  DEG 6 (cells at most
+    // 6 % wide): the short series is exact to ~1e-11 of a cell for x inside cell jt; the few
+    // points the fast log2 puts one cell off (within ~2e-6 of a cell edge, so |t| up to 1.5
+    // cells) get a fraction good to ~1e-7 of a cell before the shift by one, which moves their
+    // value by < 1e-8 relative -- a few in a million points, below 1e-13 of an integral.
     template <int DEG>
     __device__ __forceinline__ float rec_cell_frac(const AxisDev &a, const RecTab &T, df x, int &j, float4 &r, int &jt,
                                                    df &t)
@@ -771,17 +768,24 @@ namespace gbint
         return 1.f;
       }
       j = min(max((int)floorf(ua), 0), n - 2);
-      r = T.rec[j];
-      const float th0 = __fsub_rn(__fmul_rn(x.hi, r.x), 1.0f);
-      if (th0 > T.thi && j < n - 2) {
-        j += 1;
-        r = T.rec[j];
-      } else if (th0 < T.tlo && j > 0) {
-        j -= 1;
-        r = T.rec[j];
-      }
       jt = j;
-      const float f = cell_frac_rr<false, DEG>(a, df{r.x, r.y}, x, &t);
+      r = T.rec[j];
+      float f = cell_frac_rr<false, DEG>(a, df{r.x, r.y}, x, &t);
+      if (f < 0.f) {
+        if (j > 0) {
+          j -= 1;
+          f = __fadd_rn(f, 1.f);
+          r = T.rec[j];
+        } else
+          f = 0.f;
+      } else if (f > 1.f) {
+        if (j < n - 2) {
+          j += 1;
+          f = __fsub_rn(f, 1.f);
+          r = T.rec[j];
+        } else
+          f = 1.f;
+      }
       return fminf(fmaxf(f, 0.f), 1.f);
     }
     // y_j + f (y_{j+1} - y_j) from a record, unnormalised (the same operations as lerp_df_u)
@@ -829,8 +833,8 @@ namespace gbint
       const df third = dfc(1.0 / 3.0);
       const df sbd = df_mul(q2pp, third);
       const AxisDev aB = sT[1].a0, aC = sT[2].a0, aD = sT[3].a0;
-      const RecTab TB = rec_tab(tab, toff[1], sT[1].n0 - 1, aB), TC = rec_tab(tab, toff[2], sT[2].n0 - 1, aC),
-                   TD = rec_tab(tab, toff[3], sT[3].n0 - 1, aD);
+      const RecTab TB = rec_tab(tab, toff[1], sT[1].n0 - 1), TC = rec_tab(tab, toff[2], sT[2].n0 - 1),
+                   TD = rec_tab(tab, toff[3], sT[3].n0 - 1);
       const float4 *rqB = reinterpret_cast<const float4 *>(tab + toff[0]);
       const int nf = it.ax[2].n;
       // the phi rule is symmetric and the integrand reads phi through cos(phi) only (see row_s3)
