@@ -115,13 +115,13 @@ namespace gbint
       const float a0 = __fmaf_rn(kh, th, 0.5f);
       return __fadd_rn(a0, __fmaf_rn(kh, rest, __fmul_rn(kl, th)));
     }
-    template <bool SQ = false>
+    template <bool SQ = false, int DEG = 9>
     __device__ __forceinline__ float cell_frac_at(const AxisDev &a, const float2 *rc, df x, int j, df *t_out = nullptr)
     {
       const float2 r = rc[j];
       df rr{r.x, r.y};
       if constexpr (SQ) rr = df_mul(rr, rr);
-      return cell_frac_rr<SQ>(a, rr, x, t_out);
+      return cell_frac_rr<SQ, DEG>(a, rr, x, t_out);
     }
     // the same fraction as a double-float (its FP32 rounding, ~3e-8 of a cell, is otherwise the
     // largest per-point error of a lookup; used where few points carry an integral)
@@ -148,7 +148,7 @@ namespace gbint
     // axis_frac_df): a fast log2 finds the cell to within one, the fraction decides the rest
     // (jt, t): with jt non-null, the cell whose centre t = x / c_jt - 1 refers to (before the
     // off-by-one correction), or -1 where x lies outside the table and was clamped
-    template <bool SQ = false>
+    template <bool SQ = false, int DEG = 9>
     __device__ __forceinline__ float log_cell_frac(const AxisDev &a, const float2 *rc, df x, int &i, int *jt = nullptr,
                                                    df *t = nullptr)
     {
@@ -167,7 +167,7 @@ namespace gbint
       }
       int j = min(max((int)floorf(ua), 0), n - 2);
       if (jt) *jt = j;
-      float f = cell_frac_at<SQ>(a, rc, x, j, t);
+      float f = cell_frac_at<SQ, DEG>(a, rc, x, j, t);
       if (f < 0.f) {
         if (j > 0) {
           j -= 1;
@@ -958,7 +958,10 @@ namespace gbint
     // slower), A at the c2 nodes (through L1, once per (row, c2)).  A point then lerps along the
     // |q-p|^2 axis only, twice, instead of two double-float bilinears.
     // row = (c1 node j, q node i), q fastest, so a unit spans few c1 nodes.
-    // part / nsplit: this call sums the c2 nodes l = part, part + nsplit, ... of the row
+    // part / nsplit: this call sums the c2 nodes l = part, part + nsplit, ... of the row.
+    // DEG: terms of the cell fraction's ln series (6 when table A's cells are at most 6 % wide,
+    // see rec_cell_frac for the points one cell off)
+    template <int DEG>
     __device__ __forceinline__ double row_s5z(const RunParams &P, const ItemDev &it, int row, int row0, int part,
                                               int nsplit, const NodeRec *rc, const float *tab, const TableDev *sT)
     {
@@ -982,7 +985,7 @@ namespace gbint
       // the |q-p|^2 fraction, and with it the cell and t = x / c - 1 the regulator expansion uses
       auto frac0 = [&](df x, int &ix, int &jt, df &t) -> float {
         jt = -1;
-        return rca ? log_cell_frac(TA.a0, rca, x, ix, &jt, &t) : axis_frac_df(TA.a0, x.hi, x.lo, ix);
+        return rca ? log_cell_frac<false, DEG>(TA.a0, rca, x, ix, &jt, &t) : axis_frac_df(TA.a0, x.hi, x.lo, ix);
       };
       const float4 *zb = reinterpret_cast<const float4 *>(P.seg + it.slice_off2);  // B at c2 node l: [l * ns0]
       const int n2 = it.ax[2].n, n3 = it.ax[3].n;
@@ -1043,7 +1046,9 @@ namespace gbint
       if constexpr (KIND == K_S5) return row_s5<ACC>(P, it, row, rc, tab, sT, toff);
       if constexpr (KIND == K_S5Z) {
         const int sl = it.split_log2;
-        return row_s5z(P, it, row >> sl, row0 >> sl, row & ((1 << sl) - 1), 1 << sl, rc, tab, sT);
+        return narrow_cells(sT[0].a0)
+                   ? row_s5z<6>(P, it, row >> sl, row0 >> sl, row & ((1 << sl) - 1), 1 << sl, rc, tab, sT)
+                   : row_s5z<9>(P, it, row >> sl, row0 >> sl, row & ((1 << sl) - 1), 1 << sl, rc, tab, sT);
       }
       return 0.0;
     }
