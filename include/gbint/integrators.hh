@@ -287,15 +287,18 @@ namespace DiFfRG
       return n;
     }
 
-    // The device results of one launch.  wait() copies them (and the launch's error word) to the
-    // host once through the slot's pinned staging, releases the request slot and turns a CUDA
-    // error into an exception.
+    // The device results of one launch.  Their copy to the slot's pinned staging (results and the
+    // launch's error word, adjacent in the arena) is queued right behind the kernel; wait()
+    // synchronises once, takes the values, releases the request slot and turns a CUDA error into
+    // an exception.
     class LaunchResult
     {
     public:
+      // queued: the launcher already queued the read-back of results + error word into `pinned`
       LaunchResult(std::shared_ptr<gb_ctx> keep, gb_slot slot, int n_values, const double *d_values, const int *d_err,
-                   double *pinned)
-          : keep_(std::move(keep)), slot_(slot), host_(n_values), d_values_(d_values), d_err_(d_err), pinned_(pinned)
+                   double *pinned, bool queued = false)
+          : keep_(std::move(keep)), slot_(slot), host_(n_values), d_values_(d_values), d_err_(d_err), pinned_(pinned),
+            queued_(queued)
       {
       }
       ~LaunchResult()
@@ -311,8 +314,11 @@ namespace DiFfRG
         if (!done_) {
           cudaStream_t s = (cudaStream_t)slot_.stream;
           int *perr = reinterpret_cast<int *>(pinned_ + host_.size());
-          cudaError_t e = cudaMemcpyAsync(pinned_, d_values_, host_.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
-          if (e == cudaSuccess) e = cudaMemcpyAsync(perr, d_err_, sizeof(int), cudaMemcpyDeviceToHost, s);
+          cudaError_t e = cudaSuccess;
+          if (!queued_) {
+            e = cudaMemcpyAsync(pinned_, d_values_, host_.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(perr, d_err_, sizeof(int), cudaMemcpyDeviceToHost, s);
+          }
           if (e == cudaSuccess) e = cudaStreamSynchronize(s);
           if (e == cudaSuccess) {
             std::memcpy(host_.data(), pinned_, host_.size() * sizeof(double));
@@ -334,6 +340,7 @@ namespace DiFfRG
       const double *d_values_;
       const int *d_err_;
       double *pinned_;
+      bool queued_ = false;
       std::mutex mu_;
       bool done_ = false;
       std::string error_;
@@ -367,6 +374,10 @@ namespace DiFfRG
         if (units_ + u > (1ll << 28)) throw std::runtime_error("integrator: grid too large");
         if (items_.empty()) {  // the staging plan follows the first integral
           if constexpr (sizeof...(T) > 0) tables_ = tables_of(t...);
+          // descriptors are ~1 KB with interpolator arguments: no re-copying while a grid's
+          // requests arrive
+          items_.reserve(256);
+          unit_begin_.reserve(256);
         }
         items_.push_back(ItemT{P, gbint::ub::make_pack(t...)});
         unit_begin_.push_back((int)units_);
@@ -520,12 +531,14 @@ namespace DiFfRG
                                                           slot.counters, arrivals, results, err);
         e = cudaGetLastError();
       }
+      // the read-back of results and error word (adjacent in the arena) right behind the kernel
+      if (e == cudaSuccess) e = cudaMemcpyAsync(pin, results, back_bytes, cudaMemcpyDeviceToHost, s);
       if (e != cudaSuccess) {
         cudaStreamSynchronize(s);
         gb_slot_release(qp_->ctx(), &slot);
         check_cuda(e, "integrator kernel launch");
       }
-      result_ = std::make_shared<LaunchResult>(keep_, slot, n * C, results, err, static_cast<double *>(pin));
+      result_ = std::make_shared<LaunchResult>(keep_, slot, n * C, results, err, static_cast<double *>(pin), true);
     }
 #endif // __CUDACC__
 
