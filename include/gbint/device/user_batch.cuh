@@ -93,6 +93,26 @@ namespace gbint
       ArgPack<T...> args;
     };
 
+    // The fields of a batch's entries that differ between its integrals -- bit 0 the maps and
+    // rules (Params), bit 1 + I KERNEL argument I.  Integral i's varying fields sit at
+    // rows + i * stride + off[field] (16-byte aligned); every other field is item 0's, which the
+    // kernel receives by value.  A grid of requests usually varies in one or two scalars (the
+    // external momentum), so a batch uploads a few bytes per integral instead of its whole
+    // entry (~1 KB with interpolator arguments).
+    constexpr int kMaxFields = 25;
+    struct Varying {
+      unsigned mask = 0;
+      unsigned stride = 0;
+      unsigned short off[kMaxFields] = {};
+    };
+    // host: call f(field, address, bytes) for the Params and every argument of an entry
+    template <typename ctype, class... T, class F, size_t... I>
+    void for_each_field(const Item<ctype, T...> &it, F &&f, std::index_sequence<I...>)
+    {
+      f(0, static_cast<const void *>(&it.P), sizeof(it.P));
+      (f((int)I + 1, static_cast<const void *>(&pget<(int)I>(it.args)), sizeof(pget<(int)I>(it.args))), ...);
+    }
+
     // interpolator arguments with device tables opt in with a member type gbint_stageable_table
     // and device_data(), table_bytes(), retarget(const void *) -- see gbint/interpolators.hh
     template <class A, class = void> struct is_stageable : std::false_type {
@@ -174,6 +194,21 @@ namespace gbint
     {
       (retarget_arg(pget<(int)I>(p), plan, sm), ...);
     }
+    // the varying arguments of one integral over item 0's
+    template <int I, class... T>
+    __device__ __forceinline__ void overlay_arg(ArgPack<T...> &a, const char *row, const Varying &v)
+    {
+      if ((v.mask >> (I + 1)) & 1u) {
+        auto &dst = pget<I>(a);
+        memcpy(static_cast<void *>(&dst), row + v.off[I + 1], sizeof(dst));
+      }
+    }
+    template <class... T, size_t... I>
+    __device__ __forceinline__ void overlay_args(ArgPack<T...> &a, const char *row, const Varying &v,
+                                                 std::index_sequence<I...>)
+    {
+      (overlay_arg<(int)I>(a, row, v), ...);
+    }
     template <class FAM, class KERNEL, typename NT, typename ctype, class... T, size_t... I>
     __device__ __forceinline__ NT eval_point(const gbint::fam::Params<ctype> &P, long long idx,
                                              const ArgPack<T...> &a, std::index_sequence<I...>)
@@ -182,16 +217,18 @@ namespace gbint
     }
 
     // Persistent batched kernel.  COMP: the result type's components (C scalar components of
-    // type S, get(v, c) on the device).  items == nullptr: one integral, `item0` (by value).
+    // type S, get(v, c) on the device).  Integral i is item0 (by value) with its varying fields
+    // read from rows (see Varying); rows == nullptr: every integral is item0.
     // unit_begin[i] .. unit_begin[i+1]: the units of integral i (unit_begin == nullptr: all of
     // item0's units).  partials: C doubles per unit; arrivals: one counter per integral (zeroed
     // before the launch and again by the finishing block); results: C doubles per integral.
     template <class FAM, class KERNEL, typename NT, typename ctype, class COMP, class... T>
     __global__ void __launch_bounds__(kThreads)
-        k_user_batch(const Item<ctype, T...> item0, const Item<ctype, T...> *items, const int *unit_begin, int n_items,
-                     int n_units, const StagePlan plan, double *partials, int *unit_counter, int *arrivals,
+        k_user_batch(const Item<ctype, T...> item0, const char *rows, const Varying var, const int *unit_begin,
+                     int n_items, int n_units, const StagePlan plan, double *partials, int *unit_counter, int *arrivals,
                      double *results, int *err)
     {
+      static_assert(sizeof...(T) + 1 <= kMaxFields, "integrator batch: at most 24 KERNEL arguments");
       constexpr int C = COMP::C;
       using S = typename COMP::S;
       extern __shared__ __align__(16) char stage[];
@@ -243,9 +280,13 @@ namespace gbint
           first = unit_begin[item];
           units_of = unit_begin[item + 1] - first;
         }
-        const Item<ctype, T...> &it = items ? items[item] : item0;
-        gbint::fam::Params<ctype> P = it.P;
-        ArgPack<T...> A = it.args;
+        gbint::fam::Params<ctype> P = item0.P;
+        ArgPack<T...> A = item0.args;
+        if (rows) {
+          const char *row = rows + (size_t)item * var.stride;
+          if (var.mask & 1u) memcpy(static_cast<void *>(&P), row + var.off[0], sizeof(P));
+          overlay_args(A, row, var, std::index_sequence_for<T...>{});
+        }
         if (staged) {
           retarget_params(P, plan, stage);
           retarget_args(A, plan, stage, std::index_sequence_for<T...>{});

@@ -469,15 +469,43 @@ namespace DiFfRG
       constexpr int C = TR::C;
       const int n = (int)items_.size();
       const int units = (int)units_;
-      // one slot arena, in doubles: partials | results | error word | arrivals | unit_begin | items
+      // the fields that differ between the integrals (the rest travel once, as item 0): compared
+      // bytewise against item 0, each varying field 16-byte aligned in a per-integral row
       static_assert(alignof(ItemT) <= 16, "integrator batch: argument types aligned beyond 16 bytes");
+      gbint::ub::Varying var{};
+      struct FieldAt {
+        size_t off, bytes;
+      };
+      std::array<FieldAt, gbint::ub::kMaxFields> fat{};
+      if (n > 1) {
+        const char *b0 = reinterpret_cast<const char *>(&items_.front());
+        gbint::ub::for_each_field(
+            items_.front(),
+            [&](int f, const void *p, size_t bytes) {
+              fat[f] = FieldAt{(size_t)(static_cast<const char *>(p) - b0), bytes};
+              for (int i = 1; i < n; ++i)
+                if (std::memcmp(reinterpret_cast<const char *>(&items_[i]) + fat[f].off, p, bytes) != 0) {
+                  var.mask |= 1u << f;
+                  break;
+                }
+            },
+            std::index_sequence_for<T...>{});
+        for (int f = 0; f < gbint::ub::kMaxFields; ++f)
+          if ((var.mask >> f) & 1u) {
+            var.off[f] = (unsigned short)var.stride;
+            var.stride += (unsigned)((fat[f].bytes + 15) / 16 * 16);
+          }
+        if (var.stride > 60000) throw std::runtime_error("integrator batch: varying arguments too large");
+      }
+      const bool rowed = n > 1 && var.mask != 0;
+      // one slot arena, in doubles: partials | results | error word | arrivals | unit_begin | rows
       const size_t d_part = (size_t)units * C, d_res = (size_t)n * C, d_err = 1;
       const size_t d_arr = ((size_t)n * sizeof(int) + 7) / 8;
       const size_t d_head = d_part + d_res + d_err + d_arr;
       const size_t ub_d = ((size_t)(n + 1) * sizeof(int) + 7) / 8;
-      // unit_begin padded so that the items start on a 16-byte boundary
+      // unit_begin padded so that the rows start on a 16-byte boundary
       const size_t d_ub = n > 1 ? ub_d + ((d_head + ub_d) & 1) : 0;
-      const size_t d_items = n > 1 ? (n * sizeof(ItemT) + 7) / 8 : 0;
+      const size_t d_items = rowed ? ((size_t)n * var.stride + 7) / 8 : 0;
       const size_t total = d_head + d_ub + d_items;
       if (total > (size_t)(1u << 30)) throw std::runtime_error("integrator batch: too large");
       gb_slot slot;
@@ -487,7 +515,7 @@ namespace DiFfRG
       int *err = reinterpret_cast<int *>(base + d_part + d_res);
       int *arrivals = reinterpret_cast<int *>(base + d_part + d_res + d_err);
       int *d_unit_begin = n > 1 ? reinterpret_cast<int *>(base + d_head) : nullptr;
-      ItemT *d_itemsp = n > 1 ? reinterpret_cast<ItemT *>(base + d_head + d_ub) : nullptr;
+      char *d_rows = rowed ? reinterpret_cast<char *>(base + d_head + d_ub) : nullptr;
       cudaStream_t s = (cudaStream_t)slot.stream;
       // pinned host staging of the slot: [read-back: C doubles per integral + error word | upload]
       const size_t up_bytes = (d_ub + d_items) * sizeof(double), back_bytes = (d_res + 1) * sizeof(double);
@@ -503,7 +531,15 @@ namespace DiFfRG
         int *ub = reinterpret_cast<int *>(up);
         std::memcpy(ub, unit_begin_.data(), n * sizeof(int));
         ub[n] = units;
-        std::memcpy(up + d_ub * sizeof(double), items_.data(), n * sizeof(ItemT));
+        if (rowed) {
+          char *rows = up + d_ub * sizeof(double);
+          for (int i = 0; i < n; ++i) {
+            const char *src = reinterpret_cast<const char *>(&items_[i]);
+            char *row = rows + (size_t)i * var.stride;
+            for (int f = 0; f < gbint::ub::kMaxFields; ++f)
+              if ((var.mask >> f) & 1u) std::memcpy(row + var.off[f], src + fat[f].off, fat[f].bytes);
+          }
+        }
         e = cudaMemcpyAsync(d_unit_begin, up, up_bytes, cudaMemcpyHostToDevice, s);
       }
       const gbint::ub::StagePlan pl = plan();
@@ -527,8 +563,8 @@ namespace DiFfRG
       }
       const int ctas = (int)std::min<long long>(units, (long long)qp_->num_sms() * per_sm);
       if (e == cudaSuccess) {
-        kern<<<ctas, gbint::ub::kThreads, pl.total, s>>>(items_.front(), d_itemsp, d_unit_begin, n, units, pl, partials,
-                                                          slot.counters, arrivals, results, err);
+        kern<<<ctas, gbint::ub::kThreads, pl.total, s>>>(items_.front(), d_rows, var, d_unit_begin, n, units, pl,
+                                                          partials, slot.counters, arrivals, results, err);
         e = cudaGetLastError();
       }
       // the read-back of results and error word (adjacent in the arena) right behind the kernel
