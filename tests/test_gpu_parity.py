@@ -180,6 +180,21 @@ def test_workload_fp32c_matches_oracle(ctx, oracle, W, name):
 
 
 @pytest.mark.parametrize("name", ["C1", "C2", "C3", "C5"])
+def test_whole_workload_fp32c_matches_oracle(ctx, oracle, W, name):
+    """Every integral of each benchmark workload (C3: all 4096 uneven 3D loops; C5: all 128
+    4.19M-point vertex loops), FP32-compensated, against the FP64 oracle on all host cores."""
+    import os
+
+    w = getattr(W, name.lower())()
+    got = run_engine(ctx, W, w, "fp32c")
+    ref = W.oracle_values(w, oracle, threads=os.cpu_count() or 1)
+    err = rel(got, ref)
+    print("%s all %d integrals: fp32c max rel err %.3e median %.3e" % (name, len(got), err.max(), np.median(err)))
+    assert np.all(np.isfinite(got))
+    assert err.max() <= TOL32[name]
+
+
+@pytest.mark.parametrize("name", ["C1", "C2", "C3", "C5"])
 def test_workload_fp32_fast_matches_oracle(ctx, oracle, W, name):
     w = subset(W, name)
     got = run_engine(ctx, W, w, "fp32f")
