@@ -1,8 +1,10 @@
 // user_batch.cuh -- the fused kernel of the C++ class templates: any number of integrals of one
 // user KERNEL (one family, one argument signature) in one persistent launch.
 //
-// Work units are (integral, 256 x 1..4 grid points, see ppt_for); CTAs take units from an
-// atomic counter.  Before its first unit a CTA stages the arrays every integral of the launch
+// Work units are (integral, 32 x 1..8 grid points, see ppt_for): one warp's.  CTAs are two
+// warps, and every warp takes units from an atomic counter on its own, so a batch of small
+// integrals spreads over the SMs in steps of two warps rather than of whole eight-warp CTAs.
+// Before its first unit a CTA stages the arrays every integral of the launch
 // reads -- the quadrature nodes and weights of each axis, the Matsubara rule, and the data of
 // the interpolator arguments (TexLinearInterpolator*, LinearInterpolator*) -- into shared memory
 // with non-tensor TMA bulk copies (cp.async.bulk ... mbarrier::complete_tx::bytes) and waits on
@@ -27,22 +29,32 @@ namespace gbint
 {
   namespace ub
   {
-    constexpr int kThreads = 256;
+    constexpr int kThreads = 64;          // CTA size: two warps, each an independent worker
+#ifndef GBINT_UB_MIN_CTAS
+#define GBINT_UB_MIN_CTAS 8
+#endif
+    // resident CTAs per SM the register allocation is held to: 8 (16 warps, <= 128 registers
+    // a thread) keeps the FP64 pipe of GB300 busy for the generated KERNELs; a translation
+    // unit whose KERNEL spills heavily at 128 may define GBINT_UB_MIN_CTAS 6 (<= 168) first
+    constexpr int kMinCtas = GBINT_UB_MIN_CTAS;
+    constexpr int kUnitLanes = 32;        // a work unit is one warp's
     constexpr int kMaxStage = 24;         // staged arrays per launch
     constexpr unsigned kStageAlign = 16;  // TMA bulk copies: 16-byte addresses and sizes
     enum : int { ERR_STAGE_TIMEOUT = 1, ERR_STAGE_ALIGN = 2 };
 
-    // Points per thread of an integral's work units, from the integral's own size only -- so its
+    // Points per lane of an integral's work units, from the integral's own size only -- so its
     // unit decomposition, and with it the rounding of its result, is the same alone and in any
-    // batch: integrals of a few thousand points (the reference examples' 32 x 16 angle grids)
-    // spread one point per thread over more CTAs, large ones take four.
+    // batch.  A unit is one warp's (32 x ppt points): the reference examples' 512-point angle
+    // grids give 16 units each, which the warps of the whole GPU pull one at a time, so no SM
+    // ends up with a whole extra CTA's share; larger integrals take 2, 4 and 8 points per lane,
+    // which keeps the per-unit work (claim, descriptor, reduction) small against the points.
     __host__ __device__ constexpr int ppt_for(long long n_points)
     {
-      return n_points <= 16384 ? 1 : (n_points <= 131072 ? 2 : 4);
+      return n_points <= 1024 ? 1 : (n_points <= 8192 ? 2 : (n_points <= 65536 ? 4 : 8));
     }
     __host__ __device__ constexpr long long unit_points(long long n_points)
     {
-      return (long long)kThreads * ppt_for(n_points);
+      return (long long)kUnitLanes * ppt_for(n_points);
     }
 
     // ------------------------------------------------------------------ argument packs
@@ -221,22 +233,20 @@ namespace gbint
     // read from rows (see Varying); rows == nullptr: every integral is item0.
     // unit_begin[i] .. unit_begin[i+1]: the units of integral i (unit_begin == nullptr: all of
     // item0's units).  partials: C doubles per unit; arrivals: one counter per integral (zeroed
-    // before the launch and again by the finishing block); results: C doubles per integral.
+    // before the launch and again by the finishing warp); results: C doubles per integral.
     template <class FAM, class KERNEL, typename NT, typename ctype, class COMP, class... T>
-    __global__ void __launch_bounds__(kThreads)
+    __global__ void __launch_bounds__(kThreads, kMinCtas)
         k_user_batch(const Item<ctype, T...> item0, const char *rows, const Varying var, const int *unit_begin,
-                     int n_items, int n_units, const StagePlan plan, double *partials, int *unit_counter, int *arrivals,
+                     int units_per_item, int n_items, int n_units, const StagePlan plan, double *partials, int *unit_counter, int *arrivals,
                      double *results, int *err)
     {
       static_assert(sizeof...(T) + 1 <= kMaxFields, "integrator batch: at most 24 KERNEL arguments");
       constexpr int C = COMP::C;
       using S = typename COMP::S;
       extern __shared__ __align__(16) char stage[];
-      __shared__ double red[C][32];
-      __shared__ int s_unit, s_last;
       __shared__ __align__(8) uint64_t bar;
       __shared__ int s_staged;
-      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+      const int lane = threadIdx.x & 31;
 
       // stage the launch's shared arrays once per CTA
       if (threadIdx.x == 0) {
@@ -260,25 +270,31 @@ namespace gbint
         staged = __syncthreads_and(staged ? 1 : 0) != 0;
       }
 
+      // every warp pulls units on its own: claim, evaluate, reduce, and finish the integral when
+      // its unit is the last to arrive
       for (;;) {
-        if (threadIdx.x == 0) s_unit = atomicAdd(unit_counter, 1);
-        __syncthreads();
-        const int u = s_unit;
+        int u = 0;
+        if (lane == 0) u = atomicAdd(unit_counter, 1);
+        u = __shfl_sync(0xffffffffu, u, 0);
         if (u >= n_units) break;
-        // the unit's integral: unit_begin is sorted, binary search (uniform across the CTA)
+        // the unit's integral: unit_begin is sorted, binary search (uniform across the warp)
         int item = 0, first = 0, units_of = n_units;
-        if (unit_begin) {
+        if (units_per_item > 0) {  // every integral has the same number of units
+          item = u / units_per_item;
+          first = item * units_per_item;
+          units_of = units_per_item;
+        } else if (unit_begin) {
           int lo = 0, hi = n_items - 1;
           while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (unit_begin[mid] <= u)
+            if (__ldg(&unit_begin[mid]) <= u)
               lo = mid;
             else
               hi = mid - 1;
           }
           item = lo;
-          first = unit_begin[item];
-          units_of = unit_begin[item + 1] - first;
+          first = __ldg(&unit_begin[item]);
+          units_of = __ldg(&unit_begin[item + 1]) - first;
         }
         gbint::fam::Params<ctype> P = item0.P;
         ArgPack<T...> A = item0.args;
@@ -293,7 +309,7 @@ namespace gbint
         }
         const long long n_points = FAM::points(P);
         const int ppt = ppt_for(n_points);
-        const long long begin = (long long)(u - first) * kThreads * ppt;
+        const long long begin = (long long)(u - first) * kUnitLanes * ppt;
         double acc[C];
         if constexpr (std::is_same_v<S, float>) {
           float s[C], c[C];  // Kahan per component
@@ -301,7 +317,7 @@ namespace gbint
           for (int m = 0; m < C; ++m) s[m] = c[m] = 0.f;
 #pragma unroll 1
           for (int k = 0; k < ppt; ++k) {
-            const long long idx = begin + threadIdx.x + k * kThreads;
+            const long long idx = begin + lane + k * kUnitLanes;
             if (idx < n_points) {
               const NT v = eval_point<FAM, KERNEL, NT>(P, idx, A, std::index_sequence_for<T...>{});
 #pragma unroll
@@ -320,7 +336,7 @@ namespace gbint
           for (int m = 0; m < C; ++m) acc[m] = 0.0;
 #pragma unroll 1
           for (int k = 0; k < ppt; ++k) {
-            const long long idx = begin + threadIdx.x + k * kThreads;
+            const long long idx = begin + lane + k * kUnitLanes;
             if (idx < n_points) {
               const NT v = eval_point<FAM, KERNEL, NT>(P, idx, A, std::index_sequence_for<T...>{});
 #pragma unroll
@@ -329,47 +345,30 @@ namespace gbint
           }
         }
 #pragma unroll
-        for (int m = 0; m < C; ++m) {
-          acc[m] = warp_sum(acc[m]);
-          if (lane == 0) red[m][wid] = acc[m];
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
+        for (int m = 0; m < C; ++m) acc[m] = warp_sum(acc[m]);
+        int last = 0;
+        if (lane == 0) {
 #pragma unroll
-          for (int m = 0; m < C; ++m) {
-            double s = 0;
-            for (int i = 0; i < kThreads / 32; ++i) s += red[m][i];
-            partials[(size_t)u * C + m] = s;
-          }
+          for (int m = 0; m < C; ++m) partials[(size_t)u * C + m] = acc[m];
           __threadfence();
-          s_last = (atomicAdd(&arrivals[item], 1) == units_of - 1);
+          last = (atomicAdd(&arrivals[item], 1) == units_of - 1);
         }
-        __syncthreads();
-        if (s_last) {  // the integral's unit partials in unit order, with the whole block
+        if (__shfl_sync(0xffffffffu, last, 0)) {  // the integral's unit partials in unit order
           __threadfence();
           double v[C];
 #pragma unroll
           for (int m = 0; m < C; ++m) v[m] = 0.0;
-          for (int i = threadIdx.x; i < units_of; i += kThreads)
+          for (int i = lane; i < units_of; i += kUnitLanes)
 #pragma unroll
             for (int m = 0; m < C; ++m) v[m] += __ldcg(&partials[(size_t)(first + i) * C + m]);
 #pragma unroll
-          for (int m = 0; m < C; ++m) {
-            v[m] = warp_sum(v[m]);
-            if (lane == 0) red[m][wid] = v[m];
-          }
-          __syncthreads();
-          if (threadIdx.x == 0) {
+          for (int m = 0; m < C; ++m) v[m] = warp_sum(v[m]);
+          if (lane == 0) {
 #pragma unroll
-            for (int m = 0; m < C; ++m) {
-              double s = 0;
-              for (int i = 0; i < kThreads / 32; ++i) s += red[m][i];
-              results[(size_t)item * C + m] = s;
-            }
+            for (int m = 0; m < C; ++m) results[(size_t)item * C + m] = v[m];
             arrivals[item] = 0;
           }
         }
-        __syncthreads();
       }
       // a staging wait that gave up: wait (bounded again) for the copies still in flight before
       // the CTA's shared memory is released

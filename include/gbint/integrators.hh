@@ -355,13 +355,15 @@ namespace DiFfRG
       virtual void launch() = 0;
       virtual size_t size() const = 0;
       virtual bool launched() const = 0;
+      // still taking requests: not launched and below the batch size limit (one lock)
+      virtual bool accepting() const = 0;
     };
 
     template <class FAM, class KERNEL, typename NT, typename ctype, class... T> class UserBatch : public BatchBase
     {
     public:
       using ItemT = gbint::ub::Item<ctype, T...>;
-      UserBatch(QuadratureProvider &qp, std::shared_ptr<gb_ctx> keep) : qp_(&qp), keep_(std::move(keep)) {}
+      UserBatch(QuadratureProvider &qp, const std::shared_ptr<gb_ctx> &keep) : qp_(&qp), keep_(keep) {}
 
       int add(const gbint::fam::Params<ctype> &P, const T &...t)
       {
@@ -394,12 +396,27 @@ namespace DiFfRG
         std::lock_guard<std::mutex> lk(mu_);
         return launched_;
       }
+      bool accepting() const override
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        return !launched_ && items_.size() < (size_t)kMaxBatchItems;
+      }
       void launch() override;
       // the launch's results (launching the batch first if nobody has)
       std::shared_ptr<LaunchResult> result()
       {
         launch();
         return result_;
+      }
+      // the host values of the launch, C doubles per integral; after the first call a lock-free
+      // read (the futures of a grid read them one after another)
+      const double *values()
+      {
+        if (const double *v = values_.load(std::memory_order_acquire)) return v;
+        launch();
+        const double *v = result_->wait();
+        values_.store(v, std::memory_order_release);
+        return v;
       }
 
     private:
@@ -455,6 +472,7 @@ namespace DiFfRG
       mutable std::mutex mu_;
       bool launched_ = false;
       std::shared_ptr<LaunchResult> result_;
+      std::atomic<const double *> values_{nullptr};
     };
 
 #ifdef __CUDACC__
@@ -517,22 +535,29 @@ namespace DiFfRG
       int *d_unit_begin = n > 1 ? reinterpret_cast<int *>(base + d_head) : nullptr;
       char *d_rows = rowed ? reinterpret_cast<char *>(base + d_head + d_ub) : nullptr;
       cudaStream_t s = (cudaStream_t)slot.stream;
-      // pinned host staging of the slot: [read-back: C doubles per integral + error word | upload]
-      const size_t up_bytes = (d_ub + d_items) * sizeof(double), back_bytes = (d_res + 1) * sizeof(double);
+      // pinned host staging of the slot: [read-back: C doubles per integral + error word | upload:
+      // zeroed error word and arrivals, unit_begin, rows] -- error word to rows are adjacent in the
+      // arena, so one copy clears the counters and uploads the batch
+      const size_t d_zero = d_err + d_arr;
+      const size_t up_bytes = n > 1 ? (d_zero + d_ub + d_items) * sizeof(double) : 0;
+      const size_t back_bytes = (d_res + 1) * sizeof(double);
       void *pin = nullptr;
       const int rc = gb_slot_host(qp_->ctx(), &slot, back_bytes + up_bytes, &pin);
       if (rc != GB_OK) {
         gb_slot_release(qp_->ctx(), &slot);
         check(qp_->ctx(), rc, "gb_slot_host");
       }
-      cudaError_t e = cudaMemsetAsync(err, 0, (d_err + d_arr) * sizeof(double), s);
-      if (n > 1 && e == cudaSuccess) {
+      cudaError_t e = cudaSuccess;
+      if (n == 1) {
+        e = cudaMemsetAsync(err, 0, d_zero * sizeof(double), s);
+      } else {
         char *up = static_cast<char *>(pin) + back_bytes;
-        int *ub = reinterpret_cast<int *>(up);
+        std::memset(up, 0, d_zero * sizeof(double));
+        int *ub = reinterpret_cast<int *>(up + d_zero * sizeof(double));
         std::memcpy(ub, unit_begin_.data(), n * sizeof(int));
         ub[n] = units;
         if (rowed) {
-          char *rows = up + d_ub * sizeof(double);
+          char *rows = up + (d_zero + d_ub) * sizeof(double);
           for (int i = 0; i < n; ++i) {
             const char *src = reinterpret_cast<const char *>(&items_[i]);
             char *row = rows + (size_t)i * var.stride;
@@ -540,11 +565,12 @@ namespace DiFfRG
               if ((var.mask >> f) & 1u) std::memcpy(row + var.off[f], src + fat[f].off, fat[f].bytes);
           }
         }
-        e = cudaMemcpyAsync(d_unit_begin, up, up_bytes, cudaMemcpyHostToDevice, s);
+        e = cudaMemcpyAsync(err, up, up_bytes, cudaMemcpyHostToDevice, s);
       }
       const gbint::ub::StagePlan pl = plan();
-      // persistent grid: as many CTAs as fit on the GPU at once (each stages the shared arrays);
-      // the occupancy per staging size is looked up once per kernel type
+      // persistent grid: a warp per unit, up to as many CTAs as fit on the GPU at once (each
+      // stages the shared arrays); the occupancy per staging size is looked up once per kernel
+      // type
       auto kern = gbint::ub::k_user_batch<FAM, KERNEL, NT, ctype, TR, T...>;
       static std::mutex occ_mu;
       static std::map<unsigned, int> occ;
@@ -561,9 +587,14 @@ namespace DiFfRG
           occ[pl.total] = per_sm;
         }
       }
-      const int ctas = (int)std::min<long long>(units, (long long)qp_->num_sms() * per_sm);
+      const int per_cta = gbint::ub::kThreads / gbint::ub::kUnitLanes;
+      // a grid of equal quadratures: the kernel finds a unit's integral by division
+      int upi = units % n == 0 ? units / n : 0;
+      for (int i = 1; i < n && upi > 0; ++i)
+        if (unit_begin_[i] != i * upi) upi = 0;
+      const int ctas = (int)std::min<long long>((units + per_cta - 1) / per_cta, (long long)qp_->num_sms() * per_sm);
       if (e == cudaSuccess) {
-        kern<<<ctas, gbint::ub::kThreads, pl.total, s>>>(items_.front(), d_rows, var, d_unit_begin, n, units, pl,
+        kern<<<ctas, gbint::ub::kThreads, pl.total, s>>>(items_.front(), d_rows, var, d_unit_begin, upi, n, units, pl,
                                                           partials, slot.counters, arrivals, results, err);
         e = cudaGetLastError();
       }
@@ -581,8 +612,8 @@ namespace DiFfRG
     // the future of integral `idx` of a batch: constant + its components
     template <typename NT, class B> std::future<NT> batch_future(std::shared_ptr<B> b, int idx, NT constant)
     {
-      return std::async(std::launch::deferred, [b, idx, constant]() {
-        const double *v = b->result()->wait() + (size_t)idx * nt_traits<NT>::C;
+      return std::async(std::launch::deferred, [b = std::move(b), idx, constant]() {
+        const double *v = b->values() + (size_t)idx * nt_traits<NT>::C;
         return constant + nt_traits<NT>::make(v);
       });
     }
@@ -631,7 +662,7 @@ namespace DiFfRG
     }
 
     // the open batch of type B for the provider's context
-    template <class B> std::shared_ptr<B> batch(QuadratureProvider &qp, std::shared_ptr<gb_ctx> keep)
+    template <class B> std::shared_ptr<B> batch(QuadratureProvider &qp, const std::shared_ptr<gb_ctx> &keep)
     {
       // key: the provider's context and a per-batch-type tag address (pointer comparisons only;
       // comparing the types' long mangled names would cost more than the request itself)
@@ -639,13 +670,13 @@ namespace DiFfRG
       const auto key = std::make_pair((const void *)qp.ctx(), (const void *)&tag);
       auto it = open_.find(key);
       // a batch that is full, or that a future's get() already launched, is closed
-      if (it != open_.end() && (it->second->launched() || it->second->size() >= (size_t)gbint_detail::kMaxBatchItems)) {
+      if (it != open_.end() && !it->second->accepting()) {
         it->second->launch();
         open_.erase(it);
         it = open_.end();
       }
       if (it == open_.end()) {
-        auto b = std::make_shared<B>(qp, std::move(keep));
+        auto b = std::make_shared<B>(qp, keep);
         order_.push_back(b);
         it = open_.emplace(key, b).first;
       }
@@ -662,19 +693,19 @@ namespace DiFfRG
   {
     // one request: into the thread's open RequestBatch if there is one, else launched at once
     template <class FAM, class KERNEL, typename NT, typename ctype, class... T>
-    std::future<NT> submit(QuadratureProvider &qp, std::shared_ptr<gb_ctx> keep, const gbint::fam::Params<ctype> &P,
+    std::future<NT> submit(QuadratureProvider &qp, const std::shared_ptr<gb_ctx> &keep, const gbint::fam::Params<ctype> &P,
                            NT constant, const T &...t)
     {
       using B = UserBatch<FAM, KERNEL, NT, ctype, T...>;
       if (RequestBatch *scope = tl_request_scope_ptr()) {
-        auto b = scope->template batch<B>(qp, std::move(keep));
+        auto b = scope->template batch<B>(qp, keep);
         const int idx = b->add(P, t...);
-        return batch_future<NT>(b, idx, constant);
+        return batch_future<NT>(std::move(b), idx, constant);
       }
-      auto b = std::make_shared<B>(qp, std::move(keep));
+      auto b = std::make_shared<B>(qp, keep);
       const int idx = b->add(P, t...);
       b->launch();
-      return batch_future<NT>(b, idx, constant);
+      return batch_future<NT>(std::move(b), idx, constant);
     }
   } // namespace gbint_detail
 
@@ -702,7 +733,7 @@ namespace DiFfRG
         gbint::fam::Params<ctype> P = P_;
         P.k = k;
         const NT c = (NT)KERNEL::constant(k, t...);
-        return submit<FAM, KERNEL, NT, ctype>(*qp_, keep(), P, c, t...);
+        return submit<FAM, KERNEL, NT, ctype>(*qp_, qp_->ctx_shared(), P, c, t...);
       }
 
     protected:
@@ -712,7 +743,6 @@ namespace DiFfRG
         P_.x[a] = qp_->get_device_points<ctype>(n);
         P_.w[a] = qp_->get_device_weights<ctype>(n);
       }
-      std::shared_ptr<gb_ctx> keep() const { return qp_->ctx_shared(); }
 
       QuadratureProvider *qp_;
       std::array<uint, NAX> grid_sizes_;
