@@ -614,8 +614,8 @@ namespace gbint
     const int jspan = std::min(it.ax[1].n, (rpu - 1) / it.ax[0].n + 2);
     return it.ax[2].n + it.ax[3].n + (jspan * ns0 + 1) / 2;  // NodeRec units (32 B = 2 slice entries)
   }
-  // S3R: whether tables B, C, D carry cell records and B its regulator coefficients, and the
-  // bytes staged (B's coefficients, then each table's records and difference low words)
+  // S3R: whether table B carries propagator records and C, D value records, and the bytes
+  // staged (B's propagator records, then C's and D's value records and difference low words)
   bool s3r_ready(const gb_ctx *ctx, const ItemDev &it)
   {
     for (int t = 1; t < 4; ++t) {
@@ -623,12 +623,12 @@ namespace gbint
       const TableDev &D = ctx->h_dir[it.tab[t]];
       if (!D.cr_off || D.n1 != 0) return false;
     }
-    return ctx->h_dir[it.tab[1]].rq_off > 0;
+    return ctx->h_dir[it.tab[1]].gr_off > 0;
   }
   int s3r_tab_bytes(const gb_ctx *ctx, const ItemDev &it)
   {
-    int b = 48 * (ctx->h_dir[it.tab[1]].n0 - 1);
-    for (int t = 1; t < 4; ++t) {
+    int b = 64 * (ctx->h_dir[it.tab[1]].n0 - 1);
+    for (int t = 2; t < 4; ++t) {
       const int c = ctx->h_dir[it.tab[t]].n0 - 1;
       b += 16 * c + (4 * c + 15) / 16 * 16;
     }
@@ -1438,6 +1438,30 @@ namespace gbint
     }
     return out;
   }
+  // the same expansion through t^9 in FP64 (10 a cell): the propagator records are built from it
+  std::vector<double> regulator_cell_coeffs64(const dev::AxisDev &ax)
+  {
+    const int nc = ax.n - 1;
+    std::vector<double> out(10 * (size_t)nc, 0.0);
+    for (int j = 0; j < nc; ++j) {
+      const long double l2c = ((long double)j + 0.5L - (long double)ax.shift64) / (long double)ax.scale64;
+      const long double c = exp2l(l2c);
+      long double d[10], a[10];
+      d[0] = expm1l(c);
+      long double pw = 1.0L;
+      for (int k = 1; k < 10; ++k) {
+        pw *= c / k;
+        d[k] = expl(c) * pw;
+      }
+      for (int k = 0; k < 10; ++k) {
+        long double nk = k < 2 ? c : 0.0L;
+        for (int i = 0; i < k; ++i) nk -= a[i] * d[k - i];
+        a[k] = nk / d[0];
+        out[10 * (size_t)j + k] = (double)a[k];
+      }
+    }
+    return out;
+  }
 } // namespace gbint
 
 int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
@@ -1494,12 +1518,18 @@ int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
   const bool with_rq = rc_axis >= 0 && (rc_axis == 0 ? ax0 : ax1).scale64 >= kMinScaleSq;
   const std::vector<float> rq = with_rq ? regulator_cell_coeffs(rc_axis == 0 ? ax0 : ax1) : std::vector<float>{};
   // 1D tables with reciprocals also carry per-cell records (built from the data on every update):
-  // a lookup reads the cell's reciprocal, value and difference with one 16-byte load
+  // a value lookup reads the cell's reciprocal, value and difference with one 16-byte load; with
+  // the regulator, a propagator lookup reads the cell's series of 1 / (Z(x) x + R(x)) with four
+  // (the FP64 regulator coefficients they are built from sit behind them)
   const int cells = spec->n0 - 1;
   const bool with_cr = rc_axis == 0 && spec->n1 == 0;
+  const bool with_gr = with_cr && with_rq;
+  const std::vector<double> rd = with_gr ? regulator_cell_coeffs64(ax0) : std::vector<double>{};
   const size_t cr_bytes = with_cr ? (size_t)cells * 16 + ((size_t)cells * 4 + 15) / 16 * 16 : 0;
+  const size_t gr_bytes = with_gr ? (size_t)cells * 64 : 0;
   const size_t cr_at = (size_t)t->bytes + rq.size() * 4;  // 16-byte multiple
-  const size_t alloc = cr_at + cr_bytes;
+  const size_t gr_at = cr_at + cr_bytes, rd_at = gr_at + gr_bytes;
+  const size_t alloc = rd_at + rd.size() * 8;
   GB_CUDA(cudaSetDevice(ctx->device));
   GB_CUDA(cudaMalloc(&t->buf[0], alloc));
   GB_CUDA(cudaMalloc(&t->buf[1], alloc));
@@ -1511,6 +1541,9 @@ int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
                          cudaMemcpyHostToDevice));
     if (!rq.empty())
       GB_CUDA(cudaMemcpy(reinterpret_cast<char *>(t->buf[b]) + t->bytes, rq.data(), rq.size() * 4,
+                         cudaMemcpyHostToDevice));
+    if (!rd.empty())
+      GB_CUDA(cudaMemcpy(reinterpret_cast<char *>(t->buf[b]) + rd_at, rd.data(), rd.size() * 8,
                          cudaMemcpyHostToDevice));
   }
   TableDev &D = ctx->h_dir[slot];
@@ -1524,11 +1557,15 @@ int gb_table_create(gb_ctx *ctx, const gb_table_spec *spec, gb_table **out)
   D.rc_axis = std::max(rc_axis, 0);
   D.rc_sq = rc_axis >= 0 && (rc_axis == 0 ? ax0 : ax1).scale64 >= kMinScaleSq;
   D.cr_off = with_cr ? (int)(cr_at / 4) : 0;
+  D.gr_off = with_gr ? (int)(gr_at / 4) : 0;
+  D.rd_off = with_gr ? (int)(rd_at / 4) : 0;
+  D.e_lo = std::expm1(-std::log(2.0) / (2.0 * ax0.scale64));
+  D.e_hi = std::expm1(std::log(2.0) / (2.0 * ax0.scale64));
   D.a0 = ax0;
   D.a1 = ax1;
   if (with_cr) {
     for (int b = 0; b < 2; ++b)
-      GB_CUDA(launch_cell_records(static_cast<float *>(t->buf[b]), D.rc_off, D.cr_off, cells, ctx->stream));
+      GB_CUDA(launch_cell_records(static_cast<float *>(t->buf[b]), D, ctx->stream));
     GB_CUDA(cudaStreamSynchronize(ctx->stream));
   }
   GB_CUDA(cudaMemcpy(ctx->d_dir + slot, &D, sizeof(TableDev), cudaMemcpyHostToDevice));
@@ -1562,8 +1599,7 @@ static int table_update_impl(gb_ctx *ctx, gb_table *t, const float *src, cudaMem
   }
   GB_CUDA(cudaMemcpyAsync(t->buf[back], src, (size_t)t->elems * 4, kind, s));
   if (ctx->h_dir[t->slot].cr_off)
-    GB_CUDA(launch_cell_records(static_cast<float *>(t->buf[back]), ctx->h_dir[t->slot].rc_off,
-                                ctx->h_dir[t->slot].cr_off, t->spec.n0 - 1, s));
+    GB_CUDA(launch_cell_records(static_cast<float *>(t->buf[back]), ctx->h_dir[t->slot], s));
   // publish the new buffer in the directory, ordered after the data on the same stream (the
   // host copy of the entry changes only once the device write is enqueued)
   TableDev D = ctx->h_dir[t->slot];
@@ -1638,8 +1674,7 @@ int gb_table_update_many(gb_ctx *ctx, int n, gb_table *const *tables, const floa
     const int back = t->front ^ 1;
     GB_CUDA(cudaMemcpyAsync(t->buf[back], host_data[i], (size_t)t->elems * 4, cudaMemcpyHostToDevice, s));
     if (ctx->h_dir[t->slot].cr_off)
-      GB_CUDA(launch_cell_records(static_cast<float *>(t->buf[back]), ctx->h_dir[t->slot].rc_off,
-                                  ctx->h_dir[t->slot].cr_off, t->spec.n0 - 1, s));
+      GB_CUDA(launch_cell_records(static_cast<float *>(t->buf[back]), ctx->h_dir[t->slot], s));
     dir[i] = ctx->h_dir[t->slot];
     dir[i].data = t->buf[back];
   }

@@ -94,9 +94,18 @@ namespace gbint
     int rc_axis;  // the log axis they belong to (cells at most 25 % wide)
     int rc_sq;    // 1: cells at most 12 % wide, so the reciprocals also serve a squared coordinate
     int rq_off;   // float offset of the regulator's per-cell Taylor coefficients (global only); 0: none
-    int cr_off;   // float offset of the per-cell records (1D log tables with reciprocals; 0: none):
-                  // float4 {1/c_j hi, 1/c_j lo, y_j, hi(y_{j+1} - y_j)} per cell, then per cell the
-                  // low word of the difference (y_{j+1} - y_j = hi + lo exactly), rebuilt on update
+    int cr_off;   // float offset of the per-cell value records (1D log tables with reciprocals; 0:
+                  // none): float4 {1/c_j hi, 1/c_j lo, y_j, hi(y_{j+1} - y_j)} per cell, then per
+                  // cell the low word of the difference (y_{j+1} - y_j = hi + lo exactly), rebuilt
+                  // on update
+    int gr_off;   // float offset of the per-cell propagator records (with rq_off; 0: none), four
+                  // float4 arrays of a float4 per cell, rebuilt on update: {1/c_j hi, lo, g0 hi, lo}, {g1 hi, lo, g2 hi,
+                  // lo}, {g3, g4, g5, g6}, {g7, g8, el, +-eh} -- 1 / (Z(x) x + R(x)) = sum g_k t^k
+                  // through t^8, t = x / c_j - 1; (el, eh) the cell's edges in t moved inwards by
+                  // 4e-7; eh < 0: the series was not trusted over the cell
+    int rd_off;   // float offset of the regulator's per-cell Taylor coefficients in FP64 (10 a
+                  // cell; with gr_off), read only when the records are built
+    double e_lo, e_hi;  // with cr_off: the edges of every cell in t = x / c_j - 1, 2^(-+1/(2 scale)) - 1
     dev::AxisDev a0, a1;
   };
 

@@ -19,8 +19,9 @@ namespace gbint
                          cudaStream_t s);
   // writes the UnitDev records of n integrals' unit ranges, in stream order
   cudaError_t launch_expand_units(const ExpandDev *ex, int n, UnitDev *units, cudaStream_t s);
-  // rebuilds a 1D table's per-cell records (TableDev::cr_off) from its data, in stream order
-  cudaError_t launch_cell_records(float *table, int rc_off, int cr_off, int cells, cudaStream_t s);
+  // rebuilds a 1D table's per-cell records (TableDev::cr_off, gr_off) from its data (table, laid
+  // out as D describes), in stream order
+  cudaError_t launch_cell_records(float *table, const TableDev &D, cudaStream_t s);
   // writes one table directory entry in stream order (the entry travels as a kernel parameter)
   cudaError_t launch_dir_set(TableDev *dst, const TableDev &v, cudaStream_t s);
   // writes n directory entries dir[slot[i]] = v[i] in stream order (chunks travel as parameters)

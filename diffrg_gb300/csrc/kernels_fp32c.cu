@@ -390,9 +390,9 @@ namespace gbint
 
     // bytes of a table's cell-centre reciprocals (staged at the end of its data; 16-byte multiple)
     __device__ __forceinline__ int rc_bytes(const TableDev &T) { return T.rc_off ? T.bytes - 4 * T.rc_off : 0; }
-    // S3R staging: a 1D table's regulator coefficients (48 bytes a cell) and its cell records
+    // S3R staging: a 1D table's propagator records (64 bytes a cell) and its value records
     // (16 bytes a cell, then the difference low words padded to 16 bytes)
-    __device__ __forceinline__ int s3r_rq_bytes(const TableDev &T) { return 48 * (T.n0 - 1); }
+    __device__ __forceinline__ int s3r_g_bytes(const TableDev &T) { return 64 * (T.n0 - 1); }
     __device__ __forceinline__ int s3r_rec_bytes(const TableDev &T)
     {
       return 16 * (T.n0 - 1) + (4 * (T.n0 - 1) + 15) / 16 * 16;
@@ -728,11 +728,13 @@ namespace gbint
     // ---------------------------------------------------------------- S3R: S3 through cell records
     // The accurate S3 with its three point-dependent tables (B at r2 = |q-p|^2, C at
     // s = (q^2 + p^2 + r2)/3, D at t2 = |q-p/2|^2) read through per-cell records staged in shared
-    // memory: one 16-byte load gives a cell's reciprocal, value and difference (split exactly
-    // into two floats, so the lerp needs no two_sum of the endpoints), and B's regulator
-    // coefficients are staged beside them instead of read through L1.  t2 follows from r2
-    // (t2 = r2/2 + q^2/2 - P^2/4).  Staged layout (floats): [0] B's regulator coefficients,
-    // toff[t] for t = 1..3: the records of table t, then its difference low words.
+    // memory.  C's and D's value records: one 16-byte load gives a cell's reciprocal, value and
+    // difference (split exactly into two floats, so the lerp needs no two_sum of the endpoints).
+    // B's propagator records: 1 / (Z(x) x + R(x)) as the cell's series sum g_k t^k, t = x / c_j - 1,
+    // through t^8 (k_cell_records) -- no fraction, lerp, regulator or reciprocal for B per point.
+    // t2 follows from r2 (t2 = r2/2 + q^2/2 - P^2/4).  Staged layout (floats): toff[1] B's
+    // propagator records (16 a cell), toff[2], toff[3] the value records of C and D, then their
+    // difference low words.
     struct RecTab {
       const float4 *rec;
       const float *dlo;
@@ -795,15 +797,6 @@ namespace gbint
       const df s = two_sum(r.z, p.hi);
       return df{s.hi, __fadd_rn(s.lo, __fmaf_rn(f, dlo, p.lo))};
     }
-    template <int DEG> __device__ __forceinline__ df G1_rec(const RecTab &T, const float4 *rq, const AxisDev &a, df x)
-    {
-      int j, jt;
-      float4 r;
-      df t;
-      const float f = rec_cell_frac<DEG>(a, T, x, j, r, jt, t);
-      const df R = jt >= 0 ? reg_R_cell<true>(rq, jt, t) : reg_R_df(x);
-      return df_prop(rec_lerp_u(r, T.dlo[j], f), x, R);
-    }
     template <int DEG> __device__ __forceinline__ df V1_rec(const RecTab &T, const AxisDev &a, df x)
     {
       int j, jt;
@@ -811,6 +804,74 @@ namespace gbint
       df t;
       const float f = rec_cell_frac<DEG>(a, T, x, j, r, jt, t);
       return rec_lerp_u(r, T.dlo[j], f);
+    }
+    // t = x rr - 1 as a normalised double-float: fl(x.hi rr.hi) - 1 is exact (see cell_frac_rr),
+    // the product's rounding error and cross terms (~1e-7) join it by fast_two_sum, so that the
+    // low word left for the series' first-order terms is ~1e-9
+    __device__ __forceinline__ df rec_t(df x, float rh, float rl)
+    {
+      const float ph = __fmul_rn(x.hi, rh);
+      const float th = __fsub_rn(ph, 1.0f);
+      return fast_two_sum(th, __fadd_rn(__fmaf_rn(x.hi, rh, -ph), __fmaf_rn(x.hi, rl, __fmul_rn(x.lo, rh))));
+    }
+    // 1 / (Z(x) x + R(x)) on B from its propagator records G (four float4 arrays of n - 1 cells:
+    // {1/c_j hi, lo, g0 hi, lo}, {g1 hi, lo, g2 hi, lo}, {g3, g4, g5, g6}, {g7, g8, el, +-eh}).  The fast log2
+    // that picks cell j is off by up to ~3e-5 of a cell, so a t beyond the cell's edges moved in
+    // by 4e-7 (el, eh) is placed exactly (FP64 against the table's edges e_lo, e_hi).  Outside
+    // the table, or in a cell whose series is not trusted (eh < 0), the value records, the
+    // regulator expansion and a reciprocal from global memory (TBg, rqg) give the propagator.
+    template <int DEG>
+    __device__ __forceinline__ df G1_grec(const float4 *G, const TableDev &T, const RecTab &TBg, const float4 *rqg,
+                                          df x)
+    {
+      const AxisDev &a = T.a0;
+      const int n = a.n;
+      const float ua = __fmaf_rn(a.scale.hi, __log2f(x.hi), a.shift.hi);
+      if (ua >= 0.f && ua <= (float)(n - 1)) {
+        const int nc = n - 1;
+        int j = min((int)ua, n - 2);
+        float4 c0 = G[j], c3 = G[3 * nc + j];
+        df t = rec_t(x, c0.x, c0.y);
+        bool in = true;
+        if (t.hi <= c3.z || t.hi >= fabsf(c3.w)) {
+          const double td = (double)t.hi + (double)t.lo;
+          const int jn = td > T.e_hi ? j + 1 : (td < T.e_lo ? j - 1 : j);
+          if (jn != j) {
+            in = jn >= 0 && jn <= n - 2;
+            if (in) {
+              j = jn;
+              c0 = G[j];
+              c3 = G[3 * nc + j];
+              t = rec_t(x, c0.x, c0.y);
+            }
+          }
+        }
+        if (in && c3.w > 0.f) {
+          const float4 c1 = G[nc + j], c2 = G[2 * nc + j];
+          const float th = t.hi;
+          float S = __fmaf_rn(th, c3.y, c3.x);  // g7 + t g8
+          S = __fmaf_rn(th, S, c2.w);
+          S = __fmaf_rn(th, S, c2.z);
+          S = __fmaf_rn(th, S, c2.y);
+          S = __fmaf_rn(th, S, c2.x);  // g3 + t (g4 + ...)
+          // P = g2 + t S, normalised (so are Q and the result: the unnormalised products
+          // downstream drop lo x lo)
+          const df P = fast_two_sum(c1.z, __fmaf_rn(th, S, c1.w));
+          const df tp = two_prod(th, P.hi);  // Q = g1 + t P
+          const df q = two_sum(c1.x, tp.hi);
+          const float ql =
+              __fadd_rn(q.lo, __fadd_rn(c1.y, __fadd_rn(tp.lo, __fmaf_rn(th, P.lo, __fmul_rn(t.lo, P.hi)))));
+          const df tq = two_prod(th, q.hi);  // g0 + t Q
+          const df s = two_sum(c0.z, tq.hi);
+          return df{s.hi, __fadd_rn(s.lo, __fadd_rn(c0.w, __fadd_rn(tq.lo, __fmaf_rn(th, ql, __fmul_rn(t.lo, q.hi)))))};
+        }
+      }
+      int j, jt;
+      float4 r;
+      df t;
+      const float f = rec_cell_frac<DEG>(a, TBg, x, j, r, jt, t);
+      const df R = jt >= 0 ? reg_R_cell<false>(rqg, jt, t) : reg_R_df(x);
+      return df_prop(rec_lerp_u(r, TBg.dlo[j], f), x, R);
     }
     // part / nsplit: this call sums the phi nodes l = part, part + nsplit, ... of the row
     __device__ __forceinline__ double row_s3r(const RunParams &P, const ItemDev &it, int row, int part, int nsplit,
@@ -833,9 +894,10 @@ namespace gbint
       const df third = dfc(1.0 / 3.0);
       const df sbd = df_mul(q2pp, third);
       const AxisDev aB = sT[1].a0, aC = sT[2].a0, aD = sT[3].a0;
-      const RecTab TB = rec_tab(tab, toff[1], sT[1].n0 - 1), TC = rec_tab(tab, toff[2], sT[2].n0 - 1),
-                   TD = rec_tab(tab, toff[3], sT[3].n0 - 1);
-      const float4 *rqB = reinterpret_cast<const float4 *>(tab + toff[0]);
+      const float4 *GB = reinterpret_cast<const float4 *>(tab + toff[1]);
+      const RecTab TC = rec_tab(tab, toff[2], sT[2].n0 - 1), TD = rec_tab(tab, toff[3], sT[3].n0 - 1);
+      const RecTab TBg = rec_tab(sT[1].data, sT[1].cr_off, sT[1].n0 - 1);
+      const float4 *rqB = reinterpret_cast<const float4 *>(sT[1].data + sT[1].rq_off);
       const int nf = it.ax[2].n;
       // the phi rule is symmetric and the integrand reads phi through cos(phi) only (see row_s3)
       const int nh = (nf + 1) >> 1;
@@ -848,7 +910,8 @@ namespace gbint
           const df r2 = df_max(lin_dd(A, B, r.a_hi, r.a_lo), 1e-30f);
           const df t2 = df_max(df_add(df_scale2(r2, 0.5f), Ct), 1e-30f);
           const df sv = df_add(sbd, df_mul(r2, third));
-          const df g = df_mul_u(df_mul_u(G1_rec<DEG>(TB, rqB, aB, r2), V1_rec<DEG>(TC, aC, sv)), V1_rec<DEG>(TD, aD, t2));
+          const df g =
+              df_mul_u(df_mul_u(G1_grec<DEG>(GB, sT[1], TBg, rqB, r2), V1_rec<DEG>(TC, aC, sv)), V1_rec<DEG>(TD, aD, t2));
           k.add_prod(df_scale2(rec_w(r), 2 * l + 1 == nf ? 1.f : 2.f), g);
         }
         return k.value();
@@ -1120,15 +1183,15 @@ namespace gbint
             s_toff[t] = total / 4;
             if constexpr (KIND != K_S5Z && KIND != K_S3R) total += kRcOnly ? rc_bytes(sT[t]) : sT[t].bytes;
           }
-          // S3R: B's regulator coefficients, then the records of B, C, D (table A feeds the
-          // hoisted row factors only)
+          // S3R: B's propagator records, then the value records of C and D (table A feeds the
+          // hoisted row factors only; B's value records and regulator stay in global memory)
           if constexpr (KIND == K_S3R) {
-            bool has = sT[1].rq_off > 0;
-            total = s3r_rq_bytes(sT[1]);
+            bool has = sT[1].gr_off > 0;
+            total = 0;
             for (int t = 1; t < 4; ++t) {
               has = has && sT[t].cr_off > 0 && sT[t].n1 == 0;
               s_toff[t] = total / 4;
-              total += s3r_rec_bytes(sT[t]);
+              total += t == 1 ? s3r_g_bytes(sT[t]) : s3r_rec_bytes(sT[t]);
             }
             if (!has) total = tab_bytes_cap + 1;  // refused below: nothing is staged or evaluated
           }
@@ -1145,8 +1208,8 @@ namespace gbint
             if constexpr (KIND == K_S5Z) {
               tma_bulk_g2s(tab_s, sT[0].data + sT[0].rc_off, (uint32_t)total, &bar[2]);
             } else if constexpr (KIND == K_S3R) {
-              tma_bulk_g2s(tab_s, sT[1].data + sT[1].rq_off, (uint32_t)s3r_rq_bytes(sT[1]), &bar[2]);
-              for (int t = 1; t < 4; ++t)
+              tma_bulk_g2s(tab_s, sT[1].data + sT[1].gr_off, (uint32_t)s3r_g_bytes(sT[1]), &bar[2]);
+              for (int t = 2; t < 4; ++t)
                 tma_bulk_g2s(tab_s + s_toff[t], sT[t].data + sT[t].cr_off, (uint32_t)s3r_rec_bytes(sT[t]), &bar[2]);
             } else {
               for (int t = 0; t < NT; ++t) {
@@ -1233,7 +1296,8 @@ namespace gbint
   int kind_default_threads(int kind) { return kind_default_schedule(kind).threads; }
 
   // defaults measured on GB300 (the autotuner's landscapes on the benchmark workloads): S5Z runs
-  // 23 % faster at 256 threads with its c2 loop split over two threads than at 512 unsplit
+  // 23 % faster at 256 threads with its c2 loop split over two threads than at 512 unsplit; S3R
+  // 5 % faster at 256 threads (80 registers, 3 CTAs per SM) than at 128 (96, 5 CTAs)
   gb_schedule kind_default_schedule(int kind)
   {
     switch (kind_base(kind)) {
@@ -1244,7 +1308,7 @@ namespace gbint
     case K_S5Z:
       return gb_schedule{256, 1, 2, GB_ORDER_ITEM};
     case K_S3R:
-      return gb_schedule{128, 2, 1, GB_ORDER_ITEM};
+      return gb_schedule{256, 2, 1, GB_ORDER_ITEM};
     default:
       return gb_schedule{256, 1, 1, GB_ORDER_ITEM};
     }

@@ -228,23 +228,73 @@ namespace gbint
     return cudaGetLastError();
   }
 
-  // per-cell records of a 1D table: {1/c_j hi, lo, y_j, hi(d_j)} and lo(d_j), d_j = y_{j+1} - y_j
-  // split exactly into two floats
-  __global__ void k_cell_records(float *table, int rc_off, int cr_off, int cells)
+  // Per-cell records of a 1D log table, one thread a cell.  Value record: {1/c_j hi, lo, y_j,
+  // hi(d_j)} and lo(d_j), d_j = y_{j+1} - y_j split exactly into two floats.  Within cell j the
+  // table value is linear in the log index, so in t = x / c_j - 1 (c_j the cell centre) it is
+  // Z = z0 + z1 ln(1 + t), z0 = (y_j + y_{j+1}) / 2, z1 = d_j kln.  Propagator record (with the
+  // regulator's FP64 coefficients a_k of R(c_j (1 + t))), in FP64: the Taylor series of 1 / D,
+  // D = c_j (1 + t) Z + R, from D's coefficients d_k = c_j (w_k + w_{k-1}) + a_k (w_k those of Z,
+  // w_0 = z0, w_k = (-1)^(k+1) z1 / k) by the recursion
+  // g_0 = 1 / d_0, g_k = -g_0 sum_{i=1..k} d_i g_{k-i}, in four float4 arrays of a float4 per
+  // cell: {1/c_j hi, lo, g0 hi, lo}, {g1 hi, lo, g2 hi, lo}, {g3, g4, g5, g6}, {g7, g8, el, +-eh}.  (el, eh): the cell's edges in t,
+  // 2^(-+1/(2 scale)) - 1, moved inwards by 4e-7 (more than the FP32 error of the kernels' t):
+  // a t outside them sends the kernel to an exact decision of the cell.  eh is negative where the
+  // series is not trusted over the cell (its tail, estimated from the ratio of the last two
+  // coefficients, above 1e-12 of g_0); the kernels evaluate such cells from the value record and
+  // the regulator.
+  __global__ void k_cell_records(float *table, const int rc_off, const int cr_off, const int gr_off,
+                                 const int rd_off, const int cells, const double scale, const double shift)
   {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= cells) return;
     const float y0 = table[j], y1 = table[j + 1];
-    const dev::df d = dev::two_sum(y1, -y0);
+    const double d = (double)y1 - (double)y0;  // exact
+    const double kln = scale / 0.69314718055994530942;
+    const double z0 = (double)y0 + 0.5 * d, z1 = d * kln;
+    const double hl = 0.34657359027997265471 / scale;  // ln 2 / (2 scale): half a cell in ln x
+    const float el = __fadd_rn((float)expm1(-hl), 4e-7f), eh = __fsub_rn((float)expm1(hl), 4e-7f);
     const float2 r = reinterpret_cast<const float2 *>(table + rc_off)[j];
-    reinterpret_cast<float4 *>(table + cr_off)[j] = make_float4(r.x, r.y, y0, d.hi);
-    table[cr_off + 4 * cells + j] = d.lo;
+    const dev::df dd = dev::two_sum(y1, -y0);
+    reinterpret_cast<float4 *>(table + cr_off)[j] = make_float4(r.x, r.y, y0, dd.hi);
+    table[cr_off + 4 * cells + j] = dd.lo;
+    if (!gr_off) return;
+    const double *a = reinterpret_cast<const double *>(table + rd_off) + 10 * j;
+    const double c = exp2(((double)j + 0.5 - shift) / scale);
+    constexpr int K = 9;  // coefficients g0..g8
+    double w[K], D[K], g[K];
+    w[0] = z0;
+    for (int k = 1; k < K; ++k) w[k] = z1 * ((k & 1) ? 1.0 : -1.0) / k;
+    D[0] = c * w[0] + a[0];
+    for (int k = 1; k < K; ++k) D[k] = c * (w[k] + w[k - 1]) + a[k];
+    g[0] = 1.0 / D[0];
+    for (int k = 1; k < K; ++k) {
+      double s = 0.0;
+      for (int i = 1; i <= k; ++i) s += D[i] * g[k - i];
+      g[k] = -s * g[0];
+    }
+    // the cell spans |t| <= 2^(1/(2 scale)) - 1
+    const double h = expm1(hl);
+    const double rt = g[K - 2] != 0.0 ? fabs(g[K - 1] / g[K - 2]) * h : 1.0;
+    double hk = h;
+    for (int k = 1; k < K - 1; ++k) hk *= h;
+    bool ok = D[0] > 0.0 && rt < 0.5 && fabs(g[K - 1]) * hk * rt / (1.0 - rt) <= 1e-12 * fabs(g[0]);
+    for (int k = 0; k < K; ++k) ok = ok && isfinite(g[k]);
+    const dev::df G0 = dev::df_from(g[0]), G1 = dev::df_from(g[1]), G2 = dev::df_from(g[2]);
+    // four float4 arrays of `cells` entries (a lookup's 16-byte loads at different cells then
+    // fall on different shared-memory banks)
+    float4 *gr = reinterpret_cast<float4 *>(table + gr_off) + j;
+    gr[0] = make_float4(r.x, r.y, G0.hi, G0.lo);
+    gr[cells] = make_float4(G1.hi, G1.lo, G2.hi, G2.lo);
+    gr[2 * cells] = make_float4((float)g[3], (float)g[4], (float)g[5], (float)g[6]);
+    gr[3 * cells] = make_float4((float)g[7], (float)g[8], el, ok ? eh : -eh);
   }
 
-  cudaError_t launch_cell_records(float *table, int rc_off, int cr_off, int cells, cudaStream_t s)
+  cudaError_t launch_cell_records(float *table, const TableDev &D, cudaStream_t s)
   {
-    if (cells <= 0) return cudaSuccess;
-    k_cell_records<<<(cells + 127) / 128, 128, 0, s>>>(table, rc_off, cr_off, cells);
+    const int cells = D.n0 - 1;
+    if (cells <= 0 || !D.cr_off) return cudaSuccess;
+    k_cell_records<<<(cells + 127) / 128, 128, 0, s>>>(table, D.rc_off, D.cr_off, D.gr_off, D.rd_off, cells,
+                                                        D.a0.scale64, D.a0.shift64);
     return cudaGetLastError();
   }
 

@@ -502,6 +502,27 @@ def test_table_update_rebuilds_cell_records(ctx, oracle, W, many):
         t.close()
 
 
+def test_untrusted_propagator_series_cells(ctx, oracle, W):
+    """C3's kernel reads B's propagator 1 / (Z(x) x + R(x)) from a per-cell series in t = x / c_j - 1;
+    where the series is not trusted over a cell (a table whose value jumps 60 % from cell to cell
+    puts the series' radius next to the cell), the kernel evaluates the cell from the value record
+    and the regulator instead.  A B table alternating between 0.4 and 1.0 (most cells untrusted)
+    and one with a single such jump both match the oracle."""
+    w = subset(W, "C3")
+    spec, zb = w["tables"][1]
+    alt = np.where(np.arange(zb.size) % 2 == 0, 0.4, 1.0).astype(np.float32)
+    jump = zb.copy()
+    jump[120:] *= 0.4
+    for zb2 in (alt, jump):
+        w2 = dict(w)
+        w2["tables"] = list(w["tables"])
+        w2["tables"][1] = (spec, zb2)
+        got = run_engine(ctx, W, w2, "fp32c")
+        ref = W.oracle_values(w2, oracle)
+        assert np.all(np.isfinite(got))
+        assert np.max(rel(got, ref)) <= TOL32["C3"]
+
+
 def test_errors_are_status_codes(ctx, W):
     from diffrg_gb300 import GbError
     from diffrg_gb300.engine import Context, integral
