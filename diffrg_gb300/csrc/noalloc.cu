@@ -32,7 +32,10 @@
 // is part of the first call's set-up: make the first call on each device before any CUDA stream
 // capture begins.  New quadrature orders and axes fill host-side caches and
 // are copied into the context's node pool, which was allocated once at gb_ctx_create; no device
-// or pinned memory is allocated by this entry point.
+// or pinned memory is allocated by this entry point.  The call runs eagerly and waits for the
+// context's stream (it is not recorded into a graph being captured elsewhere); under CUDA's
+// capture rules that wait is an unsafe call, so a global- or thread-local-mode capture open at
+// the time is invalidated (tests/test_zz_no_alloc.py runs it under a relaxed-mode capture).
 #include <cstddef>
 #include <mutex>
 

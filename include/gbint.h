@@ -229,8 +229,15 @@ int gb_get(gb_ctx *ctx, const gb_integral *item, gb_table *const *tables, int n_
  * that device current) -- make it before any CUDA stream capture begins.  All calls on a device
  * share the array, which keeps the last call's contents (the counters are cleared before each
  * launch): calls through one context serialise, calls from two contexts whose work overlaps on
- * the GPU race.  The call runs on the context's stream and returns with the result in *out;
- * results equal gb_get(..., GB_PREC_FP64, ...). */
+ * the GPU race.  The call runs at once on the context's stream and waits for it, returning with
+ * the result in *out; a CUDA graph being captured on another stream does not record it (a replay
+ * does not evaluate the integral again).  Waiting on a stream is a potentially unsafe call in
+ * CUDA's stream-capture rules: made while this thread captures in global or thread-local mode,
+ * or while any thread captures in global mode, it invalidates that capture (CUDA's error
+ * cudaErrorStreamCaptureInvalidated at the capture's end).  Call it outside such captures, or
+ * capture in relaxed mode.  A quadrature axis seen for the first time is uploaded into the node
+ * pool on the context's stream (from pageable host memory: use each axis once before a capture
+ * begins).  Results equal gb_get(..., GB_PREC_FP64, ...). */
 #define GB_NOALLOC_MAX_POINTS 4194304
 #define GB_NOALLOC_SCRATCH_BYTES 36864
 int gb_get_noalloc(gb_ctx *ctx, const gb_integral *item, gb_table *const *tables, int n_tables, double *out);

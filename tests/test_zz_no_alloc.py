@@ -7,7 +7,9 @@ device-wide wait of cudaFree.  Its scratch is a fixed device array inside the li
 call finds the previous call's contents there: the tests call it twice in a row per integral
 and compare both results with gb_get (the allocating entry point) through the C ABI, and the
 polynomial cases also with the FP64 oracle.  A third test checks that a run of calls with new
-RG scales and new quadrature orders leaves the device's free memory unchanged.
+RG scales and new quadrature orders leaves the device's free memory unchanged, a fourth that a
+call made while another stream captures a CUDA graph (relaxed mode) runs eagerly and leaves the
+capture valid.
 
 This file is named to be collected last, so that a failure here cannot hide other tests.
 """
@@ -115,6 +117,43 @@ def test_noalloc_leaves_free_device_memory_unchanged():
         for nn, kk, v in got:  # gb_get allocates, so it runs after the window
             ref = ctx.get(_engine_integral(fam, nn, d, kk, xe, args, kw), (), "fp64")
             assert abs(v - ref) <= TOL64 * abs(ref)
+    finally:
+        ctx.close()
+
+
+def test_noalloc_runs_eagerly_while_a_relaxed_capture_is_open():
+    """A call made while this thread records a CUDA graph on another stream in relaxed capture
+    mode (the integral's axes used once before) runs at once on the context's stream and is not
+    recorded: it returns the same value as before the capture, the capture stays valid, and its
+    replays run only the captured work.  (In global or thread-local mode the call's stream wait
+    is a prohibited call and invalidates the capture -- the header says so.)"""
+    import torch
+
+    from diffrg_gb300.engine import Context
+
+    rng = np.random.default_rng(9)
+    ctx = Context(0)
+    try:
+        fam, n, d, k, xe, args, kw = _poly_cases(rng)[0]
+        g = _engine_integral(fam, n, d, k, xe, args, kw)
+        rc, before = _get_noalloc(ctx, g)
+        assert rc == 0, ctx.last_error()
+        x = torch.zeros(4, device="cuda")
+        graph = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            graph.capture_begin(capture_error_mode="relaxed")
+            x.add_(1.0)
+            rc, during = _get_noalloc(ctx, g)
+            graph.capture_end()
+        torch.cuda.current_stream().wait_stream(s)
+        assert rc == 0, ctx.last_error()
+        assert during == before
+        graph.replay()
+        graph.replay()
+        torch.cuda.synchronize()
+        assert x.tolist() == [2.0] * 4
     finally:
         ctx.close()
 
