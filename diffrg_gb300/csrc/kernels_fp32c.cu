@@ -769,7 +769,7 @@ namespace gbint
         r = T.rec[n - 2];
         return 1.f;
       }
-      j = min(max((int)floorf(ua), 0), n - 2);
+      j = min((int)ua, n - 2);  // ua >= -0.01 here: truncation gives the cell (NaN converts to 0)
       jt = j;
       r = T.rec[j];
       float f = cell_frac_rr<false, DEG>(a, df{r.x, r.y}, x, &t);
