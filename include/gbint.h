@@ -352,8 +352,8 @@ int gb_graph_destroy(gb_ctx *ctx, gb_graph *g);
  * gb_get_stats: counts, busy time, p50/p99/max latency (submit -> result ready, nearest rank)
  *   since gb_serve_start / gb_reset_stats, and the budget in use. */
 int gb_serve_start(gb_ctx *ctx, int max_inflight_batches, int max_batch_items);
-/* The device-resident request loop, the other serving mode (north star "serving": a loop on the
- * GPU that takes request() calls as they arrive; replaces the same fan-out as gb_serve_start).
+/* The device-resident request loop, the other serving mode (a loop on the GPU that takes
+ * request() calls as they arrive; replaces the same fan-out as gb_serve_start).
  * gb_submit then writes each request straight into a ring the GPU reads (descriptors and a
  * snapshot of its tables' directory entries in the request's ring slot, then the published
  * work-unit count in mapped host memory); a persistent kernel claims published units of 1024

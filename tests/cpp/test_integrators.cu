@@ -4,7 +4,7 @@
 // each family integrates a product of polynomials (a rational function in q0 for the finite-T
 // q0 families).  Cases come on stdin, one per line:
 //   family d n0 n1 n2 n3 x_extent x0_extent x0_summands T k prec a0 .. a23
-// (prec 0 = NT double, 1 = NT float; family numbers as GB_FAM_* in gbint.h); the driver prints
+// (prec 0 = NT double, 1 = NT float; family numbers as GB_FAM_* in gbint.h); this program prints
 // one value per case with 17 significant digits.  tests/test_gpu_cpp_api.py compares them with
 // the FP64 oracle and with the closed forms.
 #include <cstdio>
