@@ -45,6 +45,20 @@ namespace gbint
       const float corr = __fadd_rn(__fadd_rn(s.lo, A.lo), __fmaf_rn(B.hi, c_lo, __fmaf_rn(B.lo, c_hi, p.lo)));
       return fast_two_sum(s.hi, corr);
     }
+    // lin_dd without the final renormalisation: the low word stays a few ulp of the high one,
+    // which every consumer that takes both words (products, sums, t = x / c - 1) accepts
+    __device__ __forceinline__ df lin_du(df A, df B, float c_hi, float c_lo)
+    {
+      const df p = two_prod(B.hi, c_hi);
+      const df s = two_sum(A.hi, p.hi);
+      return df{s.hi, __fadd_rn(__fadd_rn(s.lo, A.lo), __fmaf_rn(B.hi, c_lo, __fmaf_rn(B.lo, c_hi, p.lo)))};
+    }
+    // a + b, the high parts summed exactly and the rest left in the low word (unnormalised)
+    __device__ __forceinline__ df df_add_u(df a, df b)
+    {
+      const df s = two_sum(a.hi, b.hi);
+      return df{s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo))};
+    }
     __device__ __forceinline__ df df_neg(df a) { return df{-a.hi, -a.lo}; }
     __device__ __forceinline__ df df_scale2(df a, float s) { return df{a.hi * s, a.lo * s}; }  // s a power of 2
     __device__ __forceinline__ df dfc(double v) { return df_from(v); }
@@ -907,9 +921,10 @@ namespace gbint
 #pragma unroll 1
         for (int l = part; l < nh; l += nsplit) {
           const NodeRec r = rc[l];  // a = cos(phi), w = 2 pi w_phi
-          const df r2 = df_max(lin_dd(A, B, r.a_hi, r.a_lo), 1e-30f);
-          const df t2 = df_max(df_add(df_scale2(r2, 0.5f), Ct), 1e-30f);
-          const df sv = df_add(sbd, df_mul(r2, third));
+          // r2, t2 and s unnormalised (their lookups take both words)
+          const df r2 = df_max(lin_du(A, B, r.a_hi, r.a_lo), 1e-30f);
+          const df t2 = df_max(df_add_u(df_scale2(r2, 0.5f), Ct), 1e-30f);
+          const df sv = df_add_u(sbd, df_mul_u(r2, third));
           const df g =
               df_mul_u(df_mul_u(G1_grec<DEG>(GB, sT[1], TBg, rqB, r2), V1_rec<DEG>(TC, aC, sv)), V1_rec<DEG>(TD, aD, t2));
           k.add_prod(df_scale2(rec_w(r), 2 * l + 1 == nf ? 1.f : 2.f), g);
