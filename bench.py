@@ -51,11 +51,11 @@ PER_POINT = {"C1": (12, 4), "C2": (18, 4), "C3": (30, 6), "C5": (25, 4)}
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant kernel, from one ncu
 # capture of that kernel (summaries under profiles/, named for kernel and workload); a changed
 # kernel needs a new capture -- the JSON line carries these as "traffic" with their source
-TRAFFIC_BYTES_PER_LAUNCH = {"C2": 1497600, "C3": 6239488, "C5": 799232}
+TRAFFIC_BYTES_PER_LAUNCH = {"C2": 1497600, "C3": 6239488, "C5": 819456}
 # thread instructions executed per integrand point by the dominant kernel (smsp__inst_executed.sum
 # x 32 / points, same captures): with the measured step time they give the issue rate, the
 # bound this double-float code actually meets (one warp instruction per SM sub-partition and cycle)
-INSTR_PER_POINT = {"C2": 47, "C3": 150.5, "C5": 114}
+INSTR_PER_POINT = {"C2": 47, "C3": 150.5, "C5": 111}
 CAPTURE_NOTE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,smsp__inst_executed.sum capture of the "
                 "dominant kernel on this workload (profiles/)")
 

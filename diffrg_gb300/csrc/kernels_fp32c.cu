@@ -1086,7 +1086,7 @@ namespace gbint
 #pragma unroll 1
         for (int m = 0; m < nh3; ++m) {
           const NodeRec rp = rphi[m];
-          const df x = df_max(lin_dd(A2, Bs, rp.a_hi, rp.a_lo), 1e-30f);
+          const df x = df_max(lin_du(A2, Bs, rp.a_hi, rp.a_lo), 1e-30f);  // unnormalised: see lin_du
           int ix, jx;
           df tx;
           const float fx = frac0(x, ix, jx, tx);
