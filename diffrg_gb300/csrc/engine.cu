@@ -520,6 +520,7 @@ namespace gbint
   {
     if (!b) return;
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->h_err) cudaFreeHost(b->h_err);
     if (!b->arena) {
       cudaFree(b->d_items);
       cudaFree(b->d_units);
@@ -1823,10 +1824,13 @@ int gb_batch_results(gb_ctx *ctx, gb_batch *b, double *host_out, void *stream)
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   if (capturing(s)) return set_error(ctx, GB_EINVAL, "gb_batch_results cannot be captured in a graph");
   GB_CUDA(cudaSetDevice(ctx->device));
+  // the results and the error word come back on the caller's stream behind the batch's kernels,
+  // with one synchronisation (the error word lands in the batch's pinned word, allocated once)
+  if (!b->h_err) GB_CUDA(cudaMallocHost(&b->h_err, sizeof(int)));
   GB_CUDA(cudaMemcpyAsync(host_out, b->d_out, b->n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaMemcpyAsync(b->h_err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
-  int err = 0;
-  GB_CUDA(cudaMemcpy(&err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  const int err = *b->h_err;
   if (err) {
     cudaMemset(ctx->d_err, 0, sizeof(int));
     return set_error(ctx, GB_EDEVICE, "kernel reported error flags " + std::to_string(err));

@@ -117,6 +117,7 @@ struct gb_batch {
   int *d_item_count = nullptr;
   int *d_counters = nullptr;  // one per kind run
   double *d_out = nullptr;
+  int *h_err = nullptr;  // pinned landing place of the context's error word (gb_batch_results)
   size_t bytes = 0;
   // graph replay
   cudaGraphExec_t graph = nullptr;
